@@ -1,0 +1,78 @@
+"""ctypes binding of libbsfh.so (the C ABI declared in include/bsfh.h).
+
+The library must exist (build it with bs45_quantum_explorer_gb300.build.build_library());
+loading fails loudly otherwise. There is no CPU fallback.
+"""
+import ctypes as C
+import os
+
+from .build import LIB
+
+BS_OK = 0
+ERRORS = {
+    -1: "bad argument", -2: "CUDA runtime error", -3: "out of memory",
+    -4: "device wait limit reached", -5: "internal consistency check failed",
+    -6: "output capacity exceeded", -7: "no sm_103 CUDA device",
+}
+
+HALL_FP64, HALL_TC_FP16, HALL_TC_BF16X2 = 0, 1, 2
+
+
+class BsError(RuntimeError):
+    def __init__(self, code, what=""):
+        super().__init__(f"{what}: {ERRORS.get(code, 'error')} ({code})")
+        self.code = code
+
+
+class HallStats(C.Structure):
+    _fields_ = [("pairs", C.c_longlong), ("passed", C.c_longlong), ("rechecked", C.c_longlong),
+                ("pass_below", C.c_double), ("reject_above", C.c_double),
+                ("quant_err", C.c_double), ("mode", C.c_int)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+_lib = None
+
+# (name, restype, argtypes) for every entry point of include/bsfh.h
+SIGNATURES = {
+    "bs_version": (C.c_int, []),
+    "bs_strerror": (C.c_char_p, [C.c_int]),
+    "bs_ctx_create": (C.c_int, [C.c_int] * 6 + [C.POINTER(C.c_void_p)]),
+    "bs_ctx_destroy": (None, [C.c_void_p]),
+    "bs_ctx_set_stream": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "bs_ctx_device_status": (C.c_int, [C.c_void_p]),
+    "bs_hall_filter_batch": (C.c_int, [C.c_void_p, C.c_void_p, C.c_longlong, C.c_int, C.c_void_p,
+                                       C.POINTER(HallStats)]),
+    "bs_hall_filter_packed": (C.c_int, [C.c_void_p, C.c_void_p, C.c_longlong, C.c_int, C.c_void_p,
+                                        C.POINTER(HallStats)]),
+    "bs_hall_filter_dev": (C.c_int, [C.c_void_p, C.c_void_p, C.c_longlong, C.c_int, C.c_void_p,
+                                     C.POINTER(HallStats)]),
+    "bs_hall_tc_dump_dev": (C.c_int, [C.c_void_p, C.c_void_p, C.c_longlong, C.c_int, C.c_void_p]),
+    "bs_pack_rows": (C.c_int, [C.c_void_p, C.c_longlong, C.c_int, C.c_void_p]),
+    "bs_gen_hall_pairs_dev": (C.c_int, [C.c_void_p, C.c_longlong, C.c_uint64, C.c_void_p]),
+    "bs_ctx_timing": (C.c_int, [C.c_void_p, C.c_int]),
+    "bs_ctx_timing_read": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_longlong),
+                                     C.POINTER(C.c_longlong)]),
+}
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB):
+            raise RuntimeError(f"{LIB} is missing: build it first (bs45_quantum_explorer_gb300.build)")
+        L = C.CDLL(LIB)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def check(code, what):
+    if code != BS_OK:
+        raise BsError(code, what)
+    return code

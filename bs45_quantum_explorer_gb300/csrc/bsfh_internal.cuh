@@ -1,0 +1,70 @@
+// bsfh_internal.cuh - shared definitions of the GB300 first-hit library (not part of the ABI).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cstddef>
+
+#include "../../include/bsfh.h"
+
+#define BS_MAXL 64          // longest sequence held in one packed word
+#define BS_TC_COLS 208      // tensor-core N: 104 Re columns + 104 Im columns
+#define BS_TC_IM0 104       // first Im column
+#define BS_TC_NANG 101      // unique Hall angles (j = 1..100 and 200)
+
+// One tensor-core table image: 208 rows (columns of the DFT) x 64 halves, stored in the
+// 128-byte-swizzled K-major layout the UMMA shared-memory descriptor reads.
+#define BS_TC_PART_BYTES (BS_TC_COLS * 128)
+
+struct bs_hall_tc_form {
+  int nparts;            // 1 (fp16) or 2 (bf16 hi + lo)
+  int fmt;               // UMMA operand format: 0 = f16, 1 = bf16
+  double quant_err;      // per-sequence bound e on |Re - Re_q|, |Im - Im_q|
+  float pass_below;      // certified thresholds on the fp32 max pair PSD
+  float reject_above;
+  uint8_t *d_image;      // nparts * BS_TC_PART_BYTES
+};
+
+struct bs_ctx {
+  int n, n1, sig[4], device;
+  int num_sms;
+  cudaStream_t own_stream, stream;
+  double *d_cos, *d_sin;     // FP64 Hall tables, [200][BS_MAXL] for j = 1..200
+  double lim;                // 4n + 2 + 0.5
+  bs_hall_tc_form tc[3];     // index by mode (0 unused)
+  int *d_status;             // device-side error word
+  unsigned long long *d_count;  // [0] uncertain count, [1] pass count, [2] overflow flag
+  // scratch for the host-buffer entry points
+  uint64_t *d_bits; long long bits_cap;   // pairs
+  uint8_t *d_pass; long long pass_cap;
+  int8_t *d_rows; long long rows_cap;     // int8 staging for packing
+  unsigned *d_unc; long long unc_cap;     // uncertain pair indices
+  void *h_pinned; size_t pinned_bytes;
+  // kernel timing (bs_ctx_timing): start/stop events around the timed kernel class
+  int timing;
+  int nev;                  // event pairs recorded since the last read
+  cudaEvent_t ev[2 * 512];
+  double timed_ms;          // accumulated duration of the timed kernels
+  long long timed_launches; // launches of the timed kernels
+  long long launches;       // every kernel this context has launched
+};
+
+// Record the start / stop event of one timed kernel launch on the context stream.
+void bs_timed_begin(bs_ctx *ctx);
+void bs_timed_end(bs_ctx *ctx);
+
+// Internal helpers implemented in capi.cu
+int bs_cuda_fail(cudaError_t e);
+int bs_ensure_dev(void **ptr, long long *cap, long long need, size_t elem);
+int bs_ensure_pinned(bs_ctx *ctx, size_t bytes);
+
+// Device wait limit: a spin or try_wait loop gives up after this many SM clock cycles,
+// records BS_ERR_TIMEOUT in the context's status word and returns.
+#define BS_WAIT_CYCLES (4000000000ULL)
+
+static inline int bs_grid_for(long long work, int block, int max_blocks) {
+  long long g = (work + block - 1) / block;
+  if (g < 1) g = 1;
+  if (g > max_blocks) g = max_blocks;
+  return (int)g;
+}

@@ -1,0 +1,609 @@
+// hall.cu - Theorem 2.4 spectral filter (the reference's hall_ok_pair_fast,
+// src/solver/wz_match.cpp:143-168) over batches of packed (C,D) pairs.
+//
+// Two device forms:
+//   * FP64, CUDA cores: the reference's summation order and expressions, one rounding per
+//     operation (no FMA contraction), early exit at the first failing angle. Exact.
+//   * tcgen05 tensor cores: every sequence's DFT at the 101 unique angles is one row of a
+//     [128 x K] x [K x 208] UMMA with +-1 operands and a quantised table, accumulated exactly
+//     in FP32 in TMEM. A certified margin decides almost every pair; the few pairs inside the
+//     margin band are rechecked by the FP64 form. Decisions equal the FP64 form's.
+#include <stdint.h>
+
+#include "bsfh_internal.cuh"
+
+namespace {
+
+#define FULL_MASK 0xffffffffu
+
+// ------------------------------------------------------------------------------------
+// Shared helpers
+// ------------------------------------------------------------------------------------
+__device__ __forceinline__ void set_status(int *status, int code) { atomicCAS(status, 0, code); }
+
+// One sequence's Thm 2.4 terms at angle row jr (j-1) in the reference's order.
+__device__ __forceinline__ void dft64(uint64_t x, int L, const double *c, const double *s,
+                                      double &re, double &im) {
+  double r = 0.0, q = 0.0;
+  for (int i = 0; i < L; i++) {
+    double cv = c[i], sv = s[i];
+    bool plus = (x >> i) & 1ULL;
+    r = __dadd_rn(r, plus ? cv : -cv);
+    q = __dadd_rn(q, plus ? sv : -sv);
+  }
+  re = r;
+  im = q;
+}
+
+// The reference's decision for one pair: at every angle X alone, Y alone, then the pair.
+__device__ __forceinline__ bool hall_pair64(uint64_t x, uint64_t y, int L, double lim,
+                                            const double *tc, const double *ts) {
+  for (int jr = 0; jr < 200; jr++) {
+    const double *c = tc + jr * L, *s = ts + jr * L;
+    double rx, ix;
+    dft64(x, L, c, s, rx, ix);
+    double fx = __dadd_rn(__dmul_rn(rx, rx), __dmul_rn(ix, ix));
+    if (fx > lim) return false;
+    double ry, iy;
+    dft64(y, L, c, s, ry, iy);
+    double ry2 = __dmul_rn(ry, ry), iy2 = __dmul_rn(iy, iy);
+    double fy = __dadd_rn(ry2, iy2);
+    double fp = __dadd_rn(__dadd_rn(fx, ry2), iy2);
+    if (fy > lim || fp > lim) return false;
+  }
+  return true;
+}
+
+// Load the FP64 tables for rows j = 1..200, columns i < L, into shared memory.
+__device__ __forceinline__ void load_tables64(double *sc, double *ss, const double *gc,
+                                              const double *gs, int L) {
+  for (int t = threadIdx.x; t < 200 * L; t += blockDim.x) {
+    int jr = t / L, i = t - jr * L;
+    sc[t] = gc[jr * BS_MAXL + i];
+    ss[t] = gs[jr * BS_MAXL + i];
+  }
+  __syncthreads();
+}
+
+// FP64 form over all pairs, or over an index list (the margin-band recheck; the list length
+// is read from device memory so it can follow the tensor-core kernel without a host sync).
+__global__ void __launch_bounds__(512) hall_fp64_kernel(
+    const uint64_t *__restrict__ bits, long long npairs, const unsigned *__restrict__ list,
+    const unsigned long long *list_len, unsigned long long list_cap, int L, double lim,
+    const double *__restrict__ gc, const double *__restrict__ gs, uint8_t *__restrict__ pass,
+    unsigned long long *pass_count) {
+  extern __shared__ double tabs[];
+  double *sc = tabs, *ss = tabs + 200 * L;
+  load_tables64(sc, ss, gc, gs, L);
+  long long count = npairs;
+  if (list) {
+    unsigned long long n = *list_len;
+    count = (long long)(n < list_cap ? n : list_cap);
+  }
+  unsigned local = 0;
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < count;
+       t += (long long)gridDim.x * blockDim.x) {
+    long long p = list ? (long long)list[t] : t;
+    bool ok = hall_pair64(bits[2 * p], bits[2 * p + 1], L, lim, sc, ss);
+    pass[p] = ok ? 1 : 0;
+    local += ok;
+  }
+  unsigned warp_sum = __reduce_add_sync(FULL_MASK, local);
+  if ((threadIdx.x & 31) == 0 && warp_sum) atomicAdd(pass_count, (unsigned long long)warp_sum);
+}
+
+__global__ void pack_kernel(const int8_t *__restrict__ rows, long long nrows, int L,
+                            uint64_t *__restrict__ words, int *status) {
+  for (long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x; r < nrows;
+       r += (long long)gridDim.x * blockDim.x) {
+    const int8_t *s = rows + r * L;
+    uint64_t w = 0;
+    bool bad = false;
+    for (int i = 0; i < L; i++) {
+      int8_t v = s[i];
+      w |= (uint64_t)(v == 1) << i;
+      bad |= (v != 1 && v != -1);
+    }
+    words[r] = w;
+    if (bad) set_status(status, BS_ERR_ARG);
+  }
+}
+
+// ------------------------------------------------------------------------------------
+// tcgen05 form
+// ------------------------------------------------------------------------------------
+constexpr int TC_STAGES = 4;
+constexpr int TC_THREADS = 192;  // warp 0 producer, warp 1 MMA issuer, warps 2..5 epilogue
+constexpr int A_STAGE_BYTES = 128 * 128;
+constexpr uint32_t TMEM_COLS = 512;  // two accumulators of 208 columns at 0 and 256
+
+struct TcParams {
+  const uint64_t *bits;
+  long long npairs, ntiles;
+  const uint8_t *image;
+  int nparts, ksteps;
+  uint32_t idesc;
+  uint32_t one2;  // two packed +1.0 halves in the operand format
+  float pass_below, reject_above;
+  uint8_t *pass;
+  unsigned *unc;
+  unsigned long long unc_cap;
+  unsigned long long *count;  // [0] uncertain, [1] passes, [2] overflow
+  int *status;
+  float *dump;
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint32_t a, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(a), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint32_t a) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(a) : "memory");
+}
+__device__ __forceinline__ bool mbar_try(uint32_t a, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(a), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Bounded wait: false when the abort flag is raised or the cycle limit passes.
+__device__ __forceinline__ bool mbar_wait(uint32_t a, uint32_t parity, volatile int *abort_flag,
+                                          bool honour_abort = true) {
+  long long t0 = clock64();
+  while (!mbar_try(a, parity)) {
+    if (honour_abort && *abort_flag) return false;
+    if ((unsigned long long)(clock64() - t0) > BS_WAIT_CYCLES) return false;
+  }
+  return true;
+}
+__device__ __forceinline__ void fence_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_alloc(uint32_t slot, uint32_t ncols) {
+  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(slot),
+               "r"(ncols)
+               : "memory");
+  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tc_dealloc(uint32_t taddr, uint32_t ncols) {
+  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols)
+               : "memory");
+}
+__device__ __forceinline__ void tc_mma(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc,
+                                       uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d),
+      "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+__device__ __forceinline__ void tc_commit(uint32_t mbar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar)
+      : "memory");
+}
+
+// Shared-memory matrix descriptor, K-major operand in the 128-byte swizzle layout:
+// start address >> 4, leading offset 1 (unused for this layout), stride offset 1024 B
+// between 8-row groups, descriptor version 1, layout type 2 (128B swizzle).
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
+  uint64_t d = (uint64_t)((saddr >> 4) & 0x3FFFu);
+  d |= (uint64_t)1 << 16;
+  d |= (uint64_t)(1024 >> 4) << 32;
+  d |= (uint64_t)1 << 46;
+  d |= (uint64_t)2 << 61;
+  return d;
+}
+
+// Two 32-column TMEM loads (Re chunk and Im chunk) for this warp's 32 lanes, then wait.
+__device__ __forceinline__ void tmem_ld_2x32(uint32_t ta, uint32_t tb, float *re, float *im) {
+  uint32_t r[64];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%64];\n\t"
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+      "{%32,%33,%34,%35,%36,%37,%38,%39,%40,%41,%42,%43,%44,%45,%46,%47,"
+      "%48,%49,%50,%51,%52,%53,%54,%55,%56,%57,%58,%59,%60,%61,%62,%63}, [%65];\n\t"
+      "tcgen05.wait::ld.sync.aligned;"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
+        "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]),
+        "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]),
+        "=r"(r[31]), "=r"(r[32]), "=r"(r[33]), "=r"(r[34]), "=r"(r[35]), "=r"(r[36]),
+        "=r"(r[37]), "=r"(r[38]), "=r"(r[39]), "=r"(r[40]), "=r"(r[41]), "=r"(r[42]),
+        "=r"(r[43]), "=r"(r[44]), "=r"(r[45]), "=r"(r[46]), "=r"(r[47]), "=r"(r[48]),
+        "=r"(r[49]), "=r"(r[50]), "=r"(r[51]), "=r"(r[52]), "=r"(r[53]), "=r"(r[54]),
+        "=r"(r[55]), "=r"(r[56]), "=r"(r[57]), "=r"(r[58]), "=r"(r[59]), "=r"(r[60]),
+        "=r"(r[61]), "=r"(r[62]), "=r"(r[63])
+      : "r"(ta), "r"(tb)
+      : "memory");
+#pragma unroll
+  for (int k = 0; k < 32; k++) {
+    re[k] = __uint_as_float(r[k]);
+    im[k] = __uint_as_float(r[32 + k]);
+  }
+}
+
+__device__ __forceinline__ void tmem_ld_2x8(uint32_t ta, uint32_t tb, float *re, float *im) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%16];\n\t"
+      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%8,%9,%10,%11,%12,%13,%14,%15}, [%17];\n\t"
+      "tcgen05.wait::ld.sync.aligned;"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
+        "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(ta), "r"(tb)
+      : "memory");
+#pragma unroll
+  for (int k = 0; k < 8; k++) {
+    re[k] = __uint_as_float(r[k]);
+    im[k] = __uint_as_float(r[8 + k]);
+  }
+}
+
+__device__ __forceinline__ float pair_max(const float *re, const float *im, int cnt, float mx) {
+#pragma unroll
+  for (int k = 0; k < 32; k++) {
+    if (k < cnt) {
+      float f = fmaf(re[k], re[k], im[k] * im[k]);
+      float g = __shfl_xor_sync(FULL_MASK, f, 1);
+      mx = fmaxf(mx, f + g);
+    }
+  }
+  return mx;
+}
+
+__global__ void __launch_bounds__(TC_THREADS, 1) hall_tc_kernel(TcParams P) {
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t *base = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  uint8_t *sA = base;
+  uint8_t *sB = sA + TC_STAGES * A_STAGE_BYTES;
+  uint64_t *bars = (uint64_t *)(sB + P.nparts * BS_TC_PART_BYTES);
+  uint32_t *tmem_slot = (uint32_t *)(bars + 2 * TC_STAGES + 4);
+  volatile int *abort_flag = (volatile int *)(tmem_slot + 1);
+  const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + TC_STAGES);
+  const uint32_t tfull0 = smem_u32(bars + 2 * TC_STAGES), tempty0 = tfull0 + 16;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+  {  // table image -> shared memory
+    const uint4 *src = (const uint4 *)P.image;
+    uint4 *dst = (uint4 *)sB;
+    int nvec = P.nparts * BS_TC_PART_BYTES / 16;
+    for (int i = threadIdx.x; i < nvec; i += TC_THREADS) dst[i] = src[i];
+  }
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < TC_STAGES; s++) {
+      mbar_init(full0 + 8 * s, 1);
+      mbar_init(empty0 + 8 * s, 1);
+    }
+    for (int b = 0; b < 2; b++) {
+      mbar_init(tfull0 + 8 * b, 1);
+      mbar_init(tempty0 + 8 * b, 4);
+    }
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) tc_alloc(smem_u32(tmem_slot), TMEM_COLS);
+  fence_async_smem();
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0) {
+    // ---- producer: packed words -> +-1 operand rows in the swizzled layout ----
+    int it = 0;
+    for (long long tile = blockIdx.x; tile < P.ntiles; tile += gridDim.x, it++) {
+      int s = it % TC_STAGES;
+      uint32_t par = ((it / TC_STAGES) & 1) ^ 1;
+      if (!mbar_wait(empty0 + 8 * s, par, abort_flag)) {
+        if (!*abort_flag) { set_status(P.status, BS_ERR_TIMEOUT); *abort_flag = 1; }
+        break;
+      }
+      uint8_t *A = sA + s * A_STAGE_BYTES;
+#pragma unroll
+      for (int rr = 0; rr < 4; rr++) {
+        int r = lane + 32 * rr;
+        long long row = tile * 128 + r;
+        uint64_t w = (row < 2 * P.npairs) ? __ldg(P.bits + row) : 0ULL;
+        for (int c = 0; c < 2 * P.ksteps; c++) {
+          uint32_t nb = ~(uint32_t)(w >> (8 * c));
+          uint4 v;
+          v.x = P.one2 | ((nb & 1u) << 15) | ((nb & 2u) << 30);
+          v.y = P.one2 | ((nb & 4u) << 13) | ((nb & 8u) << 28);
+          v.z = P.one2 | ((nb & 16u) << 11) | ((nb & 32u) << 26);
+          v.w = P.one2 | ((nb & 64u) << 9) | ((nb & 128u) << 24);
+          *(uint4 *)(A + r * 128 + ((c ^ (r & 7)) << 4)) = v;
+        }
+      }
+      fence_async_smem();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(full0 + 8 * s);
+    }
+  } else if (warp == 1) {
+    // ---- MMA issuer (one thread) ----
+    if (lane == 0) {
+      const uint32_t a_base = smem_u32(sA), b_base = smem_u32(sB);
+      int it = 0, last = -1;
+      for (long long tile = blockIdx.x; tile < P.ntiles; tile += gridDim.x, it++) {
+        int s = it % TC_STAGES, b = it & 1;
+        if (!mbar_wait(tempty0 + 8 * b, ((it >> 1) & 1) ^ 1, abort_flag) ||
+            !mbar_wait(full0 + 8 * s, (it / TC_STAGES) & 1, abort_flag)) {
+          if (!*abort_flag) { set_status(P.status, BS_ERR_TIMEOUT); *abort_flag = 1; }
+          break;
+        }
+        tc_fence_after();
+        uint32_t d = tmem + (uint32_t)(b * 256);
+        uint32_t acc = 0;
+        for (int p = 0; p < P.nparts; p++)
+          for (int k = 0; k < P.ksteps; k++) {
+            uint64_t ad = sw128_desc(a_base + s * A_STAGE_BYTES + k * 32);
+            uint64_t bd = sw128_desc(b_base + p * BS_TC_PART_BYTES + k * 32);
+            tc_mma(d, ad, bd, P.idesc, acc);
+            acc = 1;
+          }
+        tc_commit(empty0 + 8 * s);
+        tc_commit(tfull0 + 8 * b);
+        last = it;
+      }
+      // Before TMEM is released, the last issued MMAs must have finished.
+      if (last >= 0) mbar_wait(tfull0 + 8 * (last & 1), (last >> 1) & 1, abort_flag, false);
+    }
+    __syncwarp();
+  } else {
+    // ---- epilogue: TMEM -> max pair PSD -> decision ----
+    const int q = warp & 3;
+    const uint32_t lane_off = (uint32_t)(q * 32) << 16;
+    const int row = q * 32 + lane;
+    int it = 0;
+    for (long long tile = blockIdx.x; tile < P.ntiles; tile += gridDim.x, it++) {
+      int b = it & 1;
+      // warp-uniform outcome: the TMEM loads below are .sync.aligned
+      bool ready = __all_sync(FULL_MASK, mbar_wait(tfull0 + 8 * b, (it >> 1) & 1, abort_flag));
+      if (!ready) {
+        if (!*abort_flag) { set_status(P.status, BS_ERR_TIMEOUT); *abort_flag = 1; }
+        break;
+      }
+      tc_fence_after();
+      const uint32_t t0 = tmem + lane_off + (uint32_t)(b * 256);
+      float mx = 0.0f;
+      float *dump = P.dump ? P.dump + (size_t)(tile * 128 + row) * BS_TC_COLS : nullptr;
+#pragma unroll 1
+      for (int c0 = 0; c0 < 96; c0 += 32) {
+        float re[32], im[32];
+        tmem_ld_2x32(t0 + c0, t0 + BS_TC_IM0 + c0, re, im);
+        mx = pair_max(re, im, 32, mx);
+        if (dump)
+          for (int k = 0; k < 32; k++) { dump[c0 + k] = re[k]; dump[BS_TC_IM0 + c0 + k] = im[k]; }
+      }
+      {
+        float re[32], im[32];
+        tmem_ld_2x8(t0 + 96, t0 + BS_TC_IM0 + 96, re, im);
+        mx = pair_max(re, im, 8, mx);
+        if (dump)
+          for (int k = 0; k < 8; k++) { dump[96 + k] = re[k]; dump[BS_TC_IM0 + 96 + k] = im[k]; }
+      }
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(tempty0 + 8 * b);
+      long long pair = tile * 64 + (row >> 1);
+      bool mine = !(lane & 1) && pair < P.npairs;
+      bool sure_pass = mine && mx <= P.pass_below;
+      bool unsure = mine && mx > P.pass_below && mx < P.reject_above;
+      if (mine) P.pass[pair] = sure_pass ? 1 : 0;
+      if (unsure) {
+        unsigned long long k = atomicAdd(P.count, 1ULL);
+        if (k < P.unc_cap) P.unc[k] = (unsigned)pair;
+        else atomicExch(P.count + 2, 1ULL);
+      }
+      unsigned np = __popc(__ballot_sync(FULL_MASK, sure_pass));
+      if (lane == 0 && np) atomicAdd(P.count + 1, (unsigned long long)np);
+    }
+  }
+
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (warp == 1) tc_dealloc(tmem, TMEM_COLS);
+}
+
+size_t tc_smem_bytes(int nparts) {
+  return 1024 + (size_t)TC_STAGES * A_STAGE_BYTES + (size_t)nparts * BS_TC_PART_BYTES +
+         (2 * TC_STAGES + 4) * 8 + 16;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------------------------
+// Host side
+// ------------------------------------------------------------------------------------
+#define CK(x)                                       \
+  do {                                              \
+    cudaError_t e_ = (x);                           \
+    if (e_ != cudaSuccess) return bs_cuda_fail(e_); \
+  } while (0)
+
+static int launch_fp64(bs_ctx *ctx, const uint64_t *d_bits, long long npairs,
+                       const unsigned *list, const unsigned long long *list_len,
+                       unsigned long long list_cap, uint8_t *d_pass) {
+  const int L = ctx->n;
+  size_t smem = sizeof(double) * 2 * 200 * L;
+  static bool attr_done = false;
+  if (!attr_done) {
+    CK(cudaFuncSetAttribute(hall_fp64_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                            (int)(sizeof(double) * 2 * 200 * BS_MAXL)));
+    attr_done = true;
+  }
+  int grid = list ? ctx->num_sms : bs_grid_for(npairs, 512, ctx->num_sms);
+  const bool timed = (list == nullptr);  // the FP64 form is the dominant kernel only when alone
+  if (timed) bs_timed_begin(ctx); else ctx->launches++;
+  hall_fp64_kernel<<<grid, 512, smem, ctx->stream>>>(d_bits, npairs, list, list_len, list_cap, L,
+                                                     ctx->lim, ctx->d_cos, ctx->d_sin, d_pass,
+                                                     ctx->d_count + 1);
+  if (timed) bs_timed_end(ctx);
+  CK(cudaGetLastError());
+  return BS_OK;
+}
+
+static int launch_tc(bs_ctx *ctx, int mode, const uint64_t *d_bits, long long npairs,
+                     uint8_t *d_pass, float *d_dump) {
+  const bs_hall_tc_form &F = ctx->tc[mode];
+  TcParams P;
+  P.bits = d_bits;
+  P.npairs = npairs;
+  P.ntiles = (npairs + 63) / 64;
+  P.image = F.d_image;
+  P.nparts = F.nparts;
+  P.ksteps = (ctx->n + 15) / 16;
+  // instruction descriptor: D fp32, A/B format, both K-major, N = 208, M = 128
+  P.idesc = (1u << 4) | ((uint32_t)F.fmt << 7) | ((uint32_t)F.fmt << 10) |
+            ((uint32_t)(BS_TC_COLS >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
+  P.one2 = F.fmt ? 0x3F803F80u : 0x3C003C00u;
+  P.pass_below = F.pass_below;
+  P.reject_above = F.reject_above;
+  P.pass = d_pass;
+  P.unc = ctx->d_unc;
+  P.unc_cap = (unsigned long long)ctx->unc_cap;
+  P.count = ctx->d_count;
+  P.status = ctx->d_status;
+  P.dump = d_dump;
+  size_t smem = tc_smem_bytes(F.nparts);
+  static bool attr_done = false;
+  if (!attr_done) {
+    CK(cudaFuncSetAttribute(hall_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                            (int)tc_smem_bytes(2)));
+    attr_done = true;
+  }
+  long long grid = P.ntiles < ctx->num_sms ? P.ntiles : ctx->num_sms;
+  if (grid < 1) grid = 1;
+  bs_timed_begin(ctx);
+  hall_tc_kernel<<<(int)grid, TC_THREADS, smem, ctx->stream>>>(P);
+  bs_timed_end(ctx);
+  CK(cudaGetLastError());
+  return BS_OK;
+}
+
+static int hall_dev(bs_ctx *ctx, const uint64_t *d_bits, long long npairs, int mode,
+                    uint8_t *d_pass, bs_hall_stats *stats, float *d_dump) {
+  if (!ctx || npairs < 0 || (npairs && (!d_bits || !d_pass))) return BS_ERR_ARG;
+  if (mode < BS_HALL_FP64 || mode > BS_HALL_TC_BF16X2) return BS_ERR_ARG;
+  if (npairs >= (1LL << 32)) return BS_ERR_ARG;
+  CK(cudaSetDevice(ctx->device));
+  CK(cudaMemsetAsync(ctx->d_count, 0, sizeof(unsigned long long) * 8, ctx->stream));
+  if (npairs > 0) {
+    if (mode == BS_HALL_FP64) {
+      int rc = launch_fp64(ctx, d_bits, npairs, nullptr, nullptr, 0, d_pass);
+      if (rc) return rc;
+    } else {
+      int rc = bs_ensure_dev((void **)&ctx->d_unc, &ctx->unc_cap, npairs, sizeof(unsigned));
+      if (rc) return rc;
+      rc = launch_tc(ctx, mode, d_bits, npairs, d_pass, d_dump);
+      if (rc) return rc;
+      rc = launch_fp64(ctx, d_bits, npairs, ctx->d_unc, ctx->d_count,
+                       (unsigned long long)ctx->unc_cap, d_pass);
+      if (rc) return rc;
+    }
+  }
+  if (stats) {
+    unsigned long long cnt[8];
+    int status = 0;
+    CK(cudaMemcpyAsync(cnt, ctx->d_count, sizeof cnt, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaMemcpyAsync(&status, ctx->d_status, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    if (status) {
+      cudaMemsetAsync(ctx->d_status, 0, sizeof(int), ctx->stream);
+      return status;
+    }
+    if (cnt[2]) return BS_ERR_INTERNAL;  // cannot happen: the list holds every pair
+    stats->pairs = npairs;
+    stats->passed = (long long)cnt[1];
+    stats->rechecked = mode == BS_HALL_FP64 ? 0 : (long long)cnt[0];
+    stats->mode = mode;
+    if (mode == BS_HALL_FP64) {
+      stats->pass_below = ctx->lim;
+      stats->reject_above = ctx->lim;
+      stats->quant_err = 0.0;
+    } else {
+      stats->pass_below = ctx->tc[mode].pass_below;
+      stats->reject_above = ctx->tc[mode].reject_above;
+      stats->quant_err = ctx->tc[mode].quant_err;
+    }
+  }
+  return BS_OK;
+}
+
+extern "C" int bs_hall_filter_dev(bs_ctx *ctx, const uint64_t *d_bits, long long npairs, int mode,
+                                  uint8_t *d_pass, bs_hall_stats *stats) {
+  return hall_dev(ctx, d_bits, npairs, mode, d_pass, stats, nullptr);
+}
+
+extern "C" int bs_hall_tc_dump_dev(bs_ctx *ctx, const uint64_t *d_bits, long long npairs, int mode,
+                                   float *d_acc) {
+  if (!ctx || !d_acc || npairs <= 0 || npairs % 64 || npairs > 65536) return BS_ERR_ARG;
+  if (mode != BS_HALL_TC_FP16 && mode != BS_HALL_TC_BF16X2) return BS_ERR_ARG;
+  int rc = bs_ensure_dev((void **)&ctx->d_pass, &ctx->pass_cap, npairs, 1);
+  if (rc) return rc;
+  bs_hall_stats st;
+  return hall_dev(ctx, d_bits, npairs, mode, ctx->d_pass, &st, d_acc);
+}
+
+static int hall_host(bs_ctx *ctx, const void *src, bool packed, long long npairs, int mode,
+                     uint8_t *pass, bs_hall_stats *stats) {
+  if (!ctx || !src || !pass || npairs < 0) return BS_ERR_ARG;
+  if (npairs == 0) {
+    if (stats) { bs_hall_stats z = {}; z.mode = mode; *stats = z; }
+    return BS_OK;
+  }
+  CK(cudaSetDevice(ctx->device));
+  const int L = ctx->n;
+  int rc = bs_ensure_dev((void **)&ctx->d_bits, &ctx->bits_cap, 2 * npairs, sizeof(uint64_t));
+  if (!rc) rc = bs_ensure_dev((void **)&ctx->d_pass, &ctx->pass_cap, npairs, 1);
+  if (rc) return rc;
+  if (packed) {
+    CK(cudaMemcpyAsync(ctx->d_bits, src, sizeof(uint64_t) * 2 * npairs, cudaMemcpyHostToDevice,
+                       ctx->stream));
+  } else {
+    rc = bs_ensure_dev((void **)&ctx->d_rows, &ctx->rows_cap, 2 * npairs * L, 1);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(ctx->d_rows, src, (size_t)2 * npairs * L, cudaMemcpyHostToDevice,
+                       ctx->stream));
+    ctx->launches++;
+    pack_kernel<<<bs_grid_for(2 * npairs, 256, 8 * ctx->num_sms), 256, 0, ctx->stream>>>(
+        ctx->d_rows, 2 * npairs, L, ctx->d_bits, ctx->d_status);
+    CK(cudaGetLastError());
+  }
+  bs_hall_stats st;
+  rc = hall_dev(ctx, ctx->d_bits, npairs, mode, ctx->d_pass, &st, nullptr);
+  if (rc) return rc;
+  CK(cudaMemcpyAsync(pass, ctx->d_pass, (size_t)npairs, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  if (stats) *stats = st;
+  return BS_OK;
+}
+
+extern "C" int bs_hall_filter_batch(bs_ctx *ctx, const int8_t *XY, long long npairs, int mode,
+                                    uint8_t *pass, bs_hall_stats *stats) {
+  return hall_host(ctx, XY, false, npairs, mode, pass, stats);
+}
+
+extern "C" int bs_hall_filter_packed(bs_ctx *ctx, const uint64_t *bits, long long npairs,
+                                     int mode, uint8_t *pass, bs_hall_stats *stats) {
+  return hall_host(ctx, bits, true, npairs, mode, pass, stats);
+}

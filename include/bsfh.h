@@ -1,0 +1,101 @@
+/*
+ * bsfh.h - C ABI of the GB300 first-hit search library (libbsfh.so).
+ *
+ * One context per host thread. The context owns its device buffers and a CUDA stream.
+ * All entry points return 0 (BS_OK) or a negative BS_ERR_* code; none throws. Sequences are
+ * +1/-1. In "packed" form a sequence of length L <= 64 is one uint64 word with bit i set
+ * when element i is +1; a (C,D) pair is two consecutive words.
+ *
+ * Each entry point names the reference interface it replaces, as a path within
+ * DanielGord0n/BS45_Quantum_Explorer (file:line).
+ */
+#ifndef BSFH_H
+#define BSFH_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+  BS_OK = 0,
+  BS_ERR_ARG = -1,      /* bad argument (size, length, mode, null pointer) */
+  BS_ERR_CUDA = -2,     /* a CUDA runtime call failed */
+  BS_ERR_NOMEM = -3,    /* device or host allocation failed */
+  BS_ERR_TIMEOUT = -4,  /* a device wait ran out of its iteration limit; results invalid */
+  BS_ERR_INTERNAL = -5, /* an internal consistency check failed (e.g. NPAF recheck) */
+  BS_ERR_CAP = -6,      /* an output capacity was exceeded; the call reports how much it needs */
+  BS_ERR_NODEV = -7     /* no CUDA device, or not an sm_103 device */
+};
+
+/* Hall (Thm 2.4) filter forms. */
+enum {
+  BS_HALL_FP64 = 0,      /* CUDA-core FP64 in the reference's expression order (exact) */
+  BS_HALL_TC_FP16 = 1,   /* tcgen05 tensor cores, +-1 x fp16 quantised table, FP32 accumulate,
+                            proven margin, FP64 recheck of the margin band (exact decisions) */
+  BS_HALL_TC_BF16X2 = 2  /* as above with the table split hi+lo in bf16 (narrower band) */
+};
+
+typedef struct bs_ctx bs_ctx;
+
+typedef struct {
+  long long pairs;          /* pairs tested */
+  long long passed;         /* pairs accepted (== the reference's hall_ok_pair_fast count) */
+  long long rechecked;      /* pairs that fell inside the margin band and were rechecked in FP64 */
+  double pass_below;        /* max pair PSD at or below which a pair certainly passes */
+  double reject_above;      /* max pair PSD at or above which a pair certainly fails */
+  double quant_err;         /* per-sequence |Re|,|Im| quantisation bound e of the table */
+  int mode;
+} bs_hall_stats;
+
+/* Library identity and error text. */
+int bs_version(void);
+const char *bs_strerror(int code);
+
+/* Create a context for BS(n+1,n) with signature (a,b,c,d) on CUDA device `device`.
+ * Builds the Hall tables on the host with libm exactly as init_hall_tables does
+ * (src/solver/wz_match.cpp:106-114) and uploads them. 4 <= n <= 63. */
+int bs_ctx_create(int n, int a, int b, int c, int d, int device, bs_ctx **out);
+void bs_ctx_destroy(bs_ctx *ctx);
+/* Use a caller-owned CUDA stream (cudaStream_t) for every later call; NULL = the context's own. */
+int bs_ctx_set_stream(bs_ctx *ctx, void *cuda_stream);
+/* Last error recorded by the device (timeouts), cleared on read. */
+int bs_ctx_device_status(bs_ctx *ctx);
+/* Kernel timing, for measurement: when enabled, the dominant kernel of each call (the Hall
+ * kernel) is bracketed by CUDA events on the context stream. _read synchronises, returns the
+ * summed duration and launch count since the last read, and the number of kernels this
+ * context has launched in total. No reference counterpart (instrumentation). */
+int bs_ctx_timing(bs_ctx *ctx, int enable);
+int bs_ctx_timing_read(bs_ctx *ctx, double *ms, long long *timed_launches, long long *all_launches);
+
+/* ---- Hall filter --------------------------------------------------------------------
+ * Replaces hall_ok_pair_fast(X, L, Y, L) / hall_ok_single && hall_ok
+ * (src/solver/wz_match.cpp:117-181) over a batch: pass[i] = 1 exactly when the reference
+ * accepts pair i. Host buffers: XY is npairs rows of 2L int8 (C then D), L = n. */
+int bs_hall_filter_batch(bs_ctx *ctx, const int8_t *XY, long long npairs, int mode,
+                         uint8_t *pass, bs_hall_stats *stats);
+/* Same, host packed input (2 words per pair). */
+int bs_hall_filter_packed(bs_ctx *ctx, const uint64_t *bits, long long npairs, int mode,
+                          uint8_t *pass, bs_hall_stats *stats);
+/* Same, device-resident input and output, enqueued on the context stream. stats (host, may
+ * be NULL) is filled after a stream synchronise when non-NULL. */
+int bs_hall_filter_dev(bs_ctx *ctx, const uint64_t *d_bits, long long npairs, int mode,
+                       uint8_t *d_pass, bs_hall_stats *stats);
+/* Diagnostics: raw tensor-core accumulators for npairs (multiple of 64, <= 65536) pairs,
+ * d_acc[row][208] fp32 with row 2p = C of pair p, 2p+1 = D; columns 0..100 are Re at the
+ * unique angles j = 1..100, 200 and columns 104..204 the matching Im. */
+int bs_hall_tc_dump_dev(bs_ctx *ctx, const uint64_t *d_bits, long long npairs, int mode,
+                        float *d_acc);
+
+/* Pack host int8 sequences (rows of L values) into words. No device work. */
+int bs_pack_rows(const int8_t *seq, long long rows, int L, uint64_t *words);
+
+/* Seeded Hall-microbench input on the device (2 words per pair, length ctx n): the first
+ * half i.i.d. +-1, the second half mirror-quad pairs with sum C = sum D = 0. No reference
+ * counterpart: it generates the synthetic workload the benchmark times. */
+int bs_gen_hall_pairs_dev(bs_ctx *ctx, long long npairs, uint64_t seed, uint64_t *d_words);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
