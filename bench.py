@@ -212,7 +212,10 @@ def main():
 
     npairs = args.pairs
     ctx = Context(N, SIG, device=local)
-    stream = torch.cuda.current_stream()
+    # a dedicated stream: the library launches on it and the events below are recorded on it
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    assert stream.cuda_stream != 0
     ctx.set_stream(stream.cuda_stream)
     d_words = torch.empty(2 * npairs, dtype=torch.int64, device="cuda")
     d_pass = torch.empty(npairs, dtype=torch.uint8, device="cuda")

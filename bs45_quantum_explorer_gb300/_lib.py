@@ -33,6 +33,21 @@ class HallStats(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class Cell(C.Structure):
+    _fields_ = [("tx", C.c_int8 * 8), ("ty", C.c_int8 * 8), ("pinX", C.c_int32), ("pinY", C.c_int32)]
+
+
+class StreamOpts(C.Structure):
+    _fields_ = [("m", C.c_int32), ("rev", C.c_int32), ("endpos", C.c_int32),
+                ("cd_prune", C.c_int32), ("hall_mode", C.c_int32), ("reserved", C.c_int32),
+                ("target_prefixes", C.c_longlong), ("leaf_chunk", C.c_longlong),
+                ("survivor_cap", C.c_longlong)]
+
+
+class CellStats(C.Structure):
+    _fields_ = [("nodes", C.c_longlong), ("leaves", C.c_longlong), ("ok", C.c_longlong)]
+
+
 _lib = None
 
 # (name, restype, argtypes) for every entry point of include/bsfh.h
@@ -52,6 +67,9 @@ SIGNATURES = {
     "bs_hall_tc_dump_dev": (C.c_int, [C.c_void_p, C.c_void_p, C.c_longlong, C.c_int, C.c_void_p]),
     "bs_pack_rows": (C.c_int, [C.c_void_p, C.c_longlong, C.c_int, C.c_void_p]),
     "bs_gen_hall_pairs_dev": (C.c_int, [C.c_void_p, C.c_longlong, C.c_uint64, C.c_void_p]),
+    "bs_cd_stream": (C.c_int, [C.c_void_p, C.POINTER(Cell), C.c_int, C.POINTER(StreamOpts),
+                               C.c_void_p, C.c_void_p, C.c_longlong, C.POINTER(C.c_longlong),
+                               C.POINTER(CellStats)]),
     "bs_ctx_timing": (C.c_int, [C.c_void_p, C.c_int]),
     "bs_ctx_timing_read": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_longlong),
                                      C.POINTER(C.c_longlong)]),

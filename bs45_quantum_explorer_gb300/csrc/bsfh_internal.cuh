@@ -47,7 +47,10 @@ struct bs_ctx {
   double timed_ms;          // accumulated duration of the timed kernels
   long long timed_launches; // launches of the timed kernels
   long long launches;       // every kernel this context has launched
+  void *stream_bufs;        // C,D stream buffers (cd_stream.cu)
 };
+
+void bs_stream_free(bs_ctx *ctx);
 
 // Record the start / stop event of one timed kernel launch on the context stream.
 void bs_timed_begin(bs_ctx *ctx);

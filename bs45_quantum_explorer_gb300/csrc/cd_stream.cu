@@ -1,0 +1,622 @@
+// cd_stream.cu - the C,D mirror-quad stream (the reference's count_pairs22,
+// src/solver/wz_match.cpp:678-784) for a batch of cells, on the GPU.
+//
+// Structure:
+//   1. Host: each cell's DFS tree is expanded to a split depth D in the reference's branch
+//      order (quad index order, reversed under STREAM_REV), giving prefixes in DFS order.
+//      Nodes above D are counted here exactly as the reference counts rec() calls.
+//   2. Device, cd_dfs_kernel: persistent threads take prefixes from a queue and walk the
+//      subtree below each one iteratively, one tree step per loop iteration (so a warp's lanes
+//      stay busy on different subtrees). A class-exact leaf is appended to the leaf buffer with
+//      key (prefix index << 32 | leaf sequence inside the prefix). When the buffer is full a
+//      thread saves its position and stops; the next launch resumes it.
+//   3. Device: the Hall filter (tensor-core form by default) decides every leaf; survivors are
+//      compacted with their keys; sorting by key restores the reference's stream order.
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "bsfh_internal.cuh"
+
+namespace {
+
+#define FULL_MASK 0xffffffffu
+
+struct CellDev {
+  int8_t tx[8], ty[8];
+};
+
+struct Prefix {
+  uint32_t cell;
+  uint32_t depth;   // D: quads placed at depths 0..D-1
+  uint64_t digits;  // 4 bits per depth: the loop index kk chosen at that depth
+};
+
+// A suspended subtree walk: the node at depth d with its next child index kk.
+struct Saved {
+  uint32_t prefix;
+  uint32_t seq;        // leaves emitted so far inside this prefix
+  uint16_t d, kk;
+  uint16_t pending;    // 1: child kk of node d is a leaf that was not yet written
+  uint16_t pad;
+  uint64_t dig[2];     // digits of depths 0..d-1 (4 bits each, depths 0-15 and 16-31)
+};
+
+struct CdParams {
+  int L, m, half, rev, ns0;
+  const uint8_t *cls;  // per depth d: class of position d (low nibble) and of L-1-d (high)
+  const CellDev *cells;
+  const Prefix *prefixes;
+  long long nprefix;
+  unsigned long long *next_prefix;
+  const Saved *saved_in;
+  int nsaved_in;
+  Saved *saved_out;
+  unsigned *nsaved_out;
+  int saved_cap;
+  uint64_t *leaf_words;  // [cap][2]
+  uint64_t *leaf_keys;   // [cap]
+  unsigned long long *leaf_count;
+  unsigned long long leaf_cap;
+  unsigned long long *cell_nodes, *cell_leaves;
+  int *full_flag;
+  int *status;
+};
+
+// quad tables: index -> (v0, v1, v2, v3) as sign bits (bit 3 = v0 ... bit 0 = v3)
+__constant__ uint8_t kPos[8] = {0, 3, 5, 6, 9, 10, 12, 15};
+
+__device__ __forceinline__ int getdig(const uint64_t dig[2], int d) {
+  return (int)((dig[d >> 4] >> (4 * (d & 15))) & 15);
+}
+__device__ __forceinline__ void setdig(uint64_t dig[2], int d, int v) {
+  int w = d >> 4, s = 4 * (d & 15);
+  dig[w] = (dig[w] & ~(15ULL << s)) | ((uint64_t)v << s);
+}
+
+// Per-class remaining differences dx = tx - px, dy = ty - py and remaining slots rem, packed
+// as 8-bit fields (bias 64) of three words; class c occupies bits 8c..8c+7.
+struct Walk {
+  uint64_t dx, dy, rem;
+  uint64_t X, Y;
+};
+
+__device__ __forceinline__ int fld(uint64_t w, int c) { return (int)((w >> (8 * c)) & 255) - 64; }
+
+// Apply (sign = -1) or remove (sign = +1) quad q at depth d; returns nothing. The quad's values
+// are v = +1 for a set bit, -1 otherwise.
+__device__ __forceinline__ void apply_quad(Walk &w, const uint8_t *cls, int L, int d, uint32_t q,
+                                           int sign) {
+  const int c1 = cls[d] & 15, c2 = cls[d] >> 4;
+  int a = (q & 8) ? 1 : -1, b = (q & 4) ? 1 : -1, c = (q & 2) ? 1 : -1, e = (q & 1) ? 1 : -1;
+  // dx -= a (place) / dx += a (remove), rem -= 1 / += 1
+  w.dx += (uint64_t)(int64_t)(sign * a) << (8 * c1);
+  w.dy += (uint64_t)(int64_t)(sign * b) << (8 * c1);
+  w.dx += (uint64_t)(int64_t)(sign * c) << (8 * c2);
+  w.dy += (uint64_t)(int64_t)(sign * e) << (8 * c2);
+  w.rem += (uint64_t)(int64_t)sign << (8 * c1);
+  w.rem += (uint64_t)(int64_t)sign << (8 * c2);
+  const uint64_t m1 = 1ULL << d, m2 = 1ULL << (L - 1 - d);
+  if (sign < 0) {
+    if (a > 0) w.X |= m1;
+    if (b > 0) w.Y |= m1;
+    if (c > 0) w.X |= m2;
+    if (e > 0) w.Y |= m2;
+  } else {
+    w.X &= ~(m1 | m2);
+    w.Y &= ~(m1 | m2);
+  }
+}
+
+__device__ __forceinline__ bool cap_ok(const Walk &w, int c) {
+  int r = fld(w.rem, c), x = fld(w.dx, c), y = fld(w.dy, c);
+  return x >= -r && x <= r && y >= -r && y <= r;
+}
+
+__device__ __forceinline__ uint32_t quad_at(int d, int kk, int ns0, int rev) {
+  if (d == 0) {
+    int k = rev ? ns0 - 1 - kk : kk;
+    return ns0 == 16 ? (uint32_t)k : kPos[k];
+  }
+  int k = rev ? 7 - kk : kk;
+  return kPos[k];
+}
+
+__device__ __forceinline__ void init_walk(Walk &w, const CellDev &cell, int L, int m) {
+  w.dx = w.dy = w.rem = 0;
+  for (int c = 0; c < m; c++) {
+    int cnt = (L - c + m - 1) / m;  // positions p < L with p % m == c
+    w.dx |= (uint64_t)(cell.tx[c] + 64) << (8 * c);
+    w.dy |= (uint64_t)(cell.ty[c] + 64) << (8 * c);
+    w.rem |= (uint64_t)(cnt + 64) << (8 * c);
+  }
+  w.X = w.Y = 0;
+}
+
+__global__ void __launch_bounds__(256) cd_dfs_kernel(CdParams P) {
+  __shared__ uint8_t cls[64];
+  if (threadIdx.x < 64) cls[threadIdx.x] = P.cls[threadIdx.x];
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  const int L = P.L, m = P.m, half = P.half;
+  bool have = false;
+  uint32_t prefix = 0, cell = 0, seq = 0;
+  int D = 0, d = 0, kk = 0;
+  uint64_t dig[2] = {0, 0};
+  Walk w;
+  unsigned long long nodes = 0, leaves = 0;
+  bool pending = false;
+  int saved_slot = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+  unsigned iter = 0;
+
+  while (true) {
+    // ---- acquire work: this thread's saved walk first, then fresh prefixes ----
+    if (!have) {
+      if (saved_slot < P.nsaved_in) {
+        const Saved sv = P.saved_in[saved_slot];
+        saved_slot = P.nsaved_in;  // at most one saved walk per thread
+        prefix = sv.prefix;
+        const Prefix pf = P.prefixes[prefix];
+        cell = pf.cell;
+        D = (int)pf.depth;
+        d = sv.d;
+        kk = sv.kk;
+        seq = sv.seq;
+        dig[0] = sv.dig[0];
+        dig[1] = sv.dig[1];
+        pending = sv.pending != 0;
+      } else {
+        if (*(volatile int *)P.full_flag) break;
+        unsigned long long p = atomicAdd(P.next_prefix, 1ULL);
+        if (p >= (unsigned long long)P.nprefix) break;
+        prefix = (uint32_t)p;
+        const Prefix pf = P.prefixes[p];
+        cell = pf.cell;
+        D = (int)pf.depth;
+        d = D;
+        kk = 0;
+        seq = 0;
+        dig[0] = pf.digits;
+        dig[1] = 0;
+        pending = false;
+      }
+      init_walk(w, P.cells[cell], L, m);
+      for (int t = 0; t < d; t++)
+        apply_quad(w, cls, L, t, quad_at(t, getdig(dig, t), P.ns0, P.rev), -1);
+      have = true;
+    }
+
+    // ---- one tree step ----
+    bool emit = false, finished = false;
+    uint64_t lx = 0, ly = 0;
+    if (pending) {
+      // the leaf that could not be written last time (its node is already counted)
+      const uint32_t q = quad_at(d, kk, P.ns0, P.rev);
+      apply_quad(w, cls, L, d, q, -1);
+      lx = w.X;
+      ly = w.Y;
+      if (L & 1) {
+        const int cm = half % m;
+        if (fld(w.dx, cm) > 0) lx |= 1ULL << half;
+        if (fld(w.dy, cm) > 0) ly |= 1ULL << half;
+      }
+      apply_quad(w, cls, L, d, q, +1);
+      emit = true;
+    } else if (kk == 8) {
+      if (d == D) {
+        finished = true;
+      } else {
+        d--;
+        kk = getdig(dig, d);
+        apply_quad(w, cls, L, d, quad_at(d, kk, P.ns0, P.rev), +1);
+        kk++;
+      }
+    } else {
+      const uint32_t q = quad_at(d, kk, P.ns0, P.rev);
+      apply_quad(w, cls, L, d, q, -1);
+      nodes++;
+      const int c1 = cls[d] & 15, c2 = cls[d] >> 4;
+      if (!cap_ok(w, c1) || !cap_ok(w, c2)) {
+        apply_quad(w, cls, L, d, q, +1);
+        kk++;
+      } else if (d + 1 == half) {
+        lx = w.X;
+        ly = w.Y;
+        if (L & 1) {  // the free middle takes the only values that make the cell exact
+          const int cm = half % m;
+          if (fld(w.dx, cm) > 0) lx |= 1ULL << half;
+          if (fld(w.dy, cm) > 0) ly |= 1ULL << half;
+        }
+        apply_quad(w, cls, L, d, q, +1);
+        emit = true;
+      } else {
+        setdig(dig, d, kk);
+        d++;
+        kk = 0;
+      }
+    }
+
+    // ---- warp-aggregated leaf append ----
+    const unsigned act = __activemask();
+    const unsigned ball = __ballot_sync(act, emit);
+    if (ball) {
+      const int leader = __ffs(ball) - 1;
+      unsigned long long base = 0;
+      if (lane == leader) base = atomicAdd(P.leaf_count, (unsigned long long)__popc(ball));
+      base = __shfl_sync(act, base, leader);
+      if (emit) {
+        const unsigned long long slot = base + __popc(ball & ((1u << lane) - 1u));
+        if (slot < P.leaf_cap) {
+          P.leaf_words[2 * slot] = lx;
+          P.leaf_words[2 * slot + 1] = ly;
+          P.leaf_keys[slot] = ((unsigned long long)prefix << 32) | seq;
+          seq++;
+          leaves++;
+          pending = false;
+          kk++;
+        } else {
+          pending = true;  // suspend below with this leaf still owed
+          atomicExch(P.full_flag, 1);
+        }
+      }
+    }
+
+    // ---- suspend after an unwritten leaf, or at a clean point once the buffer is full ----
+    iter++;
+    const bool suspend = !finished &&
+                         (pending || ((iter & 255) == 0 && *(volatile int *)P.full_flag));
+    if (suspend) {
+      const unsigned k = atomicAdd(P.nsaved_out, 1u);
+      if ((int)k < P.saved_cap) {
+        Saved sv;
+        sv.prefix = prefix;
+        sv.seq = seq;
+        sv.d = (uint16_t)d;
+        sv.kk = (uint16_t)kk;
+        sv.pending = pending ? 1 : 0;
+        sv.pad = 0;
+        sv.dig[0] = dig[0];
+        sv.dig[1] = dig[1];
+        P.saved_out[k] = sv;
+      } else {
+        atomicCAS(P.status, 0, BS_ERR_INTERNAL);
+      }
+    }
+    if (finished || suspend) {
+      if (nodes) atomicAdd(P.cell_nodes + cell, nodes);
+      if (leaves) atomicAdd(P.cell_leaves + cell, leaves);
+      nodes = 0;
+      leaves = 0;
+      have = false;
+      pending = false;
+      if (suspend) break;
+    }
+  }
+}
+
+// Compact the leaves that passed the Hall filter (with their keys), count passes per cell.
+__global__ void compact_kernel(const uint64_t *__restrict__ words, const uint64_t *__restrict__ keys,
+                               const uint8_t *__restrict__ pass, long long count,
+                               const Prefix *__restrict__ prefixes, uint64_t *out_words,
+                               uint64_t *out_keys, unsigned long long *out_count,
+                               unsigned long long out_cap, unsigned long long *cell_ok) {
+  const int lane = threadIdx.x & 31;
+  for (long long base = (long long)blockIdx.x * blockDim.x; base < count;
+       base += (long long)gridDim.x * blockDim.x) {
+    long long i = base + threadIdx.x;
+    bool p = i < count && pass[i];
+    unsigned ball = __ballot_sync(FULL_MASK, p);
+    if (!ball) continue;
+    int leader = __ffs(ball) - 1;
+    unsigned long long o = 0;
+    if (lane == leader) o = atomicAdd(out_count, (unsigned long long)__popc(ball));
+    o = __shfl_sync(FULL_MASK, o, leader);
+    if (p) {
+      unsigned long long slot = o + __popc(ball & ((1u << lane) - 1u));
+      uint64_t k = keys[i];
+      if (slot < out_cap) {
+        out_words[2 * slot] = words[2 * i];
+        out_words[2 * slot + 1] = words[2 * i + 1];
+        out_keys[slot] = k;
+      }
+      atomicAdd(cell_ok + prefixes[k >> 32].cell, 1ULL);
+    }
+  }
+}
+
+// ------------------------------------------------------------------------------------
+// Host: frontier of each cell in the reference's order
+// ------------------------------------------------------------------------------------
+struct HostQuads {
+  int all[16][4], pos[8][4];
+  HostQuads() {
+    int np = 0;
+    for (int i = 0; i < 16; i++) {
+      int v[4] = {(i & 8) ? 1 : -1, (i & 4) ? 1 : -1, (i & 2) ? 1 : -1, (i & 1) ? 1 : -1};
+      memcpy(all[i], v, sizeof v);
+      if (v[0] * v[1] * v[2] * v[3] == 1) memcpy(pos[np++], v, sizeof v);
+    }
+  }
+};
+
+struct Frontier {
+  int L, m, half, D, rev, endpos, pinX, pinY, ns0;
+  int tot[8], px[8], py[8], placed[8];
+  const int8_t *tx, *ty;
+  const HostQuads *Q;
+  uint32_t cell;
+  long long nodes;
+  std::vector<Prefix> *out;
+
+  bool check() const {
+    for (int c = 0; c < m; c++) {
+      int rem = tot[c] - placed[c];
+      int dx = tx[c] - px[c], dy = ty[c] - py[c];
+      if (dx < -rem || dx > rem || dy < -rem || dy > rem) return false;
+      if (((dx + rem) & 1) != 0 || ((dy + rem) & 1) != 0) return false;
+    }
+    return true;
+  }
+
+  void rec(int d, uint64_t digits) {
+    nodes++;
+    if (!check()) return;
+    if (d == D) {
+      out->push_back(Prefix{cell, (uint32_t)D, digits});
+      return;
+    }
+    const int i1 = d, i2 = L - 1 - d, c1 = i1 % m, c2 = i2 % m;
+    const int(*S)[4] = (d == 0) ? (endpos ? Q->pos : Q->all) : Q->pos;
+    const int ns = (d == 0) ? ns0 : 8;
+    for (int kk = 0; kk < ns; kk++) {
+      int k = rev ? ns - 1 - kk : kk;
+      if (d == 0 && pinX && S[k][0] != 1) continue;
+      if (d == 0 && pinY && S[k][1] != 1) continue;
+      px[c1] += S[k][0]; py[c1] += S[k][1]; px[c2] += S[k][2]; py[c2] += S[k][3];
+      placed[c1]++; placed[c2]++;
+      rec(d + 1, digits | ((uint64_t)kk << (4 * d)));
+      px[c1] -= S[k][0]; py[c1] -= S[k][1]; px[c2] -= S[k][2]; py[c2] -= S[k][3];
+      placed[c1]--; placed[c2]--;
+    }
+  }
+};
+
+}  // namespace
+
+// ------------------------------------------------------------------------------------
+// Entry point
+// ------------------------------------------------------------------------------------
+#define CK(x)                                       \
+  do {                                              \
+    cudaError_t e_ = (x);                           \
+    if (e_ != cudaSuccess) return bs_cuda_fail(e_); \
+  } while (0)
+
+struct StreamBufs {
+  CellDev *cells = nullptr; long long cells_cap = 0;
+  Prefix *prefixes = nullptr; long long prefix_cap = 0;
+  Saved *saved[2] = {nullptr, nullptr}; long long saved_cap = 0;
+  uint64_t *leaf_words = nullptr, *leaf_keys = nullptr; long long leaf_cap = 0;
+  uint8_t *leaf_pass = nullptr; long long pass_cap = 0;
+  uint64_t *surv_words = nullptr, *surv_keys = nullptr; long long surv_cap = 0;
+  unsigned long long *counters = nullptr;  // see below
+  unsigned long long *cell_stats = nullptr; long long cell_stats_cap = 0;
+  unsigned *nsaved = nullptr;
+  int *full = nullptr;
+  uint8_t *cls = nullptr;
+};
+
+static StreamBufs *bufs_of(bs_ctx *ctx) {
+  if (!ctx->stream_bufs) ctx->stream_bufs = new StreamBufs();
+  return (StreamBufs *)ctx->stream_bufs;
+}
+
+void bs_stream_free(bs_ctx *ctx) {
+  StreamBufs *b = (StreamBufs *)ctx->stream_bufs;
+  if (!b) return;
+  cudaFree(b->cells); cudaFree(b->prefixes); cudaFree(b->saved[0]); cudaFree(b->saved[1]);
+  cudaFree(b->leaf_words); cudaFree(b->leaf_keys); cudaFree(b->leaf_pass);
+  cudaFree(b->surv_words); cudaFree(b->surv_keys); cudaFree(b->counters);
+  cudaFree(b->cell_stats); cudaFree(b->nsaved); cudaFree(b->full); cudaFree(b->cls);
+  delete b;
+  ctx->stream_bufs = nullptr;
+}
+
+extern "C" int bs_cd_stream(bs_ctx *ctx, const bs_cell *cells, int ncells, const bs_stream_opts *opt,
+                            uint64_t *out_words, uint32_t *out_cell, long long out_cap,
+                            long long *nout, bs_cell_stats *stats) {
+  if (!ctx || !cells || ncells <= 0 || !opt || !nout) return BS_ERR_ARG;
+  if (out_cap > 0 && !out_words) return BS_ERR_ARG;
+  const int L = ctx->n, m = opt->m;
+  if (m != 3 && m != 6) return BS_ERR_ARG;
+  if (L > 63 || L / 2 > 31) return BS_ERR_ARG;
+  if (opt->cd_prune != 0) return BS_ERR_ARG;  // optional CD_PRUNE is not built on the device
+  int hall_mode = opt->hall_mode;
+  if (hall_mode < BS_HALL_FP64 || hall_mode > BS_HALL_TC_BF16X2) return BS_ERR_ARG;
+  CK(cudaSetDevice(ctx->device));
+  StreamBufs *B = bufs_of(ctx);
+  const int half = L / 2;
+
+  // ---- frontier on the host ----
+  static const HostQuads Q;
+  std::vector<Prefix> prefixes;
+  std::vector<long long> host_nodes(ncells, 0);
+  long long target = opt->target_prefixes > 0 ? opt->target_prefixes : 262144;
+  long long per_cell_target = std::max<long long>(64, target / ncells);
+  for (int ci = 0; ci < ncells; ci++) {
+    const bs_cell &c = cells[ci];
+    Frontier F;
+    F.L = L; F.m = m; F.half = half; F.rev = opt->rev; F.endpos = opt->endpos;
+    F.pinX = c.pinX; F.pinY = c.pinY;
+    F.ns0 = opt->endpos ? 8 : 16;
+    for (int k = 0; k < m; k++) {
+      F.tot[k] = 0;
+      for (int p = k; p < L; p += m) F.tot[k]++;
+    }
+    F.tx = c.tx; F.ty = c.ty; F.Q = &Q; F.cell = (uint32_t)ci;
+    // deepen until the cell has enough prefixes or the split reaches depth half-1
+    std::vector<Prefix> mine;
+    int D = 1;
+    for (;;) {
+      mine.clear();
+      memset(F.px, 0, sizeof F.px); memset(F.py, 0, sizeof F.py); memset(F.placed, 0, sizeof F.placed);
+      F.D = D; F.nodes = 0; F.out = &mine;
+      F.rec(0, 0);
+      if ((long long)mine.size() >= per_cell_target || D >= half - 1 || mine.empty()) break;
+      D++;
+    }
+    host_nodes[ci] = F.nodes;
+    prefixes.insert(prefixes.end(), mine.begin(), mine.end());
+  }
+  const long long nprefix = (long long)prefixes.size();
+  if (nprefix >= (1LL << 32)) return BS_ERR_CAP;
+
+  // ---- device buffers ----
+  int rc = bs_ensure_dev((void **)&B->cells, &B->cells_cap, ncells, sizeof(CellDev));
+  if (!rc) rc = bs_ensure_dev((void **)&B->cell_stats, &B->cell_stats_cap, 3LL * ncells, sizeof(unsigned long long));
+  if (!rc && nprefix) rc = bs_ensure_dev((void **)&B->prefixes, &B->prefix_cap, nprefix, sizeof(Prefix));
+  long long leaf_cap = opt->leaf_chunk > 0 ? opt->leaf_chunk : (1LL << 24);
+  if (!rc) {
+    long long c0 = B->leaf_cap;
+    rc = bs_ensure_dev((void **)&B->leaf_keys, &B->leaf_cap, leaf_cap, sizeof(uint64_t));
+    if (!rc && (B->leaf_cap != c0 || !B->leaf_words)) {
+      cudaFree(B->leaf_words);
+      B->leaf_words = nullptr;
+      CK(cudaMalloc(&B->leaf_words, sizeof(uint64_t) * 2 * B->leaf_cap));
+    }
+  }
+  if (!rc) rc = bs_ensure_dev((void **)&B->leaf_pass, &B->pass_cap, leaf_cap, 1);
+  const int block = 256;
+  const int grid = ctx->num_sms * 6;
+  const int saved_cap = grid * block;
+  if (!rc && B->saved_cap < saved_cap) {
+    cudaFree(B->saved[0]); cudaFree(B->saved[1]);
+    CK(cudaMalloc(&B->saved[0], sizeof(Saved) * saved_cap));
+    CK(cudaMalloc(&B->saved[1], sizeof(Saved) * saved_cap));
+    B->saved_cap = saved_cap;
+  }
+  if (!rc && !B->counters) {
+    CK(cudaMalloc(&B->counters, sizeof(unsigned long long) * 8));
+    CK(cudaMalloc(&B->nsaved, sizeof(unsigned) * 2));
+    CK(cudaMalloc(&B->full, sizeof(int)));
+    CK(cudaMalloc(&B->cls, 64));
+  }
+  long long surv_cap = opt->survivor_cap > 0 ? opt->survivor_cap : (1LL << 22);
+  if (!rc) {
+    long long c0 = B->surv_cap;
+    rc = bs_ensure_dev((void **)&B->surv_keys, &B->surv_cap, surv_cap, sizeof(uint64_t));
+    if (!rc && (B->surv_cap != c0 || !B->surv_words)) {
+      cudaFree(B->surv_words);
+      B->surv_words = nullptr;
+      CK(cudaMalloc(&B->surv_words, sizeof(uint64_t) * 2 * B->surv_cap));
+    }
+  }
+  if (rc) return rc;
+  surv_cap = B->surv_cap;
+  leaf_cap = B->leaf_cap;
+
+  std::vector<CellDev> hc(ncells);
+  for (int ci = 0; ci < ncells; ci++) {
+    memset(&hc[ci], 0, sizeof(CellDev));
+    for (int k = 0; k < m; k++) { hc[ci].tx[k] = cells[ci].tx[k]; hc[ci].ty[k] = cells[ci].ty[k]; }
+  }
+  uint8_t cls[64];
+  memset(cls, 0, sizeof cls);
+  for (int dd = 0; dd < half && dd < 64; dd++) cls[dd] = (uint8_t)((dd % m) | (((L - 1 - dd) % m) << 4));
+  cudaStream_t s = ctx->stream;
+  CK(cudaMemcpyAsync(B->cls, cls, sizeof cls, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(B->cells, hc.data(), sizeof(CellDev) * ncells, cudaMemcpyHostToDevice, s));
+  if (nprefix)
+    CK(cudaMemcpyAsync(B->prefixes, prefixes.data(), sizeof(Prefix) * nprefix, cudaMemcpyHostToDevice, s));
+  CK(cudaMemsetAsync(B->cell_stats, 0, sizeof(unsigned long long) * 3 * ncells, s));
+  CK(cudaMemsetAsync(B->counters, 0, sizeof(unsigned long long) * 8, s));
+  // counters: [0] next prefix, [1] leaf count, [2] survivor count
+  unsigned long long *cell_nodes = B->cell_stats, *cell_leaves = B->cell_stats + ncells,
+                     *cell_ok = B->cell_stats + 2 * ncells;
+
+  int nsaved = 0, cur = 0;
+  long long rounds = 0;
+  while (nprefix > 0) {
+    CK(cudaMemsetAsync(B->nsaved, 0, sizeof(unsigned), s));
+    CK(cudaMemsetAsync(B->full, 0, sizeof(int), s));
+    CK(cudaMemsetAsync(B->counters + 1, 0, sizeof(unsigned long long), s));
+    CdParams P;
+    P.L = L; P.m = m; P.half = half; P.rev = opt->rev; P.ns0 = opt->endpos ? 8 : 16;
+    P.cls = B->cls;
+    P.cells = B->cells; P.prefixes = B->prefixes; P.nprefix = nprefix;
+    P.next_prefix = B->counters;
+    P.saved_in = B->saved[cur]; P.nsaved_in = nsaved;
+    P.saved_out = B->saved[cur ^ 1]; P.nsaved_out = B->nsaved; P.saved_cap = saved_cap;
+    P.leaf_words = B->leaf_words; P.leaf_keys = B->leaf_keys;
+    P.leaf_count = B->counters + 1; P.leaf_cap = (unsigned long long)leaf_cap;
+    P.cell_nodes = cell_nodes; P.cell_leaves = cell_leaves;
+    P.full_flag = B->full; P.status = ctx->d_status;
+    bs_timed_begin(ctx);
+    cd_dfs_kernel<<<grid, block, 0, s>>>(P);
+    bs_timed_end(ctx);
+    CK(cudaGetLastError());
+    unsigned long long leaf_count = 0;
+    unsigned nsv = 0;
+    CK(cudaMemcpyAsync(&leaf_count, B->counters + 1, sizeof leaf_count, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(&nsv, B->nsaved, sizeof nsv, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    if ((int)nsv > saved_cap) return BS_ERR_INTERNAL;
+    long long nleaf = (long long)std::min<unsigned long long>(leaf_count, (unsigned long long)leaf_cap);
+    if (nleaf > 0) {
+      int r2 = bs_hall_filter_dev(ctx, B->leaf_words, nleaf, hall_mode, B->leaf_pass, nullptr);
+      if (r2) return r2;
+      ctx->launches++;
+      compact_kernel<<<bs_grid_for(nleaf, 256, 8 * ctx->num_sms), 256, 0, s>>>(
+          B->leaf_words, B->leaf_keys, B->leaf_pass, nleaf, B->prefixes, B->surv_words, B->surv_keys,
+          B->counters + 2, (unsigned long long)surv_cap, cell_ok);
+      CK(cudaGetLastError());
+    }
+    rounds++;
+    nsaved = (int)nsv;
+    cur ^= 1;
+    if (nsaved == 0) {
+      unsigned long long nextp = 0;
+      CK(cudaMemcpyAsync(&nextp, B->counters, sizeof nextp, cudaMemcpyDeviceToHost, s));
+      CK(cudaStreamSynchronize(s));
+      if (nextp >= (unsigned long long)nprefix) break;
+    }
+  }
+
+  // ---- results ----
+  unsigned long long nsurv = 0;
+  int status = 0;
+  CK(cudaMemcpyAsync(&nsurv, B->counters + 2, sizeof nsurv, cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(&status, ctx->d_status, sizeof status, cudaMemcpyDeviceToHost, s));
+  std::vector<unsigned long long> cs(3 * (size_t)ncells);
+  CK(cudaMemcpyAsync(cs.data(), B->cell_stats, sizeof(unsigned long long) * 3 * ncells, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  if (status) {
+    cudaMemsetAsync(ctx->d_status, 0, sizeof(int), s);
+    return status;
+  }
+  if (stats)
+    for (int ci = 0; ci < ncells; ci++) {
+      stats[ci].nodes = host_nodes[ci] + (long long)cs[ci];
+      stats[ci].leaves = (long long)cs[ncells + ci];
+      stats[ci].ok = (long long)cs[2 * ncells + ci];
+    }
+  *nout = (long long)nsurv;
+  if ((long long)nsurv > surv_cap || (long long)nsurv > out_cap) return BS_ERR_CAP;
+  if (nsurv == 0) return BS_OK;
+  std::vector<uint64_t> keys(nsurv), words(2 * nsurv);
+  CK(cudaMemcpyAsync(keys.data(), B->surv_keys, sizeof(uint64_t) * nsurv, cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(words.data(), B->surv_words, sizeof(uint64_t) * 2 * nsurv, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  std::vector<uint32_t> order(nsurv);
+  for (uint32_t i = 0; i < (uint32_t)nsurv; i++) order[i] = i;
+  std::sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) { return keys[a] < keys[b]; });
+  for (unsigned long long i = 0; i < nsurv; i++) {
+    out_words[2 * i] = words[2 * order[i]];
+    out_words[2 * i + 1] = words[2 * order[i] + 1];
+    if (out_cell) out_cell[i] = prefixes[keys[order[i]] >> 32].cell;
+  }
+  return BS_OK;
+}

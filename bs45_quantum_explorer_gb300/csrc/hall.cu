@@ -113,7 +113,11 @@ __global__ void pack_kernel(const int8_t *__restrict__ rows, long long nrows, in
 // tcgen05 form
 // ------------------------------------------------------------------------------------
 constexpr int TC_STAGES = 4;
-constexpr int TC_THREADS = 192;  // warp 0 producer, warp 1 MMA issuer, warps 2..5 epilogue
+// warps [0, TC_PRODUCERS) producers, TC_MMA_WARP the MMA issuer (and TMEM owner), then two
+// epilogue groups of four warps
+constexpr int TC_PRODUCERS = 2;
+constexpr int TC_MMA_WARP = TC_PRODUCERS;
+constexpr int TC_THREADS = 32 * (TC_PRODUCERS + 1 + 8);
 constexpr int A_STAGE_BYTES = 128 * 128;
 constexpr uint32_t TMEM_COLS = 512;  // two accumulators of 208 columns at 0 and 256
 
@@ -281,6 +285,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) hall_tc_kernel(TcParams P) {
   const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + TC_STAGES);
   const uint32_t tfull0 = smem_u32(bars + 2 * TC_STAGES), tempty0 = tfull0 + 16;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const long long G = gridDim.x;
 
   {  // table image -> shared memory
     const uint4 *src = (const uint4 *)P.image;
@@ -300,19 +305,36 @@ __global__ void __launch_bounds__(TC_THREADS, 1) hall_tc_kernel(TcParams P) {
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  if (warp == 1) tc_alloc(smem_u32(tmem_slot), TMEM_COLS);
+  if (warp == TC_MMA_WARP) tc_alloc(smem_u32(tmem_slot), TMEM_COLS);
   fence_async_smem();
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
 
-  if (warp == 0) {
-    // ---- producer: packed words -> +-1 operand rows in the swizzled layout ----
-    int it = 0;
-    for (long long tile = blockIdx.x; tile < P.ntiles; tile += gridDim.x, it++) {
-      int s = it % TC_STAGES;
-      uint32_t par = ((it / TC_STAGES) & 1) ^ 1;
+  if (warp < TC_PRODUCERS) {
+    // ---- producers: packed words -> +-1 operand rows in the swizzled layout. Producer p
+    // fills the CTA's tiles it = p, p + TC_PRODUCERS, ...; the next tile's words are loaded
+    // before the current tile is unpacked so the global-load latency overlaps the work. ----
+    const long long rows_total = 2 * P.npairs;
+    int it = warp;
+    long long tile = blockIdx.x + (long long)it * G;
+    uint64_t wv[4];
+#pragma unroll
+    for (int rr = 0; rr < 4; rr++) {
+      long long row = tile * 128 + lane + 32 * rr;
+      wv[rr] = (tile < P.ntiles && row < rows_total) ? __ldg(P.bits + row) : 0ULL;
+    }
+    while (tile < P.ntiles) {
+      const long long next = tile + TC_PRODUCERS * G;
+      uint64_t nw[4];
+#pragma unroll
+      for (int rr = 0; rr < 4; rr++) {
+        long long row = next * 128 + lane + 32 * rr;
+        nw[rr] = (next < P.ntiles && row < rows_total) ? __ldg(P.bits + row) : 0ULL;
+      }
+      const int s = it % TC_STAGES;
+      const uint32_t par = ((it / TC_STAGES) & 1) ^ 1;
       if (!mbar_wait(empty0 + 8 * s, par, abort_flag)) {
         if (!*abort_flag) { set_status(P.status, BS_ERR_TIMEOUT); *abort_flag = 1; }
         break;
@@ -320,9 +342,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) hall_tc_kernel(TcParams P) {
       uint8_t *A = sA + s * A_STAGE_BYTES;
 #pragma unroll
       for (int rr = 0; rr < 4; rr++) {
-        int r = lane + 32 * rr;
-        long long row = tile * 128 + r;
-        uint64_t w = (row < 2 * P.npairs) ? __ldg(P.bits + row) : 0ULL;
+        const int r = lane + 32 * rr;
+        const uint64_t w = wv[rr];
         for (int c = 0; c < 2 * P.ksteps; c++) {
           uint32_t nb = ~(uint32_t)(w >> (8 * c));
           uint4 v;
@@ -336,13 +357,17 @@ __global__ void __launch_bounds__(TC_THREADS, 1) hall_tc_kernel(TcParams P) {
       fence_async_smem();
       __syncwarp();
       if (lane == 0) mbar_arrive(full0 + 8 * s);
+#pragma unroll
+      for (int rr = 0; rr < 4; rr++) wv[rr] = nw[rr];
+      tile = next;
+      it += TC_PRODUCERS;
     }
-  } else if (warp == 1) {
+  } else if (warp == TC_MMA_WARP) {
     // ---- MMA issuer (one thread) ----
     if (lane == 0) {
       const uint32_t a_base = smem_u32(sA), b_base = smem_u32(sB);
       int it = 0, last = -1;
-      for (long long tile = blockIdx.x; tile < P.ntiles; tile += gridDim.x, it++) {
+      for (long long tile = blockIdx.x; tile < P.ntiles; tile += G, it++) {
         int s = it % TC_STAGES, b = it & 1;
         if (!mbar_wait(tempty0 + 8 * b, ((it >> 1) & 1) ^ 1, abort_flag) ||
             !mbar_wait(full0 + 8 * s, (it / TC_STAGES) & 1, abort_flag)) {
@@ -368,13 +393,16 @@ __global__ void __launch_bounds__(TC_THREADS, 1) hall_tc_kernel(TcParams P) {
     }
     __syncwarp();
   } else {
-    // ---- epilogue: TMEM -> max pair PSD -> decision ----
+    // ---- epilogue: TMEM -> max pair PSD -> decision. Group g owns accumulator g (the CTA's
+    // tiles it = g, g + 2, ...); its four warps cover the four 32-lane quarters. ----
+    const int eg = (warp - TC_MMA_WARP - 1) >> 2;
     const int q = warp & 3;
     const uint32_t lane_off = (uint32_t)(q * 32) << 16;
     const int row = q * 32 + lane;
-    int it = 0;
-    for (long long tile = blockIdx.x; tile < P.ntiles; tile += gridDim.x, it++) {
-      int b = it & 1;
+    const int b = eg;
+    for (int it = eg;; it += 2) {
+      const long long tile = blockIdx.x + (long long)it * G;
+      if (tile >= P.ntiles) break;
       // warp-uniform outcome: the TMEM loads below are .sync.aligned
       bool ready = __all_sync(FULL_MASK, mbar_wait(tfull0 + 8 * b, (it >> 1) & 1, abort_flag));
       if (!ready) {
@@ -421,7 +449,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) hall_tc_kernel(TcParams P) {
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
-  if (warp == 1) tc_dealloc(tmem, TMEM_COLS);
+  if (warp == TC_MMA_WARP) tc_dealloc(tmem, TMEM_COLS);
 }
 
 size_t tc_smem_bytes(int nparts) {

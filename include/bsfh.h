@@ -87,6 +87,38 @@ int bs_hall_filter_dev(bs_ctx *ctx, const uint64_t *d_bits, long long npairs, in
 int bs_hall_tc_dump_dev(bs_ctx *ctx, const uint64_t *d_bits, long long npairs, int mode,
                         float *d_acc);
 
+/* ---- C,D stream ----------------------------------------------------------------------
+ * Replaces count_pairs22(n, px, py, false, pinC, pinD, leaves, ok, &sink, m, stop)
+ * (src/solver/wz_match.cpp:678-784) for a batch of cells of one context (L = n): every
+ * Thm 2.2 mirror-quad (C,D) whose class sums equal the cell's targets and that passes the
+ * Thm 2.4 test, in the reference's emission order (cells in the given order, then DFS
+ * order), with per-cell counts equal to the reference's CDSTAT dfs_nodes, leaves and
+ * hall_ok (CELLSIZE) figures. */
+typedef struct {
+  int8_t tx[8], ty[8];  /* class-sum targets of C and D at modulus m (entries >= m unused) */
+  int32_t pinX, pinY;   /* zero-sum pins: C[0] = +1 / D[0] = +1 (wz_match.cpp:1526-1527) */
+} bs_cell;
+
+typedef struct {
+  int32_t m;                 /* class modulus of the cells: 3 or 6 */
+  int32_t rev;               /* WZ_FH_STREAM_REV: reversed branch order */
+  int32_t endpos;            /* WZ_FH_ENDPOS: positive-product endpoint quad */
+  int32_t cd_prune;          /* WZ_FH_CD_PRUNE: only 0 (the optional prunes are host-only) */
+  int32_t hall_mode;         /* BS_HALL_* form of the leaf test */
+  int32_t reserved;
+  long long target_prefixes; /* subtrees to split the batch into (0 = 262144) */
+  long long leaf_chunk;      /* leaves buffered per round (0 = 2^24) */
+  long long survivor_cap;    /* device survivor buffer (0 = 2^22) */
+} bs_stream_opts;
+
+typedef struct { long long nodes, leaves, ok; } bs_cell_stats;
+
+/* out_words: 2 words (C, D) per survivor, out_cell (may be NULL): the survivor's cell index.
+ * *nout always receives the survivor count; BS_ERR_CAP when it exceeds out_cap. */
+int bs_cd_stream(bs_ctx *ctx, const bs_cell *cells, int ncells, const bs_stream_opts *opt,
+                 uint64_t *out_words, uint32_t *out_cell, long long out_cap, long long *nout,
+                 bs_cell_stats *stats);
+
 /* Pack host int8 sequences (rows of L values) into words. No device work. */
 int bs_pack_rows(const int8_t *seq, long long rows, int L, uint64_t *words);
 

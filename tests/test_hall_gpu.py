@@ -74,28 +74,35 @@ def test_hall_stream_leaves_parity(gpu, oracle, n):
     rng = np.random.default_rng(n)
     rows_all, pass_all = [], []
     c, d = sig[2], sig[3]
-    for _ in range(40):
-        # a random class-sum cell (m=6) with the right totals
-        tx = _rand_cell(n, c, rng)
-        ty = _rand_cell(n, d, rng)
+    cells = [(x, y) for x in _all_cells(n, c) for y in _all_cells(n, d)]
+    rng.shuffle(cells)
+    total = 0
+    for tx, ty in cells:
         rows, flags, _ = oracle.cd_stream(n, tx, ty, m=6, keep_all=True, cap=20000)
         if len(rows):
             rows_all.append(rows)
             pass_all.append(flags)
+            total += len(rows)
+        if total > 30000:
+            break
     rows = np.concatenate(rows_all)
     ref = np.concatenate(pass_all)
-    assert len(rows) > 100
+    assert len(rows) > 20
     words = pack(rows)
     ctx = _ctx(n, sig)
     _check_all_modes(ctx, words, ref)
 
 
-def _rand_cell(n, total, rng, m=6):
+def _all_cells(n, total, m=6):
+    """Every class-sum vector (m classes) of a +-1 sequence of length n summing to total."""
+    import itertools
     cnt = [len(range(c, n, m)) for c in range(m)]
-    while True:
-        v = [int(rng.integers(0, k + 1)) * 2 - k for k in cnt]
-        if sum(v) == total:
-            return v
+    out = []
+    for v in itertools.product(*[range(-k, k + 1, 2) for k in cnt[:-1]]):
+        last = total - sum(v)
+        if abs(last) <= cnt[-1] and (last + cnt[-1]) % 2 == 0:
+            out.append(list(v) + [last])
+    return out
 
 
 def _exact_psd(words, n, oracle):
