@@ -48,6 +48,17 @@ class CellStats(C.Structure):
     _fields_ = [("nodes", C.c_longlong), ("leaves", C.c_longlong), ("ok", C.c_longlong)]
 
 
+class AbCand(C.Structure):
+    _fields_ = [("c", C.c_uint64), ("d", C.c_uint64), ("row_off", C.c_longlong),
+                ("nrows", C.c_int32), ("reserved", C.c_int32)]
+
+
+class AbOpts(C.Structure):
+    _fields_ = [("budget", C.c_longlong), ("outer_k", C.c_int32), ("early", C.c_int32),
+                ("canon", C.c_int32), ("m", C.c_int32), ("first_hit", C.c_int32),
+                ("reserved", C.c_int32), ("max_seconds", C.c_double)]
+
+
 _lib = None
 
 # (name, restype, argtypes) for every entry point of include/bsfh.h
@@ -70,6 +81,13 @@ SIGNATURES = {
     "bs_cd_stream": (C.c_int, [C.c_void_p, C.POINTER(Cell), C.c_int, C.POINTER(StreamOpts),
                                C.c_void_p, C.c_void_p, C.c_longlong, C.POINTER(C.c_longlong),
                                C.POINTER(CellStats)]),
+    "bs_flat_topk": (C.c_int, [C.c_void_p, C.c_void_p, C.c_longlong, C.c_longlong, C.c_longlong,
+                               C.c_void_p, C.c_void_p, C.POINTER(C.c_longlong)]),
+    "bs_flat_topk_dev": (C.c_int, [C.c_void_p, C.c_void_p, C.c_longlong, C.c_longlong,
+                                   C.c_longlong, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "bs_complete_ab_batch": (C.c_int, [C.c_void_p, C.POINTER(AbCand), C.c_longlong, C.c_void_p,
+                                       C.c_longlong, C.POINTER(AbOpts), C.c_void_p, C.c_void_p,
+                                       C.c_void_p, C.c_void_p]),
     "bs_ctx_timing": (C.c_int, [C.c_void_p, C.c_int]),
     "bs_ctx_timing_read": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_longlong),
                                      C.POINTER(C.c_longlong)]),

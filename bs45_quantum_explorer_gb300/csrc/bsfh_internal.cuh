@@ -48,9 +48,11 @@ struct bs_ctx {
   long long timed_launches; // launches of the timed kernels
   long long launches;       // every kernel this context has launched
   void *stream_bufs;        // C,D stream buffers (cd_stream.cu)
+  void *ab_bufs;            // A,B completion buffers (complete.cu)
 };
 
 void bs_stream_free(bs_ctx *ctx);
+void bs_ab_free(bs_ctx *ctx);
 
 // Record the start / stop event of one timed kernel launch on the context stream.
 void bs_timed_begin(bs_ctx *ctx);

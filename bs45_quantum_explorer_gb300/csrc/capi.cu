@@ -222,6 +222,7 @@ extern "C" void bs_ctx_destroy(bs_ctx *ctx) {
   cudaFree(ctx->d_status); cudaFree(ctx->d_count);
   cudaFree(ctx->d_bits); cudaFree(ctx->d_pass); cudaFree(ctx->d_rows); cudaFree(ctx->d_unc);
   bs_stream_free(ctx);
+  bs_ab_free(ctx);
   if (ctx->h_pinned) cudaFreeHost(ctx->h_pinned);
   if (ctx->ev[0])
     for (int i = 0; i < 2 * 512; i++) cudaEventDestroy(ctx->ev[i]);

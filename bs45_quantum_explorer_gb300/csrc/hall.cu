@@ -11,6 +11,7 @@
 #include <stdint.h>
 
 #include "bsfh_internal.cuh"
+#include "tmem_ld.cuh"
 
 namespace {
 
@@ -90,6 +91,50 @@ __global__ void __launch_bounds__(512) hall_fp64_kernel(
   }
   unsigned warp_sum = __reduce_add_sync(FULL_MASK, local);
   if ((threadIdx.x & 31) == 0 && warp_sum) atomicAdd(pass_count, (unsigned long long)warp_sum);
+}
+
+// The reference's test of one pair at one angle row jr (true = this angle rejects the pair).
+__device__ __forceinline__ bool angle_rejects(uint64_t x, uint64_t y, int L, double lim,
+                                              const double *c, const double *s) {
+  double rx, ix, ry, iy;
+  dft64(x, L, c, s, rx, ix);
+  double fx = __dadd_rn(__dmul_rn(rx, rx), __dmul_rn(ix, ix));
+  if (fx > lim) return true;
+  dft64(y, L, c, s, ry, iy);
+  double ry2 = __dmul_rn(ry, ry), iy2 = __dmul_rn(iy, iy);
+  double fy = __dadd_rn(ry2, iy2);
+  double fp = __dadd_rn(__dadd_rn(fx, ry2), iy2);
+  return fy > lim || fp > lim;
+}
+
+// Margin-band recheck: one warp per listed pair, the 200 angles split over the lanes. The
+// pair passes when no angle rejects it, the same conjunction the reference evaluates.
+__global__ void __launch_bounds__(256) hall_fp64_recheck_kernel(
+    const uint64_t *__restrict__ bits, const unsigned *__restrict__ list,
+    const unsigned long long *list_len, unsigned long long list_cap, int L, double lim,
+    const double *__restrict__ gc, const double *__restrict__ gs, uint8_t *__restrict__ pass,
+    unsigned long long *pass_count) {
+  extern __shared__ double tabs[];
+  double *sc = tabs, *ss = tabs + 200 * L;
+  load_tables64(sc, ss, gc, gs, L);
+  const unsigned long long n = *list_len;
+  const long long count = (long long)(n < list_cap ? n : list_cap);
+  const int lane = threadIdx.x & 31;
+  const long long w0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+  unsigned local = 0;
+  for (long long t = w0; t < count; t += nw) {
+    const long long p = (long long)list[t];
+    const uint64_t x = bits[2 * p], y = bits[2 * p + 1];
+    bool rej = false;
+    for (int jr = lane; jr < 200 && !rej; jr += 32) rej = angle_rejects(x, y, L, lim, sc + jr * L, ss + jr * L);
+    const bool ok = !__any_sync(FULL_MASK, rej);
+    if (lane == 0) {
+      pass[p] = ok ? 1 : 0;
+      local += ok;
+    }
+  }
+  if (lane == 0 && local) atomicAdd(pass_count, (unsigned long long)local);
 }
 
 __global__ void pack_kernel(const int8_t *__restrict__ rows, long long nrows, int L,
@@ -211,67 +256,6 @@ __device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
   d |= (uint64_t)1 << 46;
   d |= (uint64_t)2 << 61;
   return d;
-}
-
-// Two 32-column TMEM loads (Re chunk and Im chunk) for this warp's 32 lanes, then wait.
-__device__ __forceinline__ void tmem_ld_2x32(uint32_t ta, uint32_t tb, float *re, float *im) {
-  uint32_t r[64];
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
-      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%64];\n\t"
-      "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
-      "{%32,%33,%34,%35,%36,%37,%38,%39,%40,%41,%42,%43,%44,%45,%46,%47,"
-      "%48,%49,%50,%51,%52,%53,%54,%55,%56,%57,%58,%59,%60,%61,%62,%63}, [%65];\n\t"
-      "tcgen05.wait::ld.sync.aligned;"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
-        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
-        "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]),
-        "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
-        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]),
-        "=r"(r[31]), "=r"(r[32]), "=r"(r[33]), "=r"(r[34]), "=r"(r[35]), "=r"(r[36]),
-        "=r"(r[37]), "=r"(r[38]), "=r"(r[39]), "=r"(r[40]), "=r"(r[41]), "=r"(r[42]),
-        "=r"(r[43]), "=r"(r[44]), "=r"(r[45]), "=r"(r[46]), "=r"(r[47]), "=r"(r[48]),
-        "=r"(r[49]), "=r"(r[50]), "=r"(r[51]), "=r"(r[52]), "=r"(r[53]), "=r"(r[54]),
-        "=r"(r[55]), "=r"(r[56]), "=r"(r[57]), "=r"(r[58]), "=r"(r[59]), "=r"(r[60]),
-        "=r"(r[61]), "=r"(r[62]), "=r"(r[63])
-      : "r"(ta), "r"(tb)
-      : "memory");
-#pragma unroll
-  for (int k = 0; k < 32; k++) {
-    re[k] = __uint_as_float(r[k]);
-    im[k] = __uint_as_float(r[32 + k]);
-  }
-}
-
-__device__ __forceinline__ void tmem_ld_2x8(uint32_t ta, uint32_t tb, float *re, float *im) {
-  uint32_t r[16];
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%16];\n\t"
-      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%8,%9,%10,%11,%12,%13,%14,%15}, [%17];\n\t"
-      "tcgen05.wait::ld.sync.aligned;"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
-        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
-        "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-      : "r"(ta), "r"(tb)
-      : "memory");
-#pragma unroll
-  for (int k = 0; k < 8; k++) {
-    re[k] = __uint_as_float(r[k]);
-    im[k] = __uint_as_float(r[8 + k]);
-  }
-}
-
-__device__ __forceinline__ float pair_max(const float *re, const float *im, int cnt, float mx) {
-#pragma unroll
-  for (int k = 0; k < 32; k++) {
-    if (k < cnt) {
-      float f = fmaf(re[k], re[k], im[k] * im[k]);
-      float g = __shfl_xor_sync(FULL_MASK, f, 1);
-      mx = fmaxf(mx, f + g);
-    }
-  }
-  return mx;
 }
 
 __global__ void __launch_bounds__(TC_THREADS, 1) hall_tc_kernel(TcParams P) {
@@ -413,20 +397,29 @@ __global__ void __launch_bounds__(TC_THREADS, 1) hall_tc_kernel(TcParams P) {
       const uint32_t t0 = tmem + lane_off + (uint32_t)(b * 256);
       float mx = 0.0f;
       float *dump = P.dump ? P.dump + (size_t)(tile * 128 + row) * BS_TC_COLS : nullptr;
-#pragma unroll 1
-      for (int c0 = 0; c0 < 96; c0 += 32) {
-        float re[32], im[32];
-        tmem_ld_2x32(t0 + c0, t0 + BS_TC_IM0 + c0, re, im);
-        mx = pair_max(re, im, 32, mx);
+      {  // angles 0..63: Re columns 0..63 and Im columns 104..167 in one load round
+        float v[128];
+        tmem_ld_64_64(t0, t0 + BS_TC_IM0, v);
+#pragma unroll
+        for (int k = 0; k < 64; k++) {
+          float f = fmaf(v[k], v[k], v[64 + k] * v[64 + k]);
+          float g = __shfl_xor_sync(FULL_MASK, f, 1);
+          mx = fmaxf(mx, f + g);
+        }
         if (dump)
-          for (int k = 0; k < 32; k++) { dump[c0 + k] = re[k]; dump[BS_TC_IM0 + c0 + k] = im[k]; }
+          for (int k = 0; k < 64; k++) { dump[k] = v[k]; dump[BS_TC_IM0 + k] = v[64 + k]; }
       }
-      {
-        float re[32], im[32];
-        tmem_ld_2x8(t0 + 96, t0 + BS_TC_IM0 + 96, re, im);
-        mx = pair_max(re, im, 8, mx);
+      {  // angles 64..103 (101..103 are zero padding)
+        float v[80];
+        tmem_ld_32_8_32_8(t0 + 64, t0 + 96, t0 + BS_TC_IM0 + 64, t0 + BS_TC_IM0 + 96, v);
+#pragma unroll
+        for (int k = 0; k < 40; k++) {
+          float f = fmaf(v[k], v[k], v[40 + k] * v[40 + k]);
+          float g = __shfl_xor_sync(FULL_MASK, f, 1);
+          mx = fmaxf(mx, f + g);
+        }
         if (dump)
-          for (int k = 0; k < 8; k++) { dump[96 + k] = re[k]; dump[BS_TC_IM0 + 96 + k] = im[k]; }
+          for (int k = 0; k < 40; k++) { dump[64 + k] = v[k]; dump[BS_TC_IM0 + 64 + k] = v[40 + k]; }
       }
       tc_fence_before();
       __syncwarp();
@@ -477,15 +470,24 @@ static int launch_fp64(bs_ctx *ctx, const uint64_t *d_bits, long long npairs,
   if (!attr_done) {
     CK(cudaFuncSetAttribute(hall_fp64_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                             (int)(sizeof(double) * 2 * 200 * BS_MAXL)));
+    CK(cudaFuncSetAttribute(hall_fp64_recheck_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                            (int)(sizeof(double) * 2 * 200 * BS_MAXL)));
     attr_done = true;
   }
-  int grid = list ? ctx->num_sms : bs_grid_for(npairs, 512, ctx->num_sms);
-  const bool timed = (list == nullptr);  // the FP64 form is the dominant kernel only when alone
-  if (timed) bs_timed_begin(ctx); else ctx->launches++;
-  hall_fp64_kernel<<<grid, 512, smem, ctx->stream>>>(d_bits, npairs, list, list_len, list_cap, L,
+  if (list) {  // the margin band after the tensor-core kernel: a warp per pair on every SM
+    ctx->launches++;
+    hall_fp64_recheck_kernel<<<ctx->num_sms, 256, smem, ctx->stream>>>(
+        d_bits, list, list_len, list_cap, L, ctx->lim, ctx->d_cos, ctx->d_sin, d_pass,
+        ctx->d_count + 1);
+    CK(cudaGetLastError());
+    return BS_OK;
+  }
+  int grid = bs_grid_for(npairs, 512, ctx->num_sms);
+  bs_timed_begin(ctx);  // the FP64 form alone: it is the dominant kernel of the call
+  hall_fp64_kernel<<<grid, 512, smem, ctx->stream>>>(d_bits, npairs, nullptr, nullptr, 0, L,
                                                      ctx->lim, ctx->d_cos, ctx->d_sin, d_pass,
                                                      ctx->d_count + 1);
-  if (timed) bs_timed_end(ctx);
+  bs_timed_end(ctx);
   CK(cudaGetLastError());
   return BS_OK;
 }

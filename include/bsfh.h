@@ -119,6 +119,52 @@ int bs_cd_stream(bs_ctx *ctx, const bs_cell *cells, int ncells, const bs_stream_
                  uint64_t *out_words, uint32_t *out_cell, long long out_cap, long long *nout,
                  bs_cell_stats *stats);
 
+/* ---- per-cell flattest-k keep -----------------------------------------------------------
+ * Replaces flat_score (src/solver/wz_match.cpp:2569-2583) and drain()'s stable_sort by score
+ * with its front-only cut (wz_match.cpp:2656-2714): a cell's survivors (2 words each, in
+ * stream order) are split into batches of buf_cap; each batch is ordered by flat score, ties
+ * in stream order, and its first `keep` entries (keep <= 0: all) are returned as stream
+ * indices in `order`, batch after batch, with their scores (may be NULL). *nkept = entries. */
+int bs_flat_topk(bs_ctx *ctx, const uint64_t *words, long long nsurv, long long buf_cap,
+                 long long keep, int64_t *order, int32_t *scores, long long *nkept);
+/* Device-resident form: d_order / d_scores_sorted hold ceil(nsurv/buf_cap) slots of
+ * min(keep, buf_cap) entries each (a short last batch leaves its tail unwritten); d_scores
+ * (nsurv) receives every survivor's score. Enqueued on the context stream. */
+int bs_flat_topk_dev(bs_ctx *ctx, const uint64_t *d_words, long long nsurv, long long buf_cap,
+                     long long keep, int64_t *d_order, int32_t *d_scores_sorted,
+                     int32_t *d_scores);
+
+/* ---- A,B completion --------------------------------------------------------------------
+ * Replaces fh_complete_ab(C, D) (src/solver/wz_match.cpp:1298-1341) with fh_ab_search
+ * (:1171-1293) over a batch: for candidate i, verdict[i] and nodes[i] equal the reference's
+ * return value and charged node count (the fh_nodes_total delta), and on a hit A,B (n+1
+ * int8 each, at A + i*(n+1)) equal its first completion. The cell's allowed A,B class-sum
+ * rows (AbpRow, wz_match.cpp:970: k[8] then r[8], int8) are rows[row_off .. row_off+nrows);
+ * nrows = 0 runs unconstrained (FH_ABP == nullptr). Verdicts: 0 hit, 1 prefilter, 2 clean
+ * no, 3 budget abort, 4 NPAF recheck failed, -1 not run (after an earlier hit in first_hit
+ * mode, or stopped), -2 wall limit (max_seconds) reached. */
+typedef struct {
+  uint64_t c, d;        /* packed C, D (length n) */
+  long long row_off;    /* first allowed row of the candidate's cell */
+  int32_t nrows;        /* allowed rows (0 = unconstrained), <= 65535 */
+  int32_t reserved;
+} bs_ab_cand;
+
+typedef struct {
+  long long budget;     /* WZ_FH_AB_BUDGET: nodes per candidate, 0 = exact */
+  int32_t outer_k;      /* WZ_FH_OUTER_K: 0 | 2 | 3 */
+  int32_t early;        /* WZ_FH_EARLY_CHECK (reference default 1) */
+  int32_t canon;        /* root + reversal canonicalisation (1 unless WZ_FH_NO_CANON) */
+  int32_t m;            /* class modulus of the rows: 3 or 6 */
+  int32_t first_hit;    /* 1: candidates after the lowest-index hit are not run */
+  int32_t reserved;
+  double max_seconds;   /* per-candidate wall limit on the device (0 = none) */
+} bs_ab_opts;
+
+int bs_complete_ab_batch(bs_ctx *ctx, const bs_ab_cand *cands, long long ncand,
+                         const int8_t *rows, long long nrows_total, const bs_ab_opts *opt,
+                         int32_t *verdict, long long *nodes, int8_t *A, int8_t *B);
+
 /* Pack host int8 sequences (rows of L values) into words. No device work. */
 int bs_pack_rows(const int8_t *seq, long long rows, int L, uint64_t *words);
 
