@@ -176,6 +176,37 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+# Built-in cells of the ORDER=3 lists (orbit canon + quad switch): (n, sig, px, py, raw index)
+STREAM_CELLS = {
+    "n30": (30, (1, 7, 6, 6), [-1, 1, 1, 1, 1, 3], [-1, 1, 1, 1, 5, -1], 3005),
+    "n42": (42, (7, 11, 0, 0), [-1, -1, 1, 1, 1, -1], [-1, -3, 1, 1, 3, -1], 3056),
+}
+
+
+def run_stream_only(args):
+    """Stream one cell (the DFS, the Hall filter of its leaves and the ordering) and print
+    the per-cell counts and rates."""
+    import torch
+    from bs45_quantum_explorer_gb300 import build_library
+    build_library()
+    from bs45_quantum_explorer_gb300.hall import Context
+    from bs45_quantum_explorer_gb300.stream import cd_stream
+    n, sig, px, py, pi = STREAM_CELLS[args.stream_only]
+    ctx = Context(n, sig)
+    cd_stream(ctx, [(px, py)], m=6, as_words=True)  # warm-up
+    torch.cuda.synchronize()
+    ctx.timing(True)
+    t0 = time.perf_counter()
+    surv, _, st = cd_stream(ctx, [(px, py)], m=6, as_words=True)
+    dt = time.perf_counter() - t0
+    kms, kl, _ = ctx.timing_read()
+    print(json.dumps({"workload": f"C,D stream, n={n} sig={sig} raw cell {pi} px={px} py={py}",
+                      "dfs_nodes": st[0]["nodes"], "leaves": st[0]["leaves"], "survivors": len(surv),
+                      "seconds": dt, "nodes_per_s": st[0]["nodes"] / dt, "device_kernel_ms": kms,
+                      "timed_launches": kl}), flush=True)
+    ctx.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -186,6 +217,8 @@ def main():
     ap.add_argument("--mode", default="tc_fp16", choices=["tc_fp16", "tc_bf16x2", "fp64"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true")
+    ap.add_argument("--stream-only", choices=["n30", "n42"], default=None,
+                    help="stream one built-in cell only (a small case for profiling)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     rank = env_int("RANK", 0)
@@ -194,6 +227,9 @@ def main():
 
     if args.impl == "reference":
         run_reference(args, rank, world)
+        return
+    if args.stream_only:
+        run_stream_only(args)
         return
 
     import numpy as np
@@ -363,6 +399,27 @@ def main():
                                  "max_psd_err_vs_fp64": float(np.abs(f_tc - f64).max()),
                                  "psd_err_bound_at_limit": float(4 * st["quant_err"] * (4 * N + 2.5) ** 0.5
                                                                  + 4 * st["quant_err"] ** 2)}
+        # ---- search nodes/s: the C,D stream of one n = 42 cell (DFS + Hall + order) ----
+        from bs45_quantum_explorer_gb300.stream import cd_stream
+        cell42 = ([-1, -1, 1, 1, 1, -1], [-1, -3, 1, 1, 3, -1])  # ORDER=3 raw cell 3056, sig (7,11,0,0)
+        cd_stream(ctx, [cell42], m=6, as_words=True)  # warm-up (frontier, buffers)
+        torch.cuda.synchronize()
+        ctx.timing(True)
+        t0 = time.perf_counter()
+        surv, _, sst = cd_stream(ctx, [cell42], m=6, as_words=True)
+        dt = time.perf_counter() - t0
+        dfs_ms, dfs_launches, _ = ctx.timing_read()
+        ctx.timing(False)
+        nodes = sst[0]["nodes"]
+        line["search"] = {
+            "workload": "C,D stream of the n=42 cell px=(-1,-1,1,1,1,-1) py=(-1,-3,1,1,3,-1) "
+                        "(ORDER=3 raw cell 3056 of sig (7,11,0,0)), whole cell",
+            "dfs_nodes": nodes, "leaves": sst[0]["leaves"], "survivors": int(len(surv)),
+            "seconds": dt, "nodes_per_s": nodes / dt, "leaves_per_s": sst[0]["leaves"] / dt,
+            "device_kernel_ms": dfs_ms, "timed_launches": dfs_launches,
+            "device_nodes_per_s": nodes / (dfs_ms * 1e-3) if dfs_ms > 0 else None,
+            "reference_single_core": "14,736,335,258 nodes, 448,271,835 leaves, 5,613 survivors "
+                                     "in 348.9 s (42.2 M nodes/s, one Xeon core; run interrupted)"}
         if not args.no_cpu_baseline:
             rate, samp, thr, dt = cpu_hall_rate(os.cpu_count() or 1)
             line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": thr, "kind": "port",

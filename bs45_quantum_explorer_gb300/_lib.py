@@ -39,7 +39,7 @@ class Cell(C.Structure):
 
 class StreamOpts(C.Structure):
     _fields_ = [("m", C.c_int32), ("rev", C.c_int32), ("endpos", C.c_int32),
-                ("cd_prune", C.c_int32), ("hall_mode", C.c_int32), ("reserved", C.c_int32),
+                ("cd_prune", C.c_int32), ("hall_mode", C.c_int32), ("ab_side", C.c_int32),
                 ("target_prefixes", C.c_longlong), ("leaf_chunk", C.c_longlong),
                 ("survivor_cap", C.c_longlong)]
 
@@ -88,6 +88,10 @@ SIGNATURES = {
     "bs_complete_ab_batch": (C.c_int, [C.c_void_p, C.POINTER(AbCand), C.c_longlong, C.c_void_p,
                                        C.c_longlong, C.POINTER(AbOpts), C.c_void_p, C.c_void_p,
                                        C.c_void_p, C.c_void_p]),
+    "bs_npaf_verify_batch": (C.c_int, [C.c_void_p, C.c_void_p, C.c_longlong, C.c_void_p]),
+    "bs_join_quads": (C.c_int, [C.c_void_p, C.c_void_p, C.c_longlong, C.c_void_p, C.c_longlong,
+                                C.c_void_p, C.c_longlong, C.POINTER(C.c_longlong),
+                                C.POINTER(C.c_longlong)]),
     "bs_ctx_timing": (C.c_int, [C.c_void_p, C.c_int]),
     "bs_ctx_timing_read": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_longlong),
                                      C.POINTER(C.c_longlong)]),

@@ -31,7 +31,8 @@ struct bs_ctx {
   cudaStream_t own_stream, stream;
   double *d_cos, *d_sin;     // FP64 Hall tables, [200][BS_MAXL] for j = 1..200
   double lim;                // 4n + 2 + 0.5
-  bs_hall_tc_form tc[3];     // index by mode (0 unused)
+  bs_hall_tc_form tc[3];     // index by mode (0 unused), sequences of length n (C,D)
+  bs_hall_tc_form tc_ab[3];  // the same for length n+1 (A,B)
   int *d_status;             // device-side error word
   unsigned long long *d_count;  // [0] uncertain count, [1] pass count, [2] overflow flag
   // scratch for the host-buffer entry points
@@ -52,6 +53,9 @@ struct bs_ctx {
 };
 
 void bs_stream_free(bs_ctx *ctx);
+// Hall filter of pairs of length L (n for C,D, n+1 for A,B), device buffers, no stats.
+int bs_hall_dev_len(bs_ctx *ctx, const uint64_t *d_bits, long long npairs, int mode,
+                    uint8_t *d_pass, int L);
 void bs_ab_free(bs_ctx *ctx);
 
 // Record the start / stop event of one timed kernel launch on the context stream.

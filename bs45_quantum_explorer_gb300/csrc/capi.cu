@@ -100,9 +100,8 @@ static inline int angle_of(int u) { return u < 100 ? u + 1 : 200; }
 // Every quantised value is exact in its format, so Re_q = sum_i x_i q(t_i) is a multiple of
 // the quantum with fewer than 24 significant bits and the FP32 accumulator holds it exactly.
 // e = max over angles of sum_i |t_i - q(t_i)| bounds |Re - Re_q| and |Im - Im_q|.
-static int build_tc_form(bs_ctx *ctx, const double *ct, const double *st, int mode) {
-  bs_hall_tc_form &F = ctx->tc[mode];
-  const int L = ctx->n;  // C,D length
+static int build_tc_form(bs_ctx *ctx, const double *ct, const double *st, int mode, int L,
+                         bs_hall_tc_form &F) {
   F.nparts = (mode == BS_HALL_TC_BF16X2) ? 2 : 1;
   F.fmt = (mode == BS_HALL_TC_BF16X2) ? 1 : 0;
   size_t bytes = (size_t)F.nparts * BS_TC_PART_BYTES;
@@ -205,8 +204,12 @@ extern "C" int bs_ctx_create(int n, int a, int b, int c, int d, int device, bs_c
     if (e1 == cudaSuccess) e1 = cudaMalloc(&ctx->d_count, sizeof(unsigned long long) * 8);
     if (e1 != cudaSuccess) rc = bs_cuda_fail(e1);
   }
-  if (rc == BS_OK) rc = build_tc_form(ctx, ct, st, BS_HALL_TC_FP16);
-  if (rc == BS_OK) rc = build_tc_form(ctx, ct, st, BS_HALL_TC_BF16X2);
+  // both sequence lengths: C,D (n) and A,B (n+1)
+  if (rc == BS_OK) rc = build_tc_form(ctx, ct, st, BS_HALL_TC_FP16, n, ctx->tc[BS_HALL_TC_FP16]);
+  if (rc == BS_OK) rc = build_tc_form(ctx, ct, st, BS_HALL_TC_BF16X2, n, ctx->tc[BS_HALL_TC_BF16X2]);
+  if (rc == BS_OK) rc = build_tc_form(ctx, ct, st, BS_HALL_TC_FP16, n + 1, ctx->tc_ab[BS_HALL_TC_FP16]);
+  if (rc == BS_OK)
+    rc = build_tc_form(ctx, ct, st, BS_HALL_TC_BF16X2, n + 1, ctx->tc_ab[BS_HALL_TC_BF16X2]);
   free(ct); free(st); free(gc); free(gs);
   if (rc != BS_OK) { bs_ctx_destroy(ctx); return rc; }
   *out = ctx;
@@ -218,7 +221,10 @@ extern "C" void bs_ctx_destroy(bs_ctx *ctx) {
   cudaSetDevice(ctx->device);
   if (ctx->own_stream) cudaStreamSynchronize(ctx->own_stream);
   cudaFree(ctx->d_cos); cudaFree(ctx->d_sin);
-  for (int m = 1; m < 3; m++) cudaFree(ctx->tc[m].d_image);
+  for (int m = 1; m < 3; m++) {
+    cudaFree(ctx->tc[m].d_image);
+    cudaFree(ctx->tc_ab[m].d_image);
+  }
   cudaFree(ctx->d_status); cudaFree(ctx->d_count);
   cudaFree(ctx->d_bits); cudaFree(ctx->d_pass); cudaFree(ctx->d_rows); cudaFree(ctx->d_unc);
   bs_stream_free(ctx);

@@ -46,8 +46,10 @@ struct Saved {
 };
 
 struct CdParams {
-  int L, m, half, rev, ns0;
-  const uint8_t *cls;  // per depth d: class of position d (low nibble) and of L-1-d (high)
+  int L, m, half;
+  uint64_t feas_mask;   // bit 6 of every used class byte
+  const void *fx;       // QuadFx[32][16]: effect of branch kk at depth d (reversal applied)
+  const uint64_t *posmask;  // [32]: bits of positions d and L-1-d
   const CellDev *cells;
   const Prefix *prefixes;
   long long nprefix;
@@ -66,8 +68,6 @@ struct CdParams {
   int *status;
 };
 
-// quad tables: index -> (v0, v1, v2, v3) as sign bits (bit 3 = v0 ... bit 0 = v3)
-__constant__ uint8_t kPos[8] = {0, 3, 5, 6, 9, 10, 12, 15};
 
 __device__ __forceinline__ int getdig(const uint64_t dig[2], int d) {
   return (int)((dig[d >> 4] >> (4 * (d & 15))) & 15);
@@ -77,71 +77,77 @@ __device__ __forceinline__ void setdig(uint64_t dig[2], int d, int v) {
   dig[w] = (dig[w] & ~(15ULL << s)) | ((uint64_t)v << s);
 }
 
-// Per-class remaining differences dx = tx - px, dy = ty - py and remaining slots rem, packed
-// as 8-bit fields (bias 64) of three words; class c occupies bits 8c..8c+7.
+// Per-class feasibility as four "slack" words: for each class c (byte c, bias 64)
+//   rem - dx, rem + dx, rem - dy, rem + dy,  dx = tx - px, dy = ty - py, rem = free slots.
+// The reference's capacity test |dx| <= rem and |dy| <= rem holds exactly when all four are
+// >= 0, i.e. when bit 6 of every used byte is set (bytes stay in [0, 127]: a valid node has
+// slack in [0, 22] and one quad lowers a byte by at most 4). Its parity test is invariant
+// once the root passes, so the walk needs neither. A quad at depth d, branch kk, changes the
+// words by a constant: dsl[d][kk][0..3] (host-built), and the sequences by bits bx/by.
 struct Walk {
-  uint64_t dx, dy, rem;
+  uint64_t s0, s1, s2, s3;
   uint64_t X, Y;
+};
+
+struct QuadFx {  // the effect of branch kk at depth d
+  int64_t ds[4];
+  uint64_t bx, by;
 };
 
 __device__ __forceinline__ int fld(uint64_t w, int c) { return (int)((w >> (8 * c)) & 255) - 64; }
 
-// Apply (sign = -1) or remove (sign = +1) quad q at depth d; returns nothing. The quad's values
-// are v = +1 for a set bit, -1 otherwise.
-__device__ __forceinline__ void apply_quad(Walk &w, const uint8_t *cls, int L, int d, uint32_t q,
-                                           int sign) {
-  const int c1 = cls[d] & 15, c2 = cls[d] >> 4;
-  int a = (q & 8) ? 1 : -1, b = (q & 4) ? 1 : -1, c = (q & 2) ? 1 : -1, e = (q & 1) ? 1 : -1;
-  // dx -= a (place) / dx += a (remove), rem -= 1 / += 1
-  w.dx += (uint64_t)(int64_t)(sign * a) << (8 * c1);
-  w.dy += (uint64_t)(int64_t)(sign * b) << (8 * c1);
-  w.dx += (uint64_t)(int64_t)(sign * c) << (8 * c2);
-  w.dy += (uint64_t)(int64_t)(sign * e) << (8 * c2);
-  w.rem += (uint64_t)(int64_t)sign << (8 * c1);
-  w.rem += (uint64_t)(int64_t)sign << (8 * c2);
-  const uint64_t m1 = 1ULL << d, m2 = 1ULL << (L - 1 - d);
-  if (sign < 0) {
-    if (a > 0) w.X |= m1;
-    if (b > 0) w.Y |= m1;
-    if (c > 0) w.X |= m2;
-    if (e > 0) w.Y |= m2;
-  } else {
-    w.X &= ~(m1 | m2);
-    w.Y &= ~(m1 | m2);
-  }
+__device__ __forceinline__ void place(Walk &w, const QuadFx &f) {
+  w.s0 += (uint64_t)f.ds[0];
+  w.s1 += (uint64_t)f.ds[1];
+  w.s2 += (uint64_t)f.ds[2];
+  w.s3 += (uint64_t)f.ds[3];
+  w.X |= f.bx;
+  w.Y |= f.by;
 }
-
-__device__ __forceinline__ bool cap_ok(const Walk &w, int c) {
-  int r = fld(w.rem, c), x = fld(w.dx, c), y = fld(w.dy, c);
-  return x >= -r && x <= r && y >= -r && y <= r;
+__device__ __forceinline__ void unplace(Walk &w, const QuadFx &f, uint64_t posmask) {
+  w.s0 -= (uint64_t)f.ds[0];
+  w.s1 -= (uint64_t)f.ds[1];
+  w.s2 -= (uint64_t)f.ds[2];
+  w.s3 -= (uint64_t)f.ds[3];
+  w.X &= ~posmask;
+  w.Y &= ~posmask;
 }
-
-__device__ __forceinline__ uint32_t quad_at(int d, int kk, int ns0, int rev) {
-  if (d == 0) {
-    int k = rev ? ns0 - 1 - kk : kk;
-    return ns0 == 16 ? (uint32_t)k : kPos[k];
-  }
-  int k = rev ? 7 - kk : kk;
-  return kPos[k];
+__device__ __forceinline__ bool feasible(const Walk &w, uint64_t M) {
+  return ((w.s0 & w.s1 & w.s2 & w.s3) & M) == M;
 }
 
 __device__ __forceinline__ void init_walk(Walk &w, const CellDev &cell, int L, int m) {
-  w.dx = w.dy = w.rem = 0;
+  w.s0 = w.s1 = w.s2 = w.s3 = 0x4040404040404040ULL;
   for (int c = 0; c < m; c++) {
-    int cnt = (L - c + m - 1) / m;  // positions p < L with p % m == c
-    w.dx |= (uint64_t)(cell.tx[c] + 64) << (8 * c);
-    w.dy |= (uint64_t)(cell.ty[c] + 64) << (8 * c);
-    w.rem |= (uint64_t)(cnt + 64) << (8 * c);
+    const int cnt = (L - c + m - 1) / m;  // positions p < L with p % m == c
+    const uint64_t clear = ~(0xFFULL << (8 * c));
+    w.s0 = (w.s0 & clear) | ((uint64_t)(cnt - cell.tx[c] + 64) << (8 * c));
+    w.s1 = (w.s1 & clear) | ((uint64_t)(cnt + cell.tx[c] + 64) << (8 * c));
+    w.s2 = (w.s2 & clear) | ((uint64_t)(cnt - cell.ty[c] + 64) << (8 * c));
+    w.s3 = (w.s3 & clear) | ((uint64_t)(cnt + cell.ty[c] + 64) << (8 * c));
   }
   w.X = w.Y = 0;
 }
 
+// leaf bits for an odd length: the free middle takes the only values that make the cell exact,
+// dx and dy of the middle class (each +-1)
+__device__ __forceinline__ void middle_bits(const Walk &w, int half, int cm, uint64_t &lx, uint64_t &ly) {
+  const int dx = (fld(w.s1, cm) - fld(w.s0, cm)) / 2, dy = (fld(w.s3, cm) - fld(w.s2, cm)) / 2;
+  if (dx > 0) lx |= 1ULL << half;
+  if (dy > 0) ly |= 1ULL << half;
+}
+
 __global__ void __launch_bounds__(256) cd_dfs_kernel(CdParams P) {
-  __shared__ uint8_t cls[64];
-  if (threadIdx.x < 64) cls[threadIdx.x] = P.cls[threadIdx.x];
+  __shared__ QuadFx fx[32][16];
+  __shared__ uint64_t posm[32];
+  for (int t = threadIdx.x; t < 32 * 16; t += blockDim.x)
+    fx[t >> 4][t & 15] = ((const QuadFx *)P.fx)[t];
+  if (threadIdx.x < 32) posm[threadIdx.x] = P.posmask[threadIdx.x];
   __syncthreads();
   const int lane = threadIdx.x & 31;
   const int L = P.L, m = P.m, half = P.half;
+  const uint64_t M = P.feas_mask;
+  const int cm = half % m;
   bool have = false;
   uint32_t prefix = 0, cell = 0, seq = 0;
   int D = 0, d = 0, kk = 0;
@@ -184,8 +190,7 @@ __global__ void __launch_bounds__(256) cd_dfs_kernel(CdParams P) {
         pending = false;
       }
       init_walk(w, P.cells[cell], L, m);
-      for (int t = 0; t < d; t++)
-        apply_quad(w, cls, L, t, quad_at(t, getdig(dig, t), P.ns0, P.rev), -1);
+      for (int t = 0; t < d; t++) place(w, fx[t][getdig(dig, t)]);
       have = true;
     }
 
@@ -194,16 +199,12 @@ __global__ void __launch_bounds__(256) cd_dfs_kernel(CdParams P) {
     uint64_t lx = 0, ly = 0;
     if (pending) {
       // the leaf that could not be written last time (its node is already counted)
-      const uint32_t q = quad_at(d, kk, P.ns0, P.rev);
-      apply_quad(w, cls, L, d, q, -1);
+      const QuadFx &f = fx[d][kk];
+      place(w, f);
       lx = w.X;
       ly = w.Y;
-      if (L & 1) {
-        const int cm = half % m;
-        if (fld(w.dx, cm) > 0) lx |= 1ULL << half;
-        if (fld(w.dy, cm) > 0) ly |= 1ULL << half;
-      }
-      apply_quad(w, cls, L, d, q, +1);
+      if (L & 1) middle_bits(w, half, cm, lx, ly);
+      unplace(w, f, posm[d]);
       emit = true;
     } else if (kk == 8) {
       if (d == D) {
@@ -211,26 +212,21 @@ __global__ void __launch_bounds__(256) cd_dfs_kernel(CdParams P) {
       } else {
         d--;
         kk = getdig(dig, d);
-        apply_quad(w, cls, L, d, quad_at(d, kk, P.ns0, P.rev), +1);
+        unplace(w, fx[d][kk], posm[d]);
         kk++;
       }
     } else {
-      const uint32_t q = quad_at(d, kk, P.ns0, P.rev);
-      apply_quad(w, cls, L, d, q, -1);
+      const QuadFx &f = fx[d][kk];
+      place(w, f);
       nodes++;
-      const int c1 = cls[d] & 15, c2 = cls[d] >> 4;
-      if (!cap_ok(w, c1) || !cap_ok(w, c2)) {
-        apply_quad(w, cls, L, d, q, +1);
+      if (!feasible(w, M)) {
+        unplace(w, f, posm[d]);
         kk++;
       } else if (d + 1 == half) {
         lx = w.X;
         ly = w.Y;
-        if (L & 1) {  // the free middle takes the only values that make the cell exact
-          const int cm = half % m;
-          if (fld(w.dx, cm) > 0) lx |= 1ULL << half;
-          if (fld(w.dy, cm) > 0) ly |= 1ULL << half;
-        }
-        apply_quad(w, cls, L, d, q, +1);
+        if (L & 1) middle_bits(w, half, cm, lx, ly);
+        unplace(w, f, posm[d]);
         emit = true;
       } else {
         setdig(dig, d, kk);
@@ -331,19 +327,20 @@ __global__ void compact_kernel(const uint64_t *__restrict__ words, const uint64_
 // Host: frontier of each cell in the reference's order
 // ------------------------------------------------------------------------------------
 struct HostQuads {
-  int all[16][4], pos[8][4];
+  int all[16][4], pos[8][4], neg[8][4];
   HostQuads() {
-    int np = 0;
+    int np = 0, nn = 0;
     for (int i = 0; i < 16; i++) {
       int v[4] = {(i & 8) ? 1 : -1, (i & 4) ? 1 : -1, (i & 2) ? 1 : -1, (i & 1) ? 1 : -1};
       memcpy(all[i], v, sizeof v);
       if (v[0] * v[1] * v[2] * v[3] == 1) memcpy(pos[np++], v, sizeof v);
+      else memcpy(neg[nn++], v, sizeof v);
     }
   }
 };
 
 struct Frontier {
-  int L, m, half, D, rev, endpos, pinX, pinY, ns0;
+  int L, m, half, D, rev, root, pinX, pinY, ns0;
   int tot[8], px[8], py[8], placed[8];
   const int8_t *tx, *ty;
   const HostQuads *Q;
@@ -369,7 +366,7 @@ struct Frontier {
       return;
     }
     const int i1 = d, i2 = L - 1 - d, c1 = i1 % m, c2 = i2 % m;
-    const int(*S)[4] = (d == 0) ? (endpos ? Q->pos : Q->all) : Q->pos;
+    const int(*S)[4] = (d == 0) ? (root == 2 ? Q->neg : (root == 1 ? Q->pos : Q->all)) : Q->pos;
     const int ns = (d == 0) ? ns0 : 8;
     for (int kk = 0; kk < ns; kk++) {
       int k = rev ? ns - 1 - kk : kk;
@@ -406,7 +403,8 @@ struct StreamBufs {
   unsigned long long *cell_stats = nullptr; long long cell_stats_cap = 0;
   unsigned *nsaved = nullptr;
   int *full = nullptr;
-  uint8_t *cls = nullptr;
+  QuadFx *fx = nullptr;      // [32][16] branch effects
+  uint64_t *posm = nullptr;  // [32] position masks
 };
 
 static StreamBufs *bufs_of(bs_ctx *ctx) {
@@ -420,7 +418,8 @@ void bs_stream_free(bs_ctx *ctx) {
   cudaFree(b->cells); cudaFree(b->prefixes); cudaFree(b->saved[0]); cudaFree(b->saved[1]);
   cudaFree(b->leaf_words); cudaFree(b->leaf_keys); cudaFree(b->leaf_pass);
   cudaFree(b->surv_words); cudaFree(b->surv_keys); cudaFree(b->counters);
-  cudaFree(b->cell_stats); cudaFree(b->nsaved); cudaFree(b->full); cudaFree(b->cls);
+  cudaFree(b->cell_stats); cudaFree(b->nsaved); cudaFree(b->full); cudaFree(b->fx);
+  cudaFree(b->posm);
   delete b;
   ctx->stream_bufs = nullptr;
 }
@@ -430,9 +429,12 @@ extern "C" int bs_cd_stream(bs_ctx *ctx, const bs_cell *cells, int ncells, const
                             long long *nout, bs_cell_stats *stats) {
   if (!ctx || !cells || ncells <= 0 || !opt || !nout) return BS_ERR_ARG;
   if (out_cap > 0 && !out_words) return BS_ERR_ARG;
-  const int L = ctx->n, m = opt->m;
+  // the C,D side has length n; the A,B side (ab_side, the reference's abSide) length n+1 with
+  // negative-product root quads (wz_match.cpp:766-768)
+  const int L = opt->ab_side ? ctx->n1 : ctx->n, m = opt->m;
+  const int root_kind = opt->ab_side ? 2 : (opt->endpos ? 1 : 0);
   if (m != 3 && m != 6) return BS_ERR_ARG;
-  if (L > 63 || L / 2 > 31) return BS_ERR_ARG;
+  if (L > 64 || L / 2 > 31) return BS_ERR_ARG;
   if (opt->cd_prune != 0) return BS_ERR_ARG;  // optional CD_PRUNE is not built on the device
   int hall_mode = opt->hall_mode;
   if (hall_mode < BS_HALL_FP64 || hall_mode > BS_HALL_TC_BF16X2) return BS_ERR_ARG;
@@ -449,9 +451,9 @@ extern "C" int bs_cd_stream(bs_ctx *ctx, const bs_cell *cells, int ncells, const
   for (int ci = 0; ci < ncells; ci++) {
     const bs_cell &c = cells[ci];
     Frontier F;
-    F.L = L; F.m = m; F.half = half; F.rev = opt->rev; F.endpos = opt->endpos;
+    F.L = L; F.m = m; F.half = half; F.rev = opt->rev; F.root = root_kind;
     F.pinX = c.pinX; F.pinY = c.pinY;
-    F.ns0 = opt->endpos ? 8 : 16;
+    F.ns0 = root_kind == 0 ? 16 : 8;
     for (int k = 0; k < m; k++) {
       F.tot[k] = 0;
       for (int p = k; p < L; p += m) F.tot[k]++;
@@ -502,7 +504,8 @@ extern "C" int bs_cd_stream(bs_ctx *ctx, const bs_cell *cells, int ncells, const
     CK(cudaMalloc(&B->counters, sizeof(unsigned long long) * 8));
     CK(cudaMalloc(&B->nsaved, sizeof(unsigned) * 2));
     CK(cudaMalloc(&B->full, sizeof(int)));
-    CK(cudaMalloc(&B->cls, 64));
+    CK(cudaMalloc(&B->fx, sizeof(QuadFx) * 32 * 16));
+    CK(cudaMalloc(&B->posm, sizeof(uint64_t) * 32));
   }
   long long surv_cap = opt->survivor_cap > 0 ? opt->survivor_cap : (1LL << 22);
   if (!rc) {
@@ -523,11 +526,34 @@ extern "C" int bs_cd_stream(bs_ctx *ctx, const bs_cell *cells, int ncells, const
     memset(&hc[ci], 0, sizeof(CellDev));
     for (int k = 0; k < m; k++) { hc[ci].tx[k] = cells[ci].tx[k]; hc[ci].ty[k] = cells[ci].ty[k]; }
   }
-  uint8_t cls[64];
-  memset(cls, 0, sizeof cls);
-  for (int dd = 0; dd < half && dd < 64; dd++) cls[dd] = (uint8_t)((dd % m) | (((L - 1 - dd) % m) << 4));
+  // effect of branch kk at depth d: slack deltas of the two classes it touches and the sign
+  // bits it sets; the branch -> quad map includes the reversal and the root table.
+  std::vector<QuadFx> fxh(32 * 16);
+  std::vector<uint64_t> posm(32, 0);
+  memset(fxh.data(), 0, sizeof(QuadFx) * fxh.size());
+  for (int dd = 0; dd < half && dd < 32; dd++) {
+    const int i1 = dd, i2 = L - 1 - dd, c1 = i1 % m, c2 = i2 % m;
+    posm[dd] = (1ULL << i1) | (1ULL << i2);
+    const int(*S)[4] = (dd == 0) ? (root_kind == 2 ? Q.neg : (root_kind == 1 ? Q.pos : Q.all)) : Q.pos;
+    const int ns = (dd == 0 && root_kind == 0) ? 16 : 8;
+    for (int kk = 0; kk < ns; kk++) {
+      const int k = opt->rev ? ns - 1 - kk : kk;
+      const int a = S[k][0], b = S[k][1], c = S[k][2], e = S[k][3];
+      QuadFx &f = fxh[dd * 16 + kk];
+      // placing value v of C in class c: rem -= 1, dx -= v -> (rem - dx) += v - 1, (rem + dx) -= v + 1
+      f.ds[0] = (int64_t)(a - 1) * (1LL << (8 * c1)) + (int64_t)(c - 1) * (1LL << (8 * c2));
+      f.ds[1] = (int64_t)(-a - 1) * (1LL << (8 * c1)) + (int64_t)(-c - 1) * (1LL << (8 * c2));
+      f.ds[2] = (int64_t)(b - 1) * (1LL << (8 * c1)) + (int64_t)(e - 1) * (1LL << (8 * c2));
+      f.ds[3] = (int64_t)(-b - 1) * (1LL << (8 * c1)) + (int64_t)(-e - 1) * (1LL << (8 * c2));
+      f.bx = (a > 0 ? 1ULL << i1 : 0) | (c > 0 ? 1ULL << i2 : 0);
+      f.by = (b > 0 ? 1ULL << i1 : 0) | (e > 0 ? 1ULL << i2 : 0);
+    }
+  }
+  uint64_t feas = 0;
+  for (int c = 0; c < m; c++) feas |= 0x40ULL << (8 * c);
   cudaStream_t s = ctx->stream;
-  CK(cudaMemcpyAsync(B->cls, cls, sizeof cls, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(B->fx, fxh.data(), sizeof(QuadFx) * fxh.size(), cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(B->posm, posm.data(), sizeof(uint64_t) * 32, cudaMemcpyHostToDevice, s));
   CK(cudaMemcpyAsync(B->cells, hc.data(), sizeof(CellDev) * ncells, cudaMemcpyHostToDevice, s));
   if (nprefix)
     CK(cudaMemcpyAsync(B->prefixes, prefixes.data(), sizeof(Prefix) * nprefix, cudaMemcpyHostToDevice, s));
@@ -544,8 +570,10 @@ extern "C" int bs_cd_stream(bs_ctx *ctx, const bs_cell *cells, int ncells, const
     CK(cudaMemsetAsync(B->full, 0, sizeof(int), s));
     CK(cudaMemsetAsync(B->counters + 1, 0, sizeof(unsigned long long), s));
     CdParams P;
-    P.L = L; P.m = m; P.half = half; P.rev = opt->rev; P.ns0 = opt->endpos ? 8 : 16;
-    P.cls = B->cls;
+    P.L = L; P.m = m; P.half = half;
+    P.feas_mask = feas;
+    P.fx = B->fx;
+    P.posmask = B->posm;
     P.cells = B->cells; P.prefixes = B->prefixes; P.nprefix = nprefix;
     P.next_prefix = B->counters;
     P.saved_in = B->saved[cur]; P.nsaved_in = nsaved;
@@ -566,7 +594,7 @@ extern "C" int bs_cd_stream(bs_ctx *ctx, const bs_cell *cells, int ncells, const
     if ((int)nsv > saved_cap) return BS_ERR_INTERNAL;
     long long nleaf = (long long)std::min<unsigned long long>(leaf_count, (unsigned long long)leaf_cap);
     if (nleaf > 0) {
-      int r2 = bs_hall_filter_dev(ctx, B->leaf_words, nleaf, hall_mode, B->leaf_pass, nullptr);
+      int r2 = bs_hall_dev_len(ctx, B->leaf_words, nleaf, hall_mode, B->leaf_pass, L);
       if (r2) return r2;
       ctx->launches++;
       compact_kernel<<<bs_grid_for(nleaf, 256, 8 * ctx->num_sms), 256, 0, s>>>(

@@ -463,8 +463,7 @@ size_t tc_smem_bytes(int nparts) {
 
 static int launch_fp64(bs_ctx *ctx, const uint64_t *d_bits, long long npairs,
                        const unsigned *list, const unsigned long long *list_len,
-                       unsigned long long list_cap, uint8_t *d_pass) {
-  const int L = ctx->n;
+                       unsigned long long list_cap, uint8_t *d_pass, int L) {
   size_t smem = sizeof(double) * 2 * 200 * L;
   static bool attr_done = false;
   if (!attr_done) {
@@ -493,15 +492,15 @@ static int launch_fp64(bs_ctx *ctx, const uint64_t *d_bits, long long npairs,
 }
 
 static int launch_tc(bs_ctx *ctx, int mode, const uint64_t *d_bits, long long npairs,
-                     uint8_t *d_pass, float *d_dump) {
-  const bs_hall_tc_form &F = ctx->tc[mode];
+                     uint8_t *d_pass, float *d_dump, int L) {
+  const bs_hall_tc_form &F = (L == ctx->n) ? ctx->tc[mode] : ctx->tc_ab[mode];
   TcParams P;
   P.bits = d_bits;
   P.npairs = npairs;
   P.ntiles = (npairs + 63) / 64;
   P.image = F.d_image;
   P.nparts = F.nparts;
-  P.ksteps = (ctx->n + 15) / 16;
+  P.ksteps = (L + 15) / 16;
   // instruction descriptor: D fp32, A/B format, both K-major, N = 208, M = 128
   P.idesc = (1u << 4) | ((uint32_t)F.fmt << 7) | ((uint32_t)F.fmt << 10) |
             ((uint32_t)(BS_TC_COLS >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
@@ -531,7 +530,8 @@ static int launch_tc(bs_ctx *ctx, int mode, const uint64_t *d_bits, long long np
 }
 
 static int hall_dev(bs_ctx *ctx, const uint64_t *d_bits, long long npairs, int mode,
-                    uint8_t *d_pass, bs_hall_stats *stats, float *d_dump) {
+                    uint8_t *d_pass, bs_hall_stats *stats, float *d_dump, int L) {
+  if (!ctx || (L != ctx->n && L != ctx->n1)) return BS_ERR_ARG;
   if (!ctx || npairs < 0 || (npairs && (!d_bits || !d_pass))) return BS_ERR_ARG;
   if (mode < BS_HALL_FP64 || mode > BS_HALL_TC_BF16X2) return BS_ERR_ARG;
   if (npairs >= (1LL << 32)) return BS_ERR_ARG;
@@ -539,15 +539,15 @@ static int hall_dev(bs_ctx *ctx, const uint64_t *d_bits, long long npairs, int m
   CK(cudaMemsetAsync(ctx->d_count, 0, sizeof(unsigned long long) * 8, ctx->stream));
   if (npairs > 0) {
     if (mode == BS_HALL_FP64) {
-      int rc = launch_fp64(ctx, d_bits, npairs, nullptr, nullptr, 0, d_pass);
+      int rc = launch_fp64(ctx, d_bits, npairs, nullptr, nullptr, 0, d_pass, L);
       if (rc) return rc;
     } else {
       int rc = bs_ensure_dev((void **)&ctx->d_unc, &ctx->unc_cap, npairs, sizeof(unsigned));
       if (rc) return rc;
-      rc = launch_tc(ctx, mode, d_bits, npairs, d_pass, d_dump);
+      rc = launch_tc(ctx, mode, d_bits, npairs, d_pass, d_dump, L);
       if (rc) return rc;
       rc = launch_fp64(ctx, d_bits, npairs, ctx->d_unc, ctx->d_count,
-                       (unsigned long long)ctx->unc_cap, d_pass);
+                       (unsigned long long)ctx->unc_cap, d_pass, L);
       if (rc) return rc;
     }
   }
@@ -571,9 +571,10 @@ static int hall_dev(bs_ctx *ctx, const uint64_t *d_bits, long long npairs, int m
       stats->reject_above = ctx->lim;
       stats->quant_err = 0.0;
     } else {
-      stats->pass_below = ctx->tc[mode].pass_below;
-      stats->reject_above = ctx->tc[mode].reject_above;
-      stats->quant_err = ctx->tc[mode].quant_err;
+      const bs_hall_tc_form &F = (L == ctx->n) ? ctx->tc[mode] : ctx->tc_ab[mode];
+      stats->pass_below = F.pass_below;
+      stats->reject_above = F.reject_above;
+      stats->quant_err = F.quant_err;
     }
   }
   return BS_OK;
@@ -581,7 +582,12 @@ static int hall_dev(bs_ctx *ctx, const uint64_t *d_bits, long long npairs, int m
 
 extern "C" int bs_hall_filter_dev(bs_ctx *ctx, const uint64_t *d_bits, long long npairs, int mode,
                                   uint8_t *d_pass, bs_hall_stats *stats) {
-  return hall_dev(ctx, d_bits, npairs, mode, d_pass, stats, nullptr);
+  return hall_dev(ctx, d_bits, npairs, mode, d_pass, stats, nullptr, ctx ? ctx->n : 0);
+}
+
+int bs_hall_dev_len(bs_ctx *ctx, const uint64_t *d_bits, long long npairs, int mode,
+                    uint8_t *d_pass, int L) {
+  return hall_dev(ctx, d_bits, npairs, mode, d_pass, nullptr, nullptr, L);
 }
 
 extern "C" int bs_hall_tc_dump_dev(bs_ctx *ctx, const uint64_t *d_bits, long long npairs, int mode,
@@ -591,7 +597,7 @@ extern "C" int bs_hall_tc_dump_dev(bs_ctx *ctx, const uint64_t *d_bits, long lon
   int rc = bs_ensure_dev((void **)&ctx->d_pass, &ctx->pass_cap, npairs, 1);
   if (rc) return rc;
   bs_hall_stats st;
-  return hall_dev(ctx, d_bits, npairs, mode, ctx->d_pass, &st, d_acc);
+  return hall_dev(ctx, d_bits, npairs, mode, ctx->d_pass, &st, d_acc, ctx->n);
 }
 
 static int hall_host(bs_ctx *ctx, const void *src, bool packed, long long npairs, int mode,
@@ -620,7 +626,7 @@ static int hall_host(bs_ctx *ctx, const void *src, bool packed, long long npairs
     CK(cudaGetLastError());
   }
   bs_hall_stats st;
-  rc = hall_dev(ctx, ctx->d_bits, npairs, mode, ctx->d_pass, &st, nullptr);
+  rc = hall_dev(ctx, ctx->d_bits, npairs, mode, ctx->d_pass, &st, nullptr, ctx->n);
   if (rc) return rc;
   CK(cudaMemcpyAsync(pass, ctx->d_pass, (size_t)npairs, cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));

@@ -417,6 +417,21 @@ int main(int argc, char **argv) {
   printf("[firsthit] profiles=%zu m=%d order=%d ab_budget=%lld max_cand=%lld score_max=%lld shard=%d/%d\n",
          cells.size(), fh_m, prof_order, budget, max_cand, score_max, fh_shard, fh_nshard);
   fflush(stdout);
+  // WZ_FH_LIST_CELLS=lo,hi: print raw cells [lo, hi) of the final list (with their orbit-kept
+  // flag) and exit; a tool for choosing benchmark and canary cells.
+  if (const char *e = env("WZ_FH_LIST_CELLS")) {
+    std::vector<int> r = parse_list(e);
+    long long lo = r.size() > 0 ? r[0] : 0, hi = r.size() > 1 ? r[1] : (long long)cells.size();
+    for (long long pi = std::max(0LL, lo); pi < std::min(hi, (long long)cells.size()); pi++) {
+      std::string k = cell_key(cells[pi].px, cells[pi].py);
+      printf("CELL pi=%lld kept=%d px=", pi, (!orbit_canon || keep_set.count(k)) ? 1 : 0);
+      for (int c = 0; c < fh_m; c++) printf("%d%s", cells[pi].px[c], c + 1 < fh_m ? "," : "");
+      printf(" py=");
+      for (int c = 0; c < fh_m; c++) printf("%d%s", cells[pi].py[c], c + 1 < fh_m ? "," : "");
+      printf("\n");
+    }
+    return 0;
+  }
 
   // ---------------------------------------------------------------- lane settings
   long long cand = 0, pre_rej = 0, score_rej = 0, clean_no = 0, aborted_ct = 0;

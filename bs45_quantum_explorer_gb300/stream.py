@@ -25,17 +25,20 @@ def make_cells(cells, m, pins=None):
 
 
 def cd_stream(ctx, cells, m=6, pins=None, rev=False, endpos=False, hall_mode="tc_fp16",
-              target_prefixes=0, leaf_chunk=0, survivor_cap=0, cap=None, as_words=False):
+              target_prefixes=0, leaf_chunk=0, survivor_cap=0, cap=None, as_words=False,
+              ab_side=False):
     """cells: list of (tx, ty). Returns (survivors, cell index per survivor, per-cell stats).
 
-    survivors: int8 [k, 2, n] (or uint64 words [k, 2] with as_words) in stream order.
+    survivors: int8 [k, 2, L] (or uint64 words [k, 2] with as_words) in stream order, L = n
+    (C,D) or n+1 with ab_side (the reference's abSide stream of A,B pairs).
     stats: list of dicts {nodes, leaves, ok} per cell (the reference's CDSTAT dfs_nodes and
     CELLSIZE leaves / hall_ok)."""
     ncells = len(cells)
     arr = make_cells(cells, m, pins)
     opt = StreamOpts(m=m, rev=int(rev), endpos=int(endpos), cd_prune=0,
-                     hall_mode=MODES[hall_mode], reserved=0, target_prefixes=target_prefixes,
-                     leaf_chunk=leaf_chunk, survivor_cap=survivor_cap)
+                     hall_mode=MODES[hall_mode], ab_side=int(ab_side),
+                     target_prefixes=target_prefixes, leaf_chunk=leaf_chunk,
+                     survivor_cap=survivor_cap)
     stats = (CellStats * ncells)()
     nout = C.c_longlong(0)
     cap = cap if cap is not None else (1 << 20)
@@ -53,8 +56,34 @@ def cd_stream(ctx, cells, m=6, pins=None, rev=False, endpos=False, hall_mode="tc
     k = nout.value
     st = [dict(nodes=s.nodes, leaves=s.leaves, ok=s.ok) for s in stats]
     words = words[:k]
-    out = words if as_words else unpack(words, ctx.n)
+    out = words if as_words else unpack(words, ctx.n + (1 if ab_side else 0))
     return out, cidx[:k], st
 
 
-__all__ = ["cd_stream", "make_cells", "BsError", "BS_OK"]
+def npaf_verify(ctx, quads):
+    """quads: uint64 words [k, 4] (A, B, C, D). Returns max_s |NPAF(s)| per quad (0 = valid)."""
+    quads = np.ascontiguousarray(quads, np.uint64).reshape(-1, 4)
+    out = np.zeros(max(1, len(quads)), np.int32)
+    check(lib().bs_npaf_verify_batch(ctx.h, quads.ctypes.data, len(quads), out.ctypes.data),
+          "bs_npaf_verify_batch")
+    return out[:len(quads)]
+
+
+def join_quads(ctx, cd_words, ab_words, cap=1 << 16):
+    """Every (A,B) x (C,D) pairing with AB[s] = -CD[s] for all s, verified exactly on the GPU.
+    Returns (quads uint64 [k, 4], key_hits)."""
+    cd_words = np.ascontiguousarray(cd_words, np.uint64).reshape(-1, 2)
+    ab_words = np.ascontiguousarray(ab_words, np.uint64).reshape(-1, 2)
+    nout, hits = C.c_longlong(0), C.c_longlong(0)
+    while True:
+        out = np.zeros((max(1, cap), 4), np.uint64)
+        rc = lib().bs_join_quads(ctx.h, cd_words.ctypes.data, len(cd_words), ab_words.ctypes.data,
+                                 len(ab_words), out.ctypes.data, cap, C.byref(nout), C.byref(hits))
+        if rc == -6 and nout.value > cap:
+            cap = nout.value
+            continue
+        check(rc, "bs_join_quads")
+        return out[:nout.value], hits.value
+
+
+__all__ = ["cd_stream", "make_cells", "npaf_verify", "join_quads", "BsError", "BS_OK"]

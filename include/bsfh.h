@@ -105,7 +105,7 @@ typedef struct {
   int32_t endpos;            /* WZ_FH_ENDPOS: positive-product endpoint quad */
   int32_t cd_prune;          /* WZ_FH_CD_PRUNE: only 0 (the optional prunes are host-only) */
   int32_t hall_mode;         /* BS_HALL_* form of the leaf test */
-  int32_t reserved;
+  int32_t ab_side;           /* 1: stream the A,B side (length n+1, negative-product root quads) */
   long long target_prefixes; /* subtrees to split the batch into (0 = 262144) */
   long long leaf_chunk;      /* leaves buffered per round (0 = 2^24) */
   long long survivor_cap;    /* device survivor buffer (0 = 2^22) */
@@ -164,6 +164,22 @@ typedef struct {
 int bs_complete_ab_batch(bs_ctx *ctx, const bs_ab_cand *cands, long long ncand,
                          const int8_t *rows, long long nrows_total, const bs_ab_opts *opt,
                          int32_t *verdict, long long *nodes, int8_t *A, int8_t *B);
+
+/* ---- exact verification and the autocorrelation join ------------------------------------
+ * bs_npaf_verify_batch replaces npaf_at over s = 1..n+1 (src/solver/wz_match.cpp:184-192;
+ * tools/verify_npaf.py:42-53) for a batch: quads are 4 words (A, B of length n+1, C, D of
+ * length n); maxabs[i] = max_s |NPAF(s)|, 0 for a base sequence. */
+int bs_npaf_verify_batch(bs_ctx *ctx, const uint64_t *quads, long long count, int32_t *maxabs);
+
+/* Replaces the WZ_JOIN22 hash join (src/solver/wz_match.cpp:2894-3104): every (A,B) of
+ * ab_words (length n+1) is matched against every (C,D) of cd_words (length n) with the same
+ * autocorrelation vector AB[s] = -CD[s], s = 1..n; each match is verified with the exact
+ * NPAF on the device and written as a quad (4 words). All matches are returned (the
+ * reference keeps one C,D per key). BS_ERR_CAP when more than out_cap; *nout = matches,
+ * *key_hits = equal-key pairings examined. */
+int bs_join_quads(bs_ctx *ctx, const uint64_t *cd_words, long long ncd, const uint64_t *ab_words,
+                  long long nab, uint64_t *out_quads, long long out_cap, long long *nout,
+                  long long *key_hits);
 
 /* Pack host int8 sequences (rows of L values) into words. No device work. */
 int bs_pack_rows(const int8_t *seq, long long rows, int L, uint64_t *words);

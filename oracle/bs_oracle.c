@@ -235,7 +235,7 @@ void or_outer_tables(uint8_t *outer2, uint8_t *outer3) {
 typedef struct {
   int n, L, m, half;
   const int *tx, *ty;
-  int pinX, pinY, rev, endpos;
+  int pinX, pinY, rev, endpos, ab_side;
   int cd_root, cd_reach, root_mod;
   int blk_r[3], blk_s[3], blk_of[6];
   int qrem[64][3];
@@ -317,8 +317,9 @@ static void cd_rec(cd_state *S, int d) {
     return;
   }
   int i1 = d, i2 = L - 1 - d, c1 = i1 % m, c2 = i2 % m;
-  const int(*Q)[4] = (d == 0) ? (S->endpos ? QPOS : QALL) : QPOS;
-  int ns = (d == 0 && !S->endpos) ? 16 : 8;
+  /* wz_match.cpp:766-768: the A,B side roots at the negative-product quads */
+  const int(*Q)[4] = (d == 0) ? (S->ab_side ? QNEG : (S->endpos ? QPOS : QALL)) : QPOS;
+  int ns = (d == 0 && !S->ab_side && !S->endpos) ? 16 : 8;
   for (int kk = 0; kk < ns; kk++) {
     int k = S->rev ? ns - 1 - kk : kk;
     if (d == 0 && S->pinX && Q[k][0] != 1) continue;
@@ -341,12 +342,13 @@ long long or_cd_stream(int n, int L, int m, const int *tx, const int *ty, int pi
                        uint8_t *out_pass, long long cap, or_stream_stats *st) {
   tables_init();
   cd_state *S = (cd_state *)calloc(1, sizeof(cd_state));
+  S->ab_side = (L == n + 1);  /* the A,B side is the one of length n+1 */
   S->n = n; S->L = L; S->m = m; S->half = L / 2;
   S->tx = tx; S->ty = ty;
   S->pinX = pinX; S->pinY = pinY; S->rev = rev; S->endpos = endpos;
   for (int c = 0; c < m; c++) S->tot[c] = class_count(L, c, m);
   /* CD_PRUNE set-up, wz_match.cpp:696-711 */
-  int cd_ok = (m == 6 && L % 2 == 0);
+  int cd_ok = (!S->ab_side && m == 6 && L % 2 == 0);
   S->cd_root = cd_ok && (cd_prune & 1);
   S->cd_reach = cd_ok && (cd_prune & 2);
   if (cd_ok && cd_prune) {

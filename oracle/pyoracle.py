@@ -108,12 +108,13 @@ def autocorr_key(X, Y, n, negate):
 
 
 def cd_stream(n, tx, ty, m=6, pinX=False, pinY=False, rev=False, endpos=False, cd_prune=0,
-              keep_all=False, cap=None):
-    """Returns (rows [k, 2, n] int8 in DFS order, pass flags, stats dict)."""
+              keep_all=False, cap=None, ab_side=False):
+    """Returns (rows [k, 2, L] int8 in DFS order, pass flags, stats dict); L = n, or n+1 for
+    the A,B side (ab_side)."""
     tx = np.ascontiguousarray(tx, np.int32)
     ty = np.ascontiguousarray(ty, np.int32)
     st = StreamStats()
-    L = n
+    L = n + 1 if ab_side else n
     dummy = np.zeros(2 * L, np.int8)
     dp = np.zeros(1, np.uint8)
     total = lib().or_cd_stream(n, L, m, tx, ty, int(pinX), int(pinY), int(rev), int(endpos),

@@ -40,6 +40,7 @@ unsigned long long refh_autocorr_key(const int *X, const int *Y, int L, int nega
 long long refh_stream(int L, const int *tx, const int *ty, int m, int pinX, int pinY, int rev,
                       int endpos, int cd_prune, int hall_fast, int *out, long long cap,
                       long long *nodes, long long *leaves, long long *ok) {
+  const bool abSide = (L == G_N1);  // the A,B side is the one of length n+1
   G_STREAM_REV = rev != 0;
   G_ENDPOS = endpos != 0;
   G_CD_PRUNE = cd_prune;
@@ -56,7 +57,7 @@ long long refh_stream(int L, const int *tx, const int *ty, int m, int pinX, int 
       };
   long long lv = 0, okc = 0;
   unsigned long long n0 = G_CD_NODES;
-  count_pairs22(L, vx, vy, false, pinX != 0, pinY != 0, lv, okc, &sink, m, nullptr);
+  count_pairs22(L, vx, vy, abSide, pinX != 0, pinY != 0, lv, okc, &sink, m, nullptr);
   *nodes = (long long)(G_CD_NODES - n0);
   *leaves = lv;
   *ok = okc;

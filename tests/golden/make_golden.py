@@ -153,8 +153,40 @@ def parse_quad(path):
     return {"file": os.path.relpath(path, REF), "n": n, "sig": sig, "A": A, "B": B, "C": Cc, "D": D}
 
 
+def ab_streams(R):
+    """A,B-side streams (count_pairs22 with abSide = true, length n+1)."""
+    rng = random.Random(0xB546)
+    cases, surv = [], []
+    for n in (6, 8, 9, 11, 12, 14, 15, 17):
+        for sig in rng.sample(classes(n), min(2, len(classes(n)))):
+            a, b, c, d = sig
+            R.refh_setup(n, a, b, c, d, 3)
+            L = n + 1
+            for m in (3, 6):
+                cells = [(x, y) for x in enum_cs(L, a, m) for y in enum_cs(L, b, m)]
+                rng.shuffle(cells)
+                for (tx, ty) in cells[:3]:
+                    rev, pin = rng.choice([(0, 0), (1, 1), (1, 0)])
+                    pinX, pinY = int(pin and a == 0), int(pin and b == 0)
+                    cap = 1 << 20
+                    out = np.zeros(cap * 2 * L, np.int32)
+                    nd, lv, ok = C.c_longlong(), C.c_longlong(), C.c_longlong()
+                    w = R.refh_stream(L, np.array(tx, np.int32), np.array(ty, np.int32), m, pinX, pinY, rev,
+                                      0, 0, 1, out, cap, C.byref(nd), C.byref(lv), C.byref(ok))
+                    off = sum(len(s) for s in surv)
+                    cases.append([n, a, b, c, d, m, rev, pinX, pinY, nd.value, lv.value, ok.value, off, w] +
+                                 list(tx) + [0] * (6 - m) + list(ty) + [0] * (6 - m))
+                    surv.append(pack(out[:w * 2 * L].reshape(w, 2, L)).reshape(-1, 2))
+    np.savez_compressed(os.path.join(HERE, "ab_streams_golden.npz"), cases=np.array(cases, np.int64),
+                        words=np.concatenate(surv) if surv else np.zeros((0, 2), np.uint64))
+    print("A,B streams", len(cases), sum(len(s) for s in surv))
+
+
 def main():
     R = load_ref()
+    if len(sys.argv) > 2 and sys.argv[2] == "ab":
+        ab_streams(R)
+        return
     rng = random.Random(0xB545)
 
     # ---- known-answer quads: banked champions and the published WZ controls ----
@@ -323,6 +355,7 @@ def main():
                        np.uint64)
     np.savez_compressed(os.path.join(HERE, "bs7_6_all.npz"), quads=quads76)
     print("BS(7,6) quads", len(quads76))
+    ab_streams(R)
 
 
 if __name__ == "__main__":

@@ -54,6 +54,20 @@ def test_streams_match_reference(oracle):
         assert (st["nodes"], st["leaves"], st["ok"]) == (nodes, leaves, ok)
 
 
+def test_ab_side_streams_match_reference(oracle):
+    g = np.load(os.path.join(G, "ab_streams_golden.npz"))
+    cases, words = g["cases"], g["words"]
+    assert len(cases) >= 50
+    for row in cases:
+        n, a, b, c, d, m, rev, pinX, pinY, nodes, leaves, ok, off, cnt = (int(x) for x in row[:14])
+        tx = [int(x) for x in row[14:14 + m]]
+        ty = [int(x) for x in row[20:20 + m]]
+        rows, _, st = oracle.cd_stream(n, tx, ty, m=m, pinX=pinX, pinY=pinY, rev=rev, ab_side=True)
+        assert len(rows) == cnt
+        assert (rows == unpack(words[off:off + cnt], n + 1)).all()
+        assert (st["nodes"], st["leaves"], st["ok"]) == (nodes, leaves, ok)
+
+
 def _complete_cases():
     g = np.load(os.path.join(G, "complete_golden.npz"))
     return g["cases"].astype(np.int64), g["cd"], g["rows"]
