@@ -48,6 +48,11 @@ class CellStats(C.Structure):
     _fields_ = [("nodes", C.c_longlong), ("leaves", C.c_longlong), ("ok", C.c_longlong)]
 
 
+class ListOpts(C.Structure):
+    _fields_ = [(f, C.c_int32) for f in ("m6", "thm211b", "thm212", "endpos", "orbit_canon",
+                                         "orbit_q", "qprune", "prof_order", "nshard", "reserved")]
+
+
 class AbCand(C.Structure):
     _fields_ = [("c", C.c_uint64), ("d", C.c_uint64), ("row_off", C.c_longlong),
                 ("nrows", C.c_int32), ("reserved", C.c_int32)]
@@ -81,6 +86,10 @@ SIGNATURES = {
     "bs_cd_stream": (C.c_int, [C.c_void_p, C.POINTER(Cell), C.c_int, C.POINTER(StreamOpts),
                                C.c_void_p, C.c_void_p, C.c_longlong, C.POINTER(C.c_longlong),
                                C.POINTER(CellStats)]),
+    "bs_cell_list": (C.c_int, [C.c_int] * 5 + [C.POINTER(ListOpts), C.POINTER(Cell), C.c_void_p,
+                               C.c_longlong, C.POINTER(C.c_longlong), C.c_char_p]),
+    "bs_ab_rows": (C.c_int, [C.c_int] * 4 + [C.POINTER(Cell), C.c_longlong, C.c_void_p, C.c_longlong,
+                             C.c_void_p, C.c_void_p, C.POINTER(C.c_longlong)]),
     "bs_flat_topk": (C.c_int, [C.c_void_p, C.c_void_p, C.c_longlong, C.c_longlong, C.c_longlong,
                                C.c_void_p, C.c_void_p, C.POINTER(C.c_longlong)]),
     "bs_flat_topk_dev": (C.c_int, [C.c_void_p, C.c_void_p, C.c_longlong, C.c_longlong,

@@ -39,10 +39,17 @@ def _stale(target, deps):
     return any(os.path.getmtime(d) > t for d in deps)
 
 
+# host translation units linked into the library (the cell algebra behind bs_cell_list and
+# bs_ab_rows); the lane's main() is built separately as bin/bs_firsthit
+LIB_HOST = ["celllist.cpp", "cell_capi.cpp"]
+HOSTFLAGS = ["-O2", "-std=c++17", "-fPIC", f"-I{INCLUDE}"]
+
+
 def build_library(force=False, verbose=False):
     os.makedirs(BUILD, exist_ok=True)
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))]
     headers.append(os.path.join(INCLUDE, "bsfh.h"))
+    host_headers = [os.path.join(HOST, f) for f in os.listdir(HOST) if f.endswith(".h")]
     jobs = []
     objs = []
     for src in _sources():
@@ -50,13 +57,19 @@ def build_library(force=False, verbose=False):
         objs.append(obj)
         if force or _stale(obj, [src] + headers):
             jobs.append([nvcc()] + NVFLAGS + ["-c", src, "-o", obj])
+    for name in LIB_HOST:
+        src = os.path.join(HOST, name)
+        obj = os.path.join(BUILD, "host_" + name[:-4] + ".o")
+        objs.append(obj)
+        if force or _stale(obj, [src, os.path.join(INCLUDE, "bsfh.h")] + host_headers):
+            jobs.append(["g++"] + HOSTFLAGS + ["-c", src, "-o", obj])
     with cf.ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 4))) as ex:
         results = list(ex.map(lambda c: subprocess.run(c, capture_output=True, text=True), jobs))
     for cmd, r in zip(jobs, results):
         if verbose and r.stderr:
             print(r.stderr)
         if r.returncode != 0:
-            raise RuntimeError(f"nvcc failed: {' '.join(cmd)}\n{r.stderr}")
+            raise RuntimeError(f"compile failed: {' '.join(cmd)}\n{r.stderr}")
     if force or jobs or _stale(LIB, objs):
         cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart"]
         r = subprocess.run(cmd, capture_output=True, text=True)
@@ -67,10 +80,7 @@ def build_library(force=False, verbose=False):
 
 def build_host(force=False):
     """Builds the drop-in lane binary bin/bs_firsthit (C++ host over libbsfh.so)."""
-    srcs = sorted(os.path.join(HOST, f) for f in os.listdir(HOST) if f.endswith(".cpp")) \
-        if os.path.isdir(HOST) else []
-    if not srcs:
-        return None
+    srcs = [os.path.join(HOST, "firsthit_main.cpp")]
     os.makedirs(BIN, exist_ok=True)
     exe = os.path.join(BIN, "bs_firsthit")
     hdrs = [os.path.join(HOST, f) for f in os.listdir(HOST) if f.endswith(".h")]

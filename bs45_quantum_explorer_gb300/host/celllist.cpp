@@ -6,6 +6,7 @@
 
 #include <algorithm>
 #include <cstdio>
+#include <cstdlib>
 
 namespace bsfh {
 
@@ -166,7 +167,7 @@ std::vector<Profile> survive_profiles3(int L, int sigX, int sigY, int n, const N
 
 std::vector<Profile> survive_profiles6(int L, int sigX, int sigY, int n, const NormSet &comp3,
                                        const NormSet &comp6, const AutoSet *comp6auto, bool thm212,
-                                       bool thm211b, size_t cap, bool *capped) {
+                                       bool thm211b, size_t cap, bool *capped, FILE *log) {
   const int tgt = 4 * n + 2;
   const bool abSide = (L == n + 1);
   const auto PX = enum_class_sums(L, sigX, 6), PY = enum_class_sums(L, sigY, 6);
@@ -196,8 +197,10 @@ std::vector<Profile> survive_profiles6(int L, int sigX, int sigY, int n, const N
       }
       out.push_back({px, py});
       if (out.size() >= cap) {
-        printf("[mod6] WARNING: profile-pair space hit cap %zu — mod-6 PROFILE space itself explodes (Gate-A data)\n", cap);
-        fflush(stdout);
+        if (log) {
+          fprintf(log, "[mod6] WARNING: profile-pair space hit cap %zu — mod-6 PROFILE space itself explodes (Gate-A data)\n", cap);
+          fflush(log);
+        }
         if (capped) *capped = true;
         return out;
       }
@@ -217,6 +220,331 @@ std::string cell_key(const Vec &px, const Vec &py) {
 uint64_t fnv_str(uint64_t h, const std::string &s) {
   for (unsigned char c : s) { h ^= c; h *= 1099511628211ULL; }
   return h;
+}
+
+// ---- the lane's cell list ----------------------------------------------------------------
+
+#define LOGF(...)                    \
+  do {                               \
+    if (log) {                       \
+      fprintf(log, __VA_ARGS__);     \
+      fflush(log);                   \
+    }                                \
+  } while (0)
+
+static long long prof_score(const Profile &p) {
+  long long s = 0;
+  for (int v : p.px) s += std::abs(v);
+  for (int v : p.py) s += std::abs(v);
+  return s;
+}
+
+typedef unsigned __int128 u128;
+
+// Orders keys as the reference orders its "v,v,...,|v,v,...," strings. All keys of one list
+// have the same number of tokens, so string order is token-by-token order, each token being a
+// value's decimal text followed by ','. rank[] numbers those tokens in string order, and a key
+// packs its 2m ranks, 8 bits each, most significant first.
+struct CellKeyOrder {
+  uint8_t rank[256];
+  int value_of[256];
+  CellKeyOrder() {
+    std::vector<std::pair<std::string, int>> t;
+    for (int v = -128; v < 128; v++) t.push_back({std::to_string(v) + ",", v});
+    std::sort(t.begin(), t.end());
+    for (int i = 0; i < 256; i++) {
+      rank[t[i].second + 128] = (uint8_t)i;
+      value_of[i] = t[i].second;
+    }
+  }
+  static const CellKeyOrder &get() {
+    static const CellKeyOrder k;
+    return k;
+  }
+  u128 pack(const int *px, const int *py, int m) const {
+    u128 k = 0;
+    for (int c = 0; c < m; c++) k = (k << 8) | rank[(px[c] + 128) & 255];
+    for (int c = 0; c < m; c++) k = (k << 8) | rank[(py[c] + 128) & 255];
+    return k;
+  }
+  std::string str(u128 k, int m) const {
+    Vec px(m), py(m);
+    for (int c = m - 1; c >= 0; c--) { py[c] = value_of[(int)(k & 255)]; k >>= 8; }
+    for (int c = m - 1; c >= 0; c--) { px[c] = value_of[(int)(k & 255)]; k >>= 8; }
+    return cell_key(px, py);
+  }
+};
+
+// class c of a reversed sequence is class (n-1-c) mod m of the original
+static inline void rev_classes(const int *p, int *q, int m, int n) {
+  for (int c = 0; c < m; c++) q[((n - 1 - c) % m + m) % m] = p[c];
+}
+
+// the quad switch Q(C,D) = (U+RV, U-RV), U=(C+D)/2, V=(C-D)/2, on class sums
+// (wz_match.cpp:1673-1712; C++ integer division, as there)
+static inline void quad_switch(int *px, int *py, int m, int n) {
+  int rx[8], ry[8];
+  rev_classes(px, rx, m, n);
+  rev_classes(py, ry, m, n);
+  for (int c = 0; c < m; c++) {
+    const int nx = (px[c] + py[c] + rx[c] - ry[c]) / 2;
+    const int ny = (px[c] + py[c] - rx[c] + ry[c]) / 2;
+    px[c] = nx;
+    py[c] = ny;
+  }
+}
+
+// Smallest key over the orbit of (px, py): negations, reversals, the swap, and with 64
+// variants also the quad switch, applied in the order of wz_match.cpp:1721-1730.
+static u128 orbit_id(const int *px0, const int *py0, int m, int n, int nvar, const CellKeyOrder &ko) {
+  u128 best = ~(u128)0;
+  for (int var = 0; var < nvar; var++) {
+    int px[8], py[8], t[8];
+    for (int c = 0; c < m; c++) { px[c] = px0[c]; py[c] = py0[c]; }
+    if (var & 32) quad_switch(px, py, m, n);
+    if (var & 1) for (int c = 0; c < m; c++) px[c] = -px[c];
+    if (var & 2) for (int c = 0; c < m; c++) py[c] = -py[c];
+    if (var & 4) { rev_classes(px, t, m, n); for (int c = 0; c < m; c++) px[c] = t[c]; }
+    if (var & 8) { rev_classes(py, t, m, n); for (int c = 0; c < m; c++) py[c] = t[c]; }
+    const u128 k = (var & 16) ? ko.pack(py, px, m) : ko.pack(px, py, m);
+    if (k < best) best = k;
+  }
+  return best;
+}
+
+int build_cell_list(int n, int SA, int SB, int SC, int SD, const ListOptions &opt, CellList &out,
+                    FILE *log) {
+  const int n1 = n + 1;
+  const bool thm211b = opt.thm211b, thm212 = opt.thm212;
+  out = CellList();
+  NormSet ab3, ab6, cd3, cd6;
+  ab3.build(n1, SA, SB, 3, n);
+  ab6.build(n1, SA, SB, 6, n);
+  cd3.build(n, SC, SD, 3, n);
+  cd6.build(n, SC, SD, 6, n);
+  AutoSet ab6a, cd6a;
+  if (thm211b) {
+    ab6a.build(n1, SA, SB, 6, n, thm212);
+    cd6a.build(n, SC, SD, 6, n, thm212);
+    out.ab_auto = ab6a.keys.size();
+    out.cd_auto = cd6a.keys.size();
+    LOGF("[thm2.11b] ENABLED — complement (autocorr,norm) tuples: A,B side %zu  C,D side %zu\n",
+         ab6a.keys.size(), cd6a.keys.size());
+  }
+  // wz_match.cpp:1388-1396: both sides' mod-3 survivors are always built and reported
+  auto abProfs = survive_profiles3(n1, SA, SB, n, cd3, cd6, thm211b ? &cd6a : nullptr, thm212, thm211b);
+  auto cdProfs = survive_profiles3(n, SC, SD, n, ab3, ab6, thm211b ? &ab6a : nullptr, thm212, thm211b);
+  out.ab_profiles = abProfs.size();
+  out.cd_profiles = cdProfs.size();
+  LOGF("[profiles] A,B side surviving: %zu   C,D side surviving: %zu\n", abProfs.size(), cdProfs.size());
+
+  std::vector<Profile> &cells = out.cells;
+  if (opt.m6) {
+    bool capped = false;
+    cells = survive_profiles6(n, SC, SD, n, ab3, ab6, thm211b ? &ab6a : nullptr, thm212, thm211b,
+                              20000000, &capped, log);
+    LOGF("[firsthit] mod-6 stream source: %zu C,D profile cells (mod-3 atoms exceed walltime at this n)\n",
+         cells.size());
+    if (cells.size() >= 20000000) {
+      LOGF("RESULT: CELL LIST TRUNCATED at the 20M cap — refusing to search an incomplete tile\n");
+      return 2;
+    }
+    if (opt.endpos) {
+      // endpoint-parity cell filter, wz_match.cpp:1598-1622
+      size_t before = cells.size();
+      std::vector<Profile> keep;
+      for (size_t i = 0; i < cells.size(); i++) {
+        const auto &p = cells[i];
+        int s = 0;
+        for (int c = 0; c < 6; c++) s += p.px[c] + p.py[c];
+        int mid = (n % 2 == 1) ? p.px[(n / 2) % 6] + p.py[(n / 2) % 6] : 0;
+        bool ok = (((s - mid) % 4) + 4) % 4 == 0;
+        if (opt.endpos_nocell) LOGF("ENDPOS_CELL idx=%zu ok=%d\n", i, ok ? 1 : 0);
+        if (ok || opt.endpos_nocell) keep.push_back(p);
+      }
+      cells.swap(keep);
+      LOGF("[endpos] cells %zu -> %zu (endpoint-parity filter%s)\n", before, cells.size(),
+           opt.endpos_nocell ? ", NOT applied: test hook" : "");
+    }
+  } else {
+    cells = cdProfs;
+  }
+  const int m = opt.m6 ? 6 : 3;
+  out.m = m;
+  // std::sort as the reference calls it: ties keep libstdc++'s introsort order, which the
+  // lane's raw cell indices (and so its checkpoints) inherit
+  if (opt.prof_order == 1)
+    std::sort(cells.begin(), cells.end(),
+              [](const Profile &a, const Profile &b) { return prof_score(a) < prof_score(b); });
+  else if (opt.prof_order == 2)
+    std::sort(cells.begin(), cells.end(),
+              [](const Profile &a, const Profile &b) { return prof_score(a) > prof_score(b); });
+
+  // ---- orbit canonicalisation (+ quad switch Q, Q-closure prune), ORDER=3, digests ----
+  bool orbit_q = false;
+  if (opt.orbit_q) {
+    const bool safe = opt.endpos || ((n % 2 == 0) && (((SC + SD) % 4 + 4) % 4 == 0));
+    orbit_q = (opt.orbit_q == 2) || (opt.orbit_q == 1 && safe);
+    if (opt.orbit_q == 1 && !safe)
+      LOGF("[orbitq] DISABLED: needs n even and c+d = 0 mod 4, or WZ_FH_ENDPOS=1 (n=%d c=%d d=%d)\n", n, SC, SD);
+    if (opt.orbit_q == 2 && !safe) LOGF("[orbitq] FORCED outside its proven range (test mode only)\n");
+  }
+  out.orbit_q = orbit_q;
+  const int nvar = orbit_q ? 64 : 32;
+  out.kept.assign(cells.size(), 1);
+  if (!opt.orbit_canon) return 0;
+
+  // Orbit ids are compared as the reference compares its string keys; a key is packed into
+  // 128 bits whose integer order is that string order (CellKeyOrder), so the canonicalisation
+  // works on integers and builds strings only for the digest and the certificates.
+  const CellKeyOrder &ko = CellKeyOrder::get();
+  const size_t N = cells.size();
+  std::vector<u128> own(N), oid(N);
+  for (size_t i = 0; i < N; i++) {
+    int px[8], py[8];
+    for (int c = 0; c < m; c++) { px[c] = cells[i].px[c]; py[c] = cells[i].py[c]; }
+    own[i] = ko.pack(px, py, m);
+    oid[i] = orbit_id(px, py, m, n, nvar, ko);
+  }
+  // group the cells by orbit; the orbit's representative is its smallest own key
+  std::vector<uint32_t> by_orbit(N);
+  for (size_t i = 0; i < N; i++) by_orbit[i] = (uint32_t)i;
+  std::sort(by_orbit.begin(), by_orbit.end(), [&](uint32_t x, uint32_t y) {
+    if (oid[x] != oid[y]) return oid[x] < oid[y];
+    return own[x] < own[y];
+  });
+  std::vector<uint32_t> gid(N);
+  std::vector<u128> rep_own;  // representative own key per orbit
+  for (size_t j = 0; j < N; j++) {
+    const uint32_t i = by_orbit[j];
+    if (j == 0 || oid[i] != oid[by_orbit[j - 1]]) rep_own.push_back(own[i]);
+    gid[i] = (uint32_t)(rep_own.size() - 1);
+  }
+  bool dup_keys = false;
+  for (size_t j = 1; j < N; j++)
+    if (own[by_orbit[j]] == own[by_orbit[j - 1]]) dup_keys = true;
+  std::vector<unsigned char> dead(rep_own.size(), 0);
+  size_t ndead = 0;
+  if (orbit_q && opt.qprune) {
+    if (!opt.m6 || N >= 20000000) {
+      LOGF("[qprune] DISABLED (needs mod-6 cells and an untruncated cell list)\n");
+    } else {
+      // Q-closure orbit elimination, wz_match.cpp:1745-1802
+      out.qp_active = true;
+      std::vector<u128> S(own);
+      std::sort(S.begin(), S.end());
+      int ccnt[8];
+      for (int c = 0; c < m; c++) ccnt[c] = class_count(n, c, m);
+      auto realizable = [&](const int *p) {
+        for (int c = 0; c < m; c++)
+          if (std::abs(p[c]) > ccnt[c] || ((p[c] + ccnt[c]) & 1)) return false;
+        return true;
+      };
+      long long missing = 0, nonreal = 0, eq212 = 0, unknown = 0, nonint = 0;
+      std::string cert;
+      std::vector<std::string> certs;
+      for (size_t i = 0; i < N; i++) {
+        int qx[8], qy[8];
+        bool integral = true;
+        for (int c = 0; c < m; c++) {
+          qx[c] = cells[i].px[c];
+          qy[c] = cells[i].py[c];
+        }
+        for (int c = 0; c < m; c++) {
+          int r = ((n - 1 - c) % m + m) % m;
+          if ((qx[c] + qy[c] + qx[r] - qy[r]) & 1) integral = false;
+        }
+        quad_switch(qx, qy, m, n);
+        if (integral && std::binary_search(S.begin(), S.end(), ko.pack(qx, qy, m))) continue;
+        missing++;
+        const char *why = nullptr;
+        if (!integral) { nonint++; why = "nonintegral"; }
+        else if (!realizable(qx) || !realizable(qy)) { nonreal++; why = "not_realizable"; }
+        else if (thm212 && !thm212_ok(Vec(qx, qx + m), Vec(qy, qy + m), m, n, false)) { eq212++; why = "eq2.12"; }
+        else { unknown++; continue; }
+        if (!dead[gid[i]]) {
+          dead[gid[i]] = 1;
+          ndead++;
+          const std::string okey = ko.str(oid[i], m), mine = cell_key(cells[i].px, cells[i].py);
+          const std::string qkey = cell_key(Vec(qx, qx + m), Vec(qy, qy + m));
+          certs.push_back(okey + " " + mine + " " + qkey + " " + why);
+          if (cert.find(why) == std::string::npos)
+            cert += std::string(" ") + why + ":" + mine + "->" + qkey;
+        }
+      }
+      long long removed = 0;
+      for (size_t i = 0; i < N; i++) removed += dead[gid[i]];
+      if (opt.qprune_dump) {
+        if (FILE *df = fopen(opt.qprune_dump, "w")) {
+          for (size_t i = 0; i < N; i++)
+            if (dead[gid[i]]) fprintf(df, "%zu\n", i);
+          fclose(df);
+        }
+        if (FILE *cf = fopen((std::string(opt.qprune_dump) + ".certs").c_str(), "w")) {
+          for (auto &c : certs) fprintf(cf, "%s\n", c.c_str());
+          fclose(cf);
+        }
+      }
+      LOGF("[qprune] missing_Q_images=%lld not_realizable=%lld eq212=%lld nonintegral=%lld unknown=%lld dead_orbits=%zu cells_removed=%lld\n[qprune] certificates:%s\n",
+           missing, nonreal, eq212, nonint, unknown, ndead, removed, cert.c_str());
+    }
+  }
+  // kept: the orbit's representative, unless the orbit is dead. Raw keys are distinct by
+  // construction, so kept cells and kept keys (the reference's keep set) count alike.
+  size_t nkept = 0;
+  for (size_t i = 0; i < N; i++) {
+    out.kept[i] = (own[i] == rep_own[gid[i]] && !dead[gid[i]]) ? 1 : 0;
+    nkept += out.kept[i];
+  }
+  LOGF("[orbitcanon]%s cells=%zu kept_orbits=%zu dedup=%gx\n", orbit_q ? " group=64" : "", N, nkept,
+       (double)N / std::max((size_t)1, nkept));
+  if (opt.prof_order != 3) return 0;
+
+  // deterministic order: (orbit-min profile score, orbit id, own key), wz_match.cpp:1816-1881
+  std::vector<long long> omin(rep_own.size(), -1);
+  for (size_t i = 0; i < N; i++) {
+    const long long sc = prof_score(cells[i]);
+    if (omin[gid[i]] < 0 || sc < omin[gid[i]]) omin[gid[i]] = sc;
+  }
+  std::vector<uint32_t> perm(by_orbit);  // already in (orbit id, own key) order
+  std::stable_sort(perm.begin(), perm.end(),
+                   [&](uint32_t x, uint32_t y) { return omin[gid[x]] < omin[gid[y]]; });
+  {
+    std::vector<Profile> sorted(N);
+    std::vector<unsigned char> skept(N);
+    for (size_t j = 0; j < N; j++) {
+      sorted[j] = std::move(cells[perm[j]]);
+      skept[j] = out.kept[perm[j]];
+    }
+    cells.swap(sorted);
+    out.kept.swap(skept);
+  }
+  uint64_t dl = 1469598103934665603ULL, dk = 1469598103934665603ULL;
+  long long kept_n = 0;
+  for (size_t i = 0; i < N; i++) {
+    dl = fnv_str(dl, cell_key(cells[i].px, cells[i].py));
+    kept_n += out.kept[i];
+    dk = fnv_str(dk, out.kept[i] ? "1" : "0");
+  }
+  if (dup_keys) {
+    size_t uniq = 0;
+    for (size_t j = 0; j < N; j++)
+      if (j == 0 || own[by_orbit[j]] != own[by_orbit[j - 1]]) uniq++;
+    LOGF("RESULT: DUPLICATE CELL KEYS in the raw list (%zu) — refusing\n", N - uniq);
+    return 2;
+  }
+  char dbuf[64];
+  snprintf(dbuf, sizeof dbuf, "%016llx:%016llx", (unsigned long long)dl, (unsigned long long)dk);
+  out.digest = dbuf;
+  const int ns = std::max(1, opt.nshard);
+  std::vector<long long> per_arm(ns, 0);
+  for (size_t i = 0; i < N; i++)
+    if (out.kept[i]) per_arm[i % ns]++;
+  long long arm_min = *std::min_element(per_arm.begin(), per_arm.end());
+  long long arm_max = *std::max_element(per_arm.begin(), per_arm.end());
+  LOGF("[order] ord3 cells=%zu kept=%lld windows=%zu digest=%s arms=%d kept_per_arm_min=%lld max=%lld\n",
+       N, kept_n, (N + ns - 1) / ns, dbuf, ns, arm_min, arm_max);
+  return 0;
 }
 
 uint64_t AbpRows::cell_key_of(const Profile &p, int n, int m) {

@@ -7,6 +7,7 @@
 // feasibility of the complementary A,B side, and the allowed A,B rows of a cell.
 #pragma once
 #include <cstdint>
+#include <cstdio>
 #include <string>
 #include <unordered_map>
 #include <unordered_set>
@@ -59,13 +60,43 @@ std::vector<Profile> survive_profiles3(int L, int sigX, int sigY, int n, const N
 // mod-6 profile pairs (wz_match.cpp:792-837); *capped is set when the cap was reached.
 std::vector<Profile> survive_profiles6(int L, int sigX, int sigY, int n, const NormSet &comp3,
                                        const NormSet &comp6, const AutoSet *comp6auto, bool thm212,
-                                       bool thm211b, size_t cap, bool *capped);
+                                       bool thm211b, size_t cap, bool *capped, FILE *log = stdout);
 
 // "v,v,...,|v,v,...," cell key (wz_match.cpp:1665-1671).
 std::string cell_key(const Vec &px, const Vec &py);
 
 // 64-bit FNV-1a over a string's bytes, continuing from h.
 uint64_t fnv_str(uint64_t h, const std::string &s);
+
+// ---- the lane's cell list ----------------------------------------------------------------
+// Options of the first-hit lane that shape the C,D cell list (the reference's WZ_FH_M6,
+// WZ_THM211B, WZ_THM212, WZ_FH_ENDPOS, WZ_FH_ORBIT_CANON, WZ_FH_ORBIT_Q,
+// WZ_FH_ORBIT_QPRUNE, WZ_FH_PROF_ORDER).
+struct ListOptions {
+  bool m6 = false, thm211b = false, thm212 = false;
+  bool endpos = false, endpos_nocell = false;
+  bool orbit_canon = false;
+  int orbit_q = 0;         // 0 off, 1 on where proven safe, 2 forced (tests)
+  bool qprune = false;
+  int prof_order = 0;      // 0 natural, 1 flat first, 2 reverse, 3 orbit-deterministic
+  int nshard = 1;          // for the [order] per-arm balance line
+  const char *qprune_dump = nullptr;
+};
+
+struct CellList {
+  int m = 6;
+  std::vector<Profile> cells;          // in the lane's final order (raw index = position)
+  std::vector<unsigned char> kept;     // 1: the cell is its orbit's representative (canon)
+  std::string digest;                  // "<list>:<kept>" under ORDER=3, else empty
+  bool orbit_q = false, qp_active = false;
+  size_t ab_profiles = 0, cd_profiles = 0, ab_auto = 0, cd_auto = 0;
+};
+
+// Builds the list exactly as the reference's first-hit block does (wz_match.cpp:1388-1886),
+// printing the same bracketed lines to `log` when it is non-null. Returns 0, or 2 where the
+// reference refuses (truncated list, duplicate keys, ORDER=3 without canon).
+int build_cell_list(int n, int a, int b, int c, int d, const ListOptions &opt, CellList &out,
+                    FILE *log);
 
 // Allowed A,B class-sum rows keyed by the cell invariant (need, needT): the reference's
 // abpMap (wz_match.cpp:2318-2378). A row is k[8] then r[8] (int8).

@@ -154,25 +154,6 @@ int main(int argc, char **argv) {
   fflush(stdout);
   const auto G_T0 = Clock::now();
 
-  NormSet ab3, ab6, cd3, cd6;
-  ab3.build(n1, SA, SB, 3, n);
-  ab6.build(n1, SA, SB, 6, n);
-  cd3.build(n, SC, SD, 3, n);
-  cd6.build(n, SC, SD, 6, n);
-  AutoSet ab6a, cd6a;
-  if (thm211b) {
-    ab6a.build(n1, SA, SB, 6, n, thm212);
-    cd6a.build(n, SC, SD, 6, n, thm212);
-    printf("[thm2.11b] ENABLED — complement (autocorr,norm) tuples: A,B side %zu  C,D side %zu\n",
-           ab6a.keys.size(), cd6a.keys.size());
-    fflush(stdout);
-  }
-  auto abProfs = survive_profiles3(n1, SA, SB, n, cd3, cd6, thm211b ? &cd6a : nullptr, thm212, thm211b);
-  auto cdProfs = survive_profiles3(n, SC, SD, n, ab3, ab6, thm211b ? &ab6a : nullptr, thm212, thm211b);
-  printf("[profiles] A,B side surviving: %zu   C,D side surviving: %zu\n", abProfs.size(), cdProfs.size());
-  fflush(stdout);
-  bool pinC = (SC == 0), pinD = (SD == 0);
-
   // ---------------------------------------------------------------- run configuration
   bool fh_m6 = (n >= 36);
   if (const char *e = env("WZ_FH_M6")) fh_m6 = atoi(e) != 0;
@@ -189,225 +170,39 @@ int main(int argc, char **argv) {
   }
 
   // ---------------------------------------------------------------- cell list
-  std::vector<Profile> cells;
-  if (fh_m6) {
-    bool capped = false;
-    cells = survive_profiles6(n, SC, SD, n, ab3, ab6, thm211b ? &ab6a : nullptr, thm212, thm211b,
-                              20000000, &capped);
-    printf("[firsthit] mod-6 stream source: %zu C,D profile cells (mod-3 atoms exceed walltime at this n)\n",
-           cells.size());
-    fflush(stdout);
-    if (cells.size() >= 20000000) {
-      printf("RESULT: CELL LIST TRUNCATED at the 20M cap — refusing to search an incomplete tile\n");
-      fflush(stdout);
-      return 2;
-    }
-    if (endpos) {
-      // endpoint-parity cell filter, wz_match.cpp:1598-1622
-      const bool nocell = env_on("WZ_FH_ENDPOS_NOCELL");
-      size_t before = cells.size();
-      std::vector<Profile> keep;
-      for (size_t i = 0; i < cells.size(); i++) {
-        const auto &p = cells[i];
-        int s = 0;
-        for (int c = 0; c < 6; c++) s += p.px[c] + p.py[c];
-        int mid = (n % 2 == 1) ? p.px[(n / 2) % 6] + p.py[(n / 2) % 6] : 0;
-        bool ok = (((s - mid) % 4) + 4) % 4 == 0;
-        if (nocell) printf("ENDPOS_CELL idx=%zu ok=%d\n", i, ok ? 1 : 0);
-        if (ok || nocell) keep.push_back(p);
-      }
-      cells.swap(keep);
-      printf("[endpos] cells %zu -> %zu (endpoint-parity filter%s)\n", before, cells.size(),
-             nocell ? ", NOT applied: test hook" : "");
-      fflush(stdout);
-    }
-  } else {
-    cells = cdProfs;
-  }
-  const int fh_m = fh_m6 ? 6 : 3;
-  auto prof_score = [](const Profile &p) {
-    long long s = 0;
-    for (int v : p.px) s += std::abs(v);
-    for (int v : p.py) s += std::abs(v);
-    return s;
-  };
-  if (prof_order == 1)
-    std::sort(cells.begin(), cells.end(), [&](const Profile &a, const Profile &b) { return prof_score(a) < prof_score(b); });
-  else if (prof_order == 2)
-    std::sort(cells.begin(), cells.end(), [&](const Profile &a, const Profile &b) { return prof_score(a) > prof_score(b); });
-
-  // ---- orbit canonicalisation (+ quad switch Q, Q-closure prune), ORDER=3, digests ----
-  bool orbit_canon = env_i("WZ_FH_ORBIT_CANON", 0) != 0;
-  bool pins_dropped = false;
-  if (orbit_canon && (pinC || pinD)) { pinC = false; pinD = false; pins_dropped = true; }
-  std::unordered_set<std::string> keep_set;
-  bool orbit_q = false;
-  if (const char *e = env("WZ_FH_ORBIT_Q")) {
-    int v = atoi(e);
-    bool safe = endpos || ((n % 2 == 0) && (((SC + SD) % 4 + 4) % 4 == 0));
-    orbit_q = (v == 2) || (v == 1 && safe);
-    if (v == 1 && !safe)
-      printf("[orbitq] DISABLED: needs n even and c+d = 0 mod 4, or WZ_FH_ENDPOS=1 (n=%d c=%d d=%d)\n", n, SC, SD);
-    if (v == 2 && !safe) printf("[orbitq] FORCED outside its proven range (test mode only)\n");
-    fflush(stdout);
-  }
-  const int nvar = orbit_q ? 64 : 32;
-  bool qp_active = false;
-  std::string order_digest;
-  auto revp = [&](const Vec &p) {
-    Vec q(fh_m);
-    for (int c = 0; c < fh_m; c++) q[((n - 1 - c) % fh_m + fh_m) % fh_m] = p[c];
-    return q;
-  };
-  auto quadq = [&](Vec &px, Vec &py) {
-    Vec rx = revp(px), ry = revp(py), nx(fh_m), ny(fh_m);
-    for (int c = 0; c < fh_m; c++) {
-      nx[c] = (px[c] + py[c] + rx[c] - ry[c]) / 2;
-      ny[c] = (px[c] + py[c] - rx[c] + ry[c]) / 2;
-    }
-    px.swap(nx);
-    py.swap(ny);
-  };
-  if (orbit_canon) {
-    auto negp = [](Vec p) { for (auto &x : p) x = -x; return p; };
-    std::unordered_map<std::string, std::string> orbit_min;
-    std::vector<std::string> own(cells.size()), oid(cells.size());
-    for (size_t i = 0; i < cells.size(); i++) {
-      own[i] = cell_key(cells[i].px, cells[i].py);
-      std::string best;
-      for (int var = 0; var < nvar; var++) {
-        Vec px = cells[i].px, py = cells[i].py;
-        if (var & 32) quadq(px, py);
-        if (var & 1) px = negp(px);
-        if (var & 2) py = negp(py);
-        if (var & 4) px = revp(px);
-        if (var & 8) py = revp(py);
-        if (var & 16) std::swap(px, py);
-        std::string k = cell_key(px, py);
-        if (best.empty() || k < best) best = k;
-      }
-      oid[i] = best;
-      auto it = orbit_min.find(best);
-      if (it == orbit_min.end() || own[i] < it->second) orbit_min[best] = own[i];
-    }
-    std::unordered_set<std::string> qp_dead;
-    if (orbit_q && env_on("WZ_FH_ORBIT_QPRUNE")) {
-      if (!fh_m6 || cells.size() >= 20000000) {
-        printf("[qprune] DISABLED (needs mod-6 cells and an untruncated cell list)\n");
-      } else {
-        // Q-closure orbit elimination, wz_match.cpp:1745-1802
-        qp_active = true;
-        std::unordered_set<std::string> S(own.begin(), own.end());
-        int ccnt[8];
-        for (int c = 0; c < fh_m; c++) ccnt[c] = class_count(n, c, fh_m);
-        auto realizable = [&](const Vec &p) {
-          for (int c = 0; c < fh_m; c++)
-            if (std::abs(p[c]) > ccnt[c] || ((p[c] + ccnt[c]) & 1)) return false;
-          return true;
-        };
-        long long missing = 0, nonreal = 0, eq212 = 0, unknown = 0, nonint = 0;
-        std::string cert;
-        std::vector<std::string> certs;
-        for (size_t i = 0; i < cells.size(); i++) {
-          Vec qx = cells[i].px, qy = cells[i].py;
-          bool integral = true;
-          for (int c = 0; c < fh_m; c++) {
-            int r = ((n - 1 - c) % fh_m + fh_m) % fh_m;
-            if ((qx[c] + qy[c] + qx[r] - qy[r]) & 1) integral = false;
-          }
-          quadq(qx, qy);
-          if (integral && S.count(cell_key(qx, qy))) continue;
-          missing++;
-          const char *why = nullptr;
-          if (!integral) { nonint++; why = "nonintegral"; }
-          else if (!realizable(qx) || !realizable(qy)) { nonreal++; why = "not_realizable"; }
-          else if (thm212 && !thm212_ok(qx, qy, fh_m, n, false)) { eq212++; why = "eq2.12"; }
-          else { unknown++; continue; }
-          if (qp_dead.insert(oid[i]).second) {
-            certs.push_back(oid[i] + " " + own[i] + " " + cell_key(qx, qy) + " " + why);
-            if (cert.find(why) == std::string::npos)
-              cert += std::string(" ") + why + ":" + own[i] + "->" + cell_key(qx, qy);
-          }
-        }
-        long long removed = 0;
-        for (size_t i = 0; i < cells.size(); i++) removed += qp_dead.count(oid[i]);
-        if (const char *dp = env("WZ_FH_QPRUNE_DUMP")) {
-          if (FILE *df = fopen(dp, "w")) {
-            for (size_t i = 0; i < cells.size(); i++)
-              if (qp_dead.count(oid[i])) fprintf(df, "%zu\n", i);
-            fclose(df);
-          }
-          if (FILE *cf = fopen((std::string(dp) + ".certs").c_str(), "w")) {
-            for (auto &c : certs) fprintf(cf, "%s\n", c.c_str());
-            fclose(cf);
-          }
-        }
-        printf("[qprune] missing_Q_images=%lld not_realizable=%lld eq212=%lld nonintegral=%lld unknown=%lld dead_orbits=%zu cells_removed=%lld\n[qprune] certificates:%s\n",
-               missing, nonreal, eq212, nonint, unknown, qp_dead.size(), removed, cert.c_str());
-      }
-    }
-    for (size_t i = 0; i < cells.size(); i++)
-      if (orbit_min[oid[i]] == own[i] && !qp_dead.count(oid[i])) keep_set.insert(own[i]);
-    printf("[orbitcanon]%s cells=%zu kept_orbits=%zu dedup=%gx\n", orbit_q ? " group=64" : "", cells.size(),
-           keep_set.size(), (double)cells.size() / std::max((size_t)1, keep_set.size()));
-    fflush(stdout);
-    if (prof_order == 3) {
-      // deterministic order: (orbit-min profile score, orbit id, own key), wz_match.cpp:1816-1881
-      std::unordered_map<std::string, long long> omin;
-      for (size_t i = 0; i < cells.size(); i++) {
-        long long sc = prof_score(cells[i]);
-        auto it = omin.find(oid[i]);
-        if (it == omin.end() || sc < it->second) omin[oid[i]] = sc;
-      }
-      std::vector<size_t> perm(cells.size());
-      for (size_t i = 0; i < perm.size(); i++) perm[i] = i;
-      std::sort(perm.begin(), perm.end(), [&](size_t a, size_t b) {
-        long long sa = omin[oid[a]], sb = omin[oid[b]];
-        if (sa != sb) return sa < sb;
-        if (oid[a] != oid[b]) return oid[a] < oid[b];
-        return own[a] < own[b];
-      });
-      std::vector<Profile> sorted(cells.size());
-      for (size_t i = 0; i < perm.size(); i++) sorted[i] = cells[perm[i]];
-      cells.swap(sorted);
-      uint64_t dl = 1469598103934665603ULL, dk = 1469598103934665603ULL;
-      long long kept_n = 0;
-      for (size_t i = 0; i < cells.size(); i++) {
-        std::string k = cell_key(cells[i].px, cells[i].py);
-        dl = fnv_str(dl, k);
-        bool kept = keep_set.count(k) > 0;
-        kept_n += kept;
-        dk = fnv_str(dk, kept ? "1" : "0");
-      }
-      {
-        std::unordered_set<std::string> uniq(own.begin(), own.end());
-        if (uniq.size() != own.size()) {
-          printf("RESULT: DUPLICATE CELL KEYS in the raw list (%zu) — refusing\n", own.size() - uniq.size());
-          return 2;
-        }
-      }
-      char dbuf[64];
-      snprintf(dbuf, sizeof dbuf, "%016llx:%016llx", (unsigned long long)dl, (unsigned long long)dk);
-      order_digest = dbuf;
-      std::vector<long long> per_arm(fh_nshard, 0);
-      for (size_t i = 0; i < cells.size(); i++)
-        if (keep_set.count(cell_key(cells[i].px, cells[i].py))) per_arm[i % fh_nshard]++;
-      long long arm_min = *std::min_element(per_arm.begin(), per_arm.end());
-      long long arm_max = *std::max_element(per_arm.begin(), per_arm.end());
-      printf("[order] ord3 cells=%zu kept=%lld windows=%zu digest=%s arms=%d kept_per_arm_min=%lld max=%lld\n",
-             cells.size(), kept_n, (cells.size() + fh_nshard - 1) / fh_nshard, dbuf, fh_nshard, arm_min, arm_max);
-      fflush(stdout);
-      if (const char *e = env("WZ_FH_EXPECT_DIGEST"))
-        if (strcmp(e, dbuf) != 0) {
-          printf("RESULT: DIGEST MISMATCH (expected %s) — refusing to search or resume\n", e);
-          return 2;
-        }
-      if (env("WZ_FH_LIST_ONLY")) return 0;
-      if (!env("WZ_FH_EXPECT_DIGEST") && !env("WZ_FH_LOCATE_C") && !env("WZ_FH_ORBIT_AUDIT") &&
-          !env("WZ_FH_CELLSIZE") && !env("WZ_FH_ORD3_NODIGEST_OK")) {
-        printf("RESULT: PROF_ORDER=3 search requires WZ_FH_EXPECT_DIGEST (from the manifest)\n");
+  ListOptions lopt;
+  lopt.m6 = fh_m6;
+  lopt.thm211b = thm211b;
+  lopt.thm212 = thm212;
+  lopt.endpos = endpos;
+  lopt.endpos_nocell = env_on("WZ_FH_ENDPOS_NOCELL");
+  const bool orbit_canon = env_i("WZ_FH_ORBIT_CANON", 0) != 0;
+  lopt.orbit_canon = orbit_canon;
+  lopt.orbit_q = env_i("WZ_FH_ORBIT_Q", 0);
+  lopt.qprune = env_on("WZ_FH_ORBIT_QPRUNE");
+  lopt.prof_order = prof_order;
+  lopt.nshard = fh_nshard;
+  lopt.qprune_dump = env("WZ_FH_QPRUNE_DUMP");
+  CellList list;
+  if (build_cell_list(n, SA, SB, SC, SD, lopt, list, stdout) != 0) return 2;
+  std::vector<Profile> &cells = list.cells;
+  const int fh_m = list.m;
+  const bool orbit_q = list.orbit_q, qp_active = list.qp_active;
+  const std::string order_digest = list.digest;
+  // the canonical orbit representative need not carry the zero-sum pin (wz_match.cpp:1659-1662)
+  const bool pins_dropped = orbit_canon && (SC == 0 || SD == 0);
+  const bool pinC = (SC == 0) && !orbit_canon, pinD = (SD == 0) && !orbit_canon;
+  if (orbit_canon && prof_order == 3) {
+    if (const char *e = env("WZ_FH_EXPECT_DIGEST"))
+      if (order_digest != e) {
+        printf("RESULT: DIGEST MISMATCH (expected %s) — refusing to search or resume\n", e);
         return 2;
       }
+    if (env("WZ_FH_LIST_ONLY")) return 0;
+    if (!env("WZ_FH_EXPECT_DIGEST") && !env("WZ_FH_LOCATE_C") && !env("WZ_FH_ORBIT_AUDIT") &&
+        !env("WZ_FH_CELLSIZE") && !env("WZ_FH_ORD3_NODIGEST_OK")) {
+      printf("RESULT: PROF_ORDER=3 search requires WZ_FH_EXPECT_DIGEST (from the manifest)\n");
+      return 2;
     }
   }
   if (prof_order == 3 && !orbit_canon) {
@@ -423,8 +218,7 @@ int main(int argc, char **argv) {
     std::vector<int> r = parse_list(e);
     long long lo = r.size() > 0 ? r[0] : 0, hi = r.size() > 1 ? r[1] : (long long)cells.size();
     for (long long pi = std::max(0LL, lo); pi < std::min(hi, (long long)cells.size()); pi++) {
-      std::string k = cell_key(cells[pi].px, cells[pi].py);
-      printf("CELL pi=%lld kept=%d px=", pi, (!orbit_canon || keep_set.count(k)) ? 1 : 0);
+      printf("CELL pi=%lld kept=%d px=", pi, (int)list.kept[pi]);
       for (int c = 0; c < fh_m; c++) printf("%d%s", cells[pi].px[c], c + 1 < fh_m ? "," : "");
       printf(" py=");
       for (int c = 0; c < fh_m; c++) printf("%d%s", cells[pi].py[c], c + 1 < fh_m ? "," : "");
@@ -529,7 +323,7 @@ int main(int argc, char **argv) {
     auto tb0 = Clock::now();
     std::vector<uint64_t> keys;
     for (long long pi = fh_shard + (long long)fh_skip * fh_nshard; pi < (long long)cells.size(); pi += fh_nshard) {
-      if (orbit_canon && !keep_set.count(cell_key(cells[pi].px, cells[pi].py))) continue;
+      if (!list.kept[pi]) continue;
       keys.push_back(AbpRows::cell_key_of(cells[pi], n, fh_m));
     }
     abp.build(keys, n, SA, SB, fh_m);
@@ -622,7 +416,7 @@ int main(int argc, char **argv) {
   for (long long pi = fh_shard + (long long)fh_skip * fh_nshard; pi < pi_end && !fh_stop; pi += fh_nshard) {
     if (resuming && pi < res_pi) continue;
     if (resuming && pi > res_pi) resuming = false;
-    if (orbit_canon && !keep_set.count(cell_key(cells[pi].px, cells[pi].py))) {
+    if (!list.kept[pi]) {
       cells_orbit_dup++;
       if (resuming && pi == res_pi) resuming = false;
       ck_pi = pi + fh_nshard; ck_batch = 0; ck_k = 0;

@@ -113,6 +113,41 @@ typedef struct {
 
 typedef struct { long long nodes, leaves, ok; } bs_cell_stats;
 
+/* ---- the lane's cell list (host only: no device, no context) -----------------------------
+ * Replaces the first-hit lane's cell-list block (src/solver/wz_match.cpp:1388-1886): the
+ * mod-3 or mod-6 C,D profile cells surviving 2.11a (+2.11b/2.12), the ENDPOS filter, the
+ * profile order (WZ_FH_PROF_ORDER 0..3), orbit canonicalisation with the quad switch and its
+ * Q-closure prune, and the ORDER=3 digest "<list>:<kept>". cells[i] is raw cell i of the
+ * lane (pins set as the lane sets them), kept[i] = 1 when the lane searches it (its orbit's
+ * representative under canon; always 1 without). Nothing is printed. Returns BS_ERR_CAP
+ * (with *ncells set) when cap is too small, 2 where the reference refuses (truncated list,
+ * duplicate keys). digest (may be NULL) receives up to 40 bytes, "" unless prof_order 3. */
+typedef struct {
+  int32_t m6;           /* WZ_FH_M6 (the lane's default is n >= 36) */
+  int32_t thm211b;      /* WZ_THM211B (forced at n >= 36) */
+  int32_t thm212;       /* WZ_THM212 (forced at n >= 36) */
+  int32_t endpos;       /* WZ_FH_ENDPOS */
+  int32_t orbit_canon;  /* WZ_FH_ORBIT_CANON */
+  int32_t orbit_q;      /* WZ_FH_ORBIT_Q: 0, 1, 2 */
+  int32_t qprune;       /* WZ_FH_ORBIT_QPRUNE */
+  int32_t prof_order;   /* WZ_FH_PROF_ORDER: 0..3 */
+  int32_t nshard;       /* WZ_FH_NSHARD (only the [order] balance figures use it) */
+  int32_t reserved;
+} bs_list_opts;
+
+int bs_cell_list(int n, int a, int b, int c, int d, const bs_list_opts *opt, bs_cell *cells,
+                 uint8_t *kept, long long cap, long long *ncells, char *digest);
+
+/* Replaces the lane's abpMap build (src/solver/wz_match.cpp:2318-2378): for each given cell,
+ * the allowed A,B class-sum rows (16 int8 each: k[8] then r[8]) of its invariant, written
+ * back to back; row_off[i] / nrows[i] locate cell i's rows (cells with one invariant share
+ * them). nrows[i] = 0 means no allowed row: the cell holds no base sequence and the lane
+ * skips it (cells_prof_dead) -- do not pass it on as an unconstrained bs_ab_cand. The lane
+ * runs cells with more than WZ_FH_AB_PROF_CAP rows unconstrained. *nrows_total = rows
+ * written; BS_ERR_CAP (with *nrows_total = rows needed) when rows_cap is too small. */
+int bs_ab_rows(int n, int a, int b, int m, const bs_cell *cells, long long ncells, int8_t *rows,
+               long long rows_cap, long long *row_off, int32_t *nrows, long long *nrows_total);
+
 /* out_words: 2 words (C, D) per survivor, out_cell (may be NULL): the survivor's cell index.
  * *nout always receives the survivor count; BS_ERR_CAP when it exceeds out_cap. */
 int bs_cd_stream(bs_ctx *ctx, const bs_cell *cells, int ncells, const bs_stream_opts *opt,

@@ -1,0 +1,146 @@
+"""The lane's cell list on the host, against the reference's own list stage
+(tests/golden/list_golden.json: WZ_FH_LIST_ONLY runs of the reference binary under
+WZ_FH_PROF_ORDER=3, whose digest covers every raw cell key in order and every kept flag).
+
+Checked two ways: the drop-in binary bin/bs_firsthit prints the same bracketed lines and exit
+code, and the host-only C ABI bs_cell_list returns the same cell count, kept count and digest.
+bs_ab_rows is checked against a direct restatement of the abpMap rule at small n.
+"""
+import itertools
+import json
+import os
+import re
+import sys
+
+import numpy as np
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(HERE, "golden"))
+
+
+def _cases(large=None):
+    cs = json.load(open(os.path.join(HERE, "golden", "list_golden.json")))
+    return [c for c in cs if large is None or c["large"] == large]
+
+
+def _order_line(lines):
+    for l in lines:
+        m = re.match(r"\[order\] ord3 cells=(\d+) kept=(\d+) .*digest=([0-9a-f]+:[0-9a-f]+)", l)
+        if m:
+            return int(m.group(1)), int(m.group(2)), m.group(3)
+    raise AssertionError("no [order] line")
+
+
+def test_lane_binary_list_stage_matches_reference(built_lib):
+    from make_list_golden import run
+    from bs45_quantum_explorer_gb300.build import build_host
+    exe = build_host()
+    for c in _cases():
+        if c["large"] and c["n"] != 42:
+            continue
+        rc, lines = run(exe, c["n"], c["sig"], c["settings"])
+        assert (rc, lines) == (c["rc"], c["lines"]), (c["n"], c["sig"], c["settings"])
+
+
+def _opts(c):
+    st = c["settings"]
+    big = c["n"] >= 36
+    return dict(m6=bool(st.get("WZ_FH_M6", big)), thm211b=bool(st.get("WZ_THM211B", big)),
+                thm212=bool(st.get("WZ_THM212", big)), endpos=bool(st.get("WZ_FH_ENDPOS", 0)),
+                orbit_canon=True, orbit_q=int(st.get("WZ_FH_ORBIT_Q", 0)),
+                qprune=bool(st.get("WZ_FH_ORBIT_QPRUNE", 0)), prof_order=3,
+                nshard=int(st.get("WZ_FH_NSHARD", 1)))
+
+
+def test_cell_list_capi_matches_reference(built_lib):
+    from bs45_quantum_explorer_gb300.cells import cell_list
+    for c in _cases():
+        if c["large"] and c["n"] != 36:   # (n=42 is covered through the binary above)
+            continue
+        cells, kept, digest, m = cell_list(c["n"], tuple(c["sig"]), **_opts(c))
+        ncell, nkept, want = _order_line(c["lines"])
+        assert (len(kept), int(kept.sum()), digest) == (ncell, nkept, want), (c["n"], c["sig"], c["settings"])
+        assert m == (6 if _opts(c)["m6"] else 3)
+
+
+def test_cell_list_without_canon_keeps_every_cell_and_sets_pins(built_lib):
+    from bs45_quantum_explorer_gb300.cells import cell_list
+    cells, kept, digest, m = cell_list(12, (1, 7, 0, 0), m6=True)
+    assert digest == "" and kept.all() and len(kept) > 0
+    assert all(cells[i].pinX == 1 and cells[i].pinY == 1 for i in range(len(kept)))
+    cells2, kept2, _, _ = cell_list(12, (1, 7, 0, 0), m6=True, orbit_canon=True)
+    assert len(kept2) == len(kept) and 0 < kept2.sum() < len(kept2)
+    assert all(cells2[i].pinX == 0 and cells2[i].pinY == 0 for i in range(len(kept2)))
+
+
+def test_cell_list_refuses_bad_arguments(built_lib):
+    from bs45_quantum_explorer_gb300._lib import BsError
+    from bs45_quantum_explorer_gb300.cells import cell_list
+    with pytest.raises(BsError):
+        cell_list(12, (1, 7, 0, 2))                     # signature norm != 4n+2
+    with pytest.raises(BsError):
+        cell_list(12, (1, 7, 0, 0), prof_order=3)        # ORDER=3 without canon
+
+
+# ---- allowed A,B rows, restated from the rule (wz_match.cpp:2318-2378) ----
+
+def _enum_cs(L, target, m):
+    cnt = [len(range(c, L, m)) for c in range(m)]
+    out = []
+    for v in itertools.product(*[range(-k, k + 1, 2) for k in cnt[:-1]]):
+        last = target - sum(v)
+        if abs(last) <= cnt[-1] and (last + cnt[-1]) % 2 == 0:
+            out.append(list(v) + [last])
+    return out
+
+
+def _acf(v, s):
+    return sum(v[i] * v[i + s] for i in range(len(v) - s))
+
+
+def _ab_side_212(x, y, m, n):
+    c1 = n % m
+    want = 2 if c1 else 0
+    if (x[0] + y[0] + x[c1] + y[c1]) % 4 != want:
+        return False
+    for j in range(2, m + 1):
+        if j == c1 + 1:
+            continue
+        c = (n + 1 - j) % m
+        if (x[j - 1] + y[j - 1] + x[c] + y[c]) % 4:
+            return False
+    return True
+
+
+def _rows_brute(n, sig, m, px, py):
+    tgt, hm = 4 * n + 2, m // 2
+    need = tgt - sum(v * v for v in px) - sum(v * v for v in py)
+    needT = [-(_acf(px, s) + _acf(py, s) + _acf(px, m - s) + _acf(py, m - s)) for s in range(1, hm + 1)]
+    def side(sg):
+        return [v for s in ((1, -1) if sg else (1,)) for v in _enum_cs(n + 1, s * sg, m)]
+    rows = []
+    for k in side(sig[0]):
+        for r in side(sig[1]):
+            if sum(v * v for v in k) + sum(v * v for v in r) != need:
+                continue
+            T = [_acf(k, s) + _acf(k, m - s) + _acf(r, s) + _acf(r, m - s) for s in range(1, hm + 1)]
+            if T == needT and _ab_side_212(k, r, m, n):
+                rows.append(tuple(k) + (0,) * (8 - m) + tuple(r) + (0,) * (8 - m))
+    return rows
+
+
+@pytest.mark.parametrize("n,sig,m6", [(12, (1, 7, 0, 0), True), (13, (0, 2, 1, 7), True),
+                                      (12, (1, 3, 2, 6), False)])
+def test_ab_rows_match_the_rule(built_lib, n, sig, m6):
+    from bs45_quantum_explorer_gb300.cells import ab_rows, cell_list, cell_tuple
+    cells, kept, _, m = cell_list(n, sig, m6=m6, thm211b=True, thm212=True)
+    pick = list(range(0, len(kept), max(1, len(kept) // 40)))[:40]
+    sub = [cells[i] for i in pick]
+    rows, row_off, nrows = ab_rows(n, sig, m, sub)
+    assert rows.shape[1] == 16
+    for j, i in enumerate(pick):
+        px, py = cell_tuple(cells[i], m)
+        got = [tuple(int(x) for x in r) for r in rows[row_off[j]:row_off[j] + nrows[j]]]
+        want = _rows_brute(n, sig, m, list(px), list(py))
+        assert got == want, (n, sig, px, py)
