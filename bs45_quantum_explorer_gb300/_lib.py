@@ -81,6 +81,8 @@ SIGNATURES = {
     "bs_hall_filter_dev": (C.c_int, [C.c_void_p, C.c_void_p, C.c_longlong, C.c_int, C.c_void_p,
                                      C.POINTER(HallStats)]),
     "bs_hall_tc_dump_dev": (C.c_int, [C.c_void_p, C.c_void_p, C.c_longlong, C.c_int, C.c_void_p]),
+    "bs_hall_filter_noalloc": (C.c_int, [C.c_int, C.c_void_p, C.c_longlong, C.c_void_p,
+                                         C.c_void_p]),
     "bs_pack_rows": (C.c_int, [C.c_void_p, C.c_longlong, C.c_int, C.c_void_p]),
     "bs_gen_hall_pairs_dev": (C.c_int, [C.c_void_p, C.c_longlong, C.c_uint64, C.c_void_p]),
     "bs_cd_stream": (C.c_int, [C.c_void_p, C.POINTER(Cell), C.c_int, C.POINTER(StreamOpts),

@@ -10,6 +10,10 @@
 //     margin band are rechecked by the FP64 form. Decisions equal the FP64 form's.
 #include <stdint.h>
 
+#include <cmath>
+#include <cstring>
+#include <mutex>
+
 #include "bsfh_internal.cuh"
 #include "tmem_ld.cuh"
 
@@ -642,4 +646,161 @@ extern "C" int bs_hall_filter_batch(bs_ctx *ctx, const int8_t *XY, long long npa
 extern "C" int bs_hall_filter_packed(bs_ctx *ctx, const uint64_t *bits, long long npairs,
                                      int mode, uint8_t *pass, bs_hall_stats *stats) {
   return hall_host(ctx, bits, true, npairs, mode, pass, stats);
+}
+
+// ------------------------------------------------------------------------------------
+// Allocation-free Hall filter (bs_hall_filter_noalloc)
+//
+// For callers that may not allocate device memory: code that runs under a device-memory
+// budget owned by someone else (a scheduler or host framework that pre-reserves the GPU's
+// memory and forbids allocations during a job), and latency-sensitive callers in the middle
+// of overlapped multi-stream work, where cudaMalloc/cudaFree would synchronise the device.
+// The tensor-core form needs scratch memory (the margin-band list, its counters, the status
+// word) and its tables; here all of it lives in one file-scope __device__ array of fixed
+// size, which every GPU that loads this library holds until the process exits.
+// ------------------------------------------------------------------------------------
+namespace {
+constexpr long long NOALLOC_MAX_PAIRS = 1LL << 20;  // pairs per call
+constexpr size_t NA_COUNT_OFF = 0;                   // 8 x uint64 counters
+constexpr size_t NA_STATUS_OFF = 64;                 // int status word
+constexpr size_t NA_COS_OFF = 256;                   // FP64 cos [200][BS_MAXL]
+constexpr size_t NA_SIN_OFF = NA_COS_OFF + sizeof(double) * 200 * BS_MAXL;
+constexpr size_t NA_IMG_OFF = NA_SIN_OFF + sizeof(double) * 200 * BS_MAXL;  // fp16 table image
+constexpr size_t NA_UNC_OFF = NA_IMG_OFF + BS_TC_PART_BYTES;                // uint32 band list
+constexpr size_t NA_BYTES = NA_UNC_OFF + sizeof(unsigned) * NOALLOC_MAX_PAIRS;
+
+struct NoallocDevice {
+  unsigned char *scratch;  // device address of g_hall_noalloc_scratch on this device
+  int n;                   // sequence length whose tables the scratch holds (0: none)
+  double lim;
+  float pass_below, reject_above;
+};
+NoallocDevice g_na[64];
+std::mutex g_na_mutex;
+// host staging of the tables (static storage, no heap)
+double g_na_cos[200 * BS_MAXL], g_na_sin[200 * BS_MAXL];
+uint8_t g_na_img[BS_TC_PART_BYTES];
+}  // namespace
+
+static __device__ __align__(256) unsigned char g_hall_noalloc_scratch[NA_BYTES];
+
+// Tables of length n (as bs_ctx_create builds them: host libm, then the fp16 quantisation
+// q(t) = round(t * 2^11) / 2^11 in the 128B-swizzled image) and the certified thresholds.
+static void noalloc_tables(int n, NoallocDevice &S) {
+  memset(g_na_cos, 0, sizeof g_na_cos);
+  memset(g_na_sin, 0, sizeof g_na_sin);
+  memset(g_na_img, 0, sizeof g_na_img);
+  for (int j = 1; j <= 200; j++) {
+    double th = j * 3.14159265358979323846 / 100.0;
+    for (int i = 0; i <= n; i++) {
+      g_na_cos[(j - 1) * BS_MAXL + i] = cos(i * th);
+      g_na_sin[(j - 1) * BS_MAXL + i] = sin(i * th);
+    }
+  }
+  double e = 0.0;
+  for (int u = 0; u < BS_TC_NANG; u++) {
+    const int j = u < 100 ? u + 1 : 200;
+    for (int kind = 0; kind < 2; kind++) {
+      const double *tab = kind ? g_na_sin : g_na_cos;
+      const int row = kind ? BS_TC_IM0 + u : u;
+      double esum = 0.0;
+      for (int i = 0; i < n; i++) {
+        const double t = tab[(j - 1) * BS_MAXL + i];
+        const double q = nearbyint(t * 2048.0) / 2048.0;
+        esum += fabs(t - q);
+        // exact fp16 bits of q (a multiple of 2^-11 in [-1, 1])
+        uint16_t bits = 0;
+        if (q != 0.0) {
+          int ex;
+          const double m = frexp(fabs(q), &ex);
+          const int e16 = ex - 1 + 15;
+          bits = (uint16_t)((q < 0 ? 0x8000 : 0) | (e16 << 10) | (int)llrint((m * 2.0 - 1.0) * 1024.0));
+        }
+        const size_t off = (size_t)row * 128 + ((size_t)((i >> 3) ^ (row & 7)) << 4) + (size_t)(i & 7) * 2;
+        g_na_img[off] = (uint8_t)(bits & 0xFF);
+        g_na_img[off + 1] = (uint8_t)(bits >> 8);
+      }
+      if (esum > e) e = esum;
+    }
+  }
+  e = e * (1.0 + 1e-9) + 1e-12;
+  const double eps64 = 1e-9, rho = ldexp(1.0, -20), kappa = 1.0 + 4.0 * rho;
+  const double lim = (4.0 * n + 2.0) + 0.5;
+  double pb = sqrt(lim - eps64) - 2.0 * e;
+  pb = pb * pb / kappa;
+  double ra = 2.0 * e + sqrt(lim + 8.0 * e * e + eps64);
+  ra = ra * ra * kappa;
+  float pbf = (float)pb;
+  if ((double)pbf > pb) pbf = nextafterf(pbf, 0.0f);
+  float raf = (float)ra;
+  if ((double)raf < ra) raf = nextafterf(raf, 1e30f);
+  S.lim = lim;
+  S.pass_below = pbf;
+  S.reject_above = nextafterf(raf, 1e30f);
+}
+
+extern "C" int bs_hall_filter_noalloc(int n, const uint64_t *d_bits, long long npairs,
+                                      uint8_t *d_pass, void *stream) {
+  if (n < 4 || n + 1 > BS_MAXL || npairs < 0 || (npairs && (!d_bits || !d_pass))) return BS_ERR_ARG;
+  if (npairs > NOALLOC_MAX_PAIRS) return BS_ERR_CAP;  // beyond the fixed scratch size
+  cudaStream_t s = (cudaStream_t)stream;
+  int dev = 0;
+  CK(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return BS_ERR_ARG;
+  std::lock_guard<std::mutex> lock(g_na_mutex);
+  NoallocDevice &S = g_na[dev];
+  if (!S.scratch) {  // set-up, once per device, with that device current
+    void *p = nullptr;
+    CK(cudaGetSymbolAddress(&p, g_hall_noalloc_scratch));
+    S.scratch = (unsigned char *)p;
+    S.n = 0;
+    CK(cudaFuncSetAttribute(hall_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                            (int)tc_smem_bytes(2)));
+    CK(cudaFuncSetAttribute(hall_fp64_recheck_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                            (int)(sizeof(double) * 2 * 200 * BS_MAXL)));
+  }
+  if (S.n != n) {  // tables of another length: rebuild and upload (no device allocation)
+    noalloc_tables(n, S);
+    CK(cudaMemcpyAsync(S.scratch + NA_COS_OFF, g_na_cos, sizeof g_na_cos, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(S.scratch + NA_SIN_OFF, g_na_sin, sizeof g_na_sin, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(S.scratch + NA_IMG_OFF, g_na_img, sizeof g_na_img, cudaMemcpyHostToDevice, s));
+    CK(cudaStreamSynchronize(s));  // the host staging arrays are reused by the next call
+    S.n = n;
+  }
+  unsigned long long *count = (unsigned long long *)(S.scratch + NA_COUNT_OFF);
+  int *status = (int *)(S.scratch + NA_STATUS_OFF);
+  CK(cudaMemsetAsync(S.scratch, 0, 128, s));  // counters and status start at zero
+  if (npairs > 0) {
+    TcParams P;
+    P.bits = d_bits;
+    P.npairs = npairs;
+    P.ntiles = (npairs + 63) / 64;
+    P.image = S.scratch + NA_IMG_OFF;
+    P.nparts = 1;
+    P.ksteps = (n + 15) / 16;
+    P.idesc = (1u << 4) | ((uint32_t)(BS_TC_COLS >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
+    P.one2 = 0x3C003C00u;
+    P.pass_below = S.pass_below;
+    P.reject_above = S.reject_above;
+    P.pass = d_pass;
+    P.unc = (unsigned *)(S.scratch + NA_UNC_OFF);
+    P.unc_cap = (unsigned long long)NOALLOC_MAX_PAIRS;
+    P.count = count;
+    P.status = status;
+    P.dump = nullptr;
+    int dev_sms = 0;
+    CK(cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, dev));
+    const long long grid = P.ntiles < dev_sms ? P.ntiles : dev_sms;
+    hall_tc_kernel<<<(int)grid, TC_THREADS, tc_smem_bytes(1), s>>>(P);
+    CK(cudaGetLastError());
+    hall_fp64_recheck_kernel<<<dev_sms, 256, sizeof(double) * 2 * 200 * n, s>>>(
+        d_bits, P.unc, count, (unsigned long long)NOALLOC_MAX_PAIRS, n, S.lim,
+        (const double *)(S.scratch + NA_COS_OFF), (const double *)(S.scratch + NA_SIN_OFF), d_pass,
+        count + 1);
+    CK(cudaGetLastError());
+  }
+  int st = 0;
+  CK(cudaMemcpyAsync(&st, status, sizeof(int), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  return st ? st : BS_OK;
 }

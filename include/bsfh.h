@@ -81,6 +81,23 @@ int bs_hall_filter_packed(bs_ctx *ctx, const uint64_t *bits, long long npairs, i
  * be NULL) is filled after a stream synchronise when non-NULL. */
 int bs_hall_filter_dev(bs_ctx *ctx, const uint64_t *d_bits, long long npairs, int mode,
                        uint8_t *d_pass, bs_hall_stats *stats);
+/* Allocation-free form of bs_hall_filter_dev (tensor-core fp16 form + FP64 recheck of the
+ * margin band), for callers that may not allocate device memory: code running under a
+ * device-memory budget owned by a scheduler or host framework, or latency-sensitive code in
+ * the middle of overlapped multi-stream work, where cudaMalloc / cudaFree would synchronise
+ * the device. No counterpart in the reference. It needs no context and allocates nothing:
+ * its scratch (band list, counters, status word, tables) is one fixed static device array of
+ * about 4.2 MiB, which every GPU that loads the library keeps until the process exits.
+ * n is the sequence length (4 <= n <= 63); d_bits holds 2 words per pair and d_pass
+ * receives the decisions, both device memory owned by the caller; at most 1,048,576 pairs
+ * per call (BS_ERR_CAP beyond). The work is enqueued on `stream` (a cudaStream_t; NULL is
+ * the legacy default stream) and the call waits for it to return the status. The first call
+ * on a device, and the first call with a new n, set the scratch up (device symbol address,
+ * tables); make that first call before any stream capture. Calls share the one array and
+ * keep the last call's tables: calls that overlap on the GPU (other streams, other host
+ * threads) race and must be serialised by the caller. */
+int bs_hall_filter_noalloc(int n, const uint64_t *d_bits, long long npairs, uint8_t *d_pass,
+                           void *stream);
 /* Diagnostics: raw tensor-core accumulators for npairs (multiple of 64, <= 65536) pairs,
  * d_acc[row][208] fp32 with row 2p = C of pair p, 2p+1 = D; columns 0..100 are Re at the
  * unique angles j = 1..100, 200 and columns 104..204 the matching Im. */
