@@ -192,19 +192,137 @@ def run_stream_only(args):
     from bs45_quantum_explorer_gb300.hall import Context
     from bs45_quantum_explorer_gb300.stream import cd_stream
     n, sig, px, py, pi = STREAM_CELLS[args.stream_only]
+    limit = args.limit if args.limit is not None else (0 if n <= 30 else 500000)
     ctx = Context(n, sig)
-    cd_stream(ctx, [(px, py)], m=6, as_words=True)  # warm-up
+    cd_stream(ctx, [(px, py)], m=6, as_words=True, limit=min(limit, 1000) if limit else 0)  # warm-up
     torch.cuda.synchronize()
     ctx.timing(True)
     t0 = time.perf_counter()
-    surv, _, st = cd_stream(ctx, [(px, py)], m=6, as_words=True)
+    surv, _, st = cd_stream(ctx, [(px, py)], m=6, as_words=True, limit=limit)
     dt = time.perf_counter() - t0
     kms, kl, _ = ctx.timing_read()
-    print(json.dumps({"workload": f"C,D stream, n={n} sig={sig} raw cell {pi} px={px} py={py}",
+    what = "whole cell" if not limit else f"first {limit} survivors (front-only cut)"
+    print(json.dumps({"workload": f"C,D stream, n={n} sig={sig} raw cell {pi} px={px} py={py}, {what}",
                       "dfs_nodes": st[0]["nodes"], "leaves": st[0]["leaves"], "survivors": len(surv),
                       "seconds": dt, "nodes_per_s": st[0]["nodes"] / dt, "device_kernel_ms": kms,
                       "timed_launches": kl}), flush=True)
     ctx.close()
+
+
+# ---- first-hit pipeline at n = 36: a seeded window of 4096 raw cells ----
+FH_N, FH_SIG = 36, (5, 11, 0, 0)
+
+
+def _classes(n):
+    out = []
+    for a in range((n + 1) % 2, n + 2, 2):
+        for b in range(a, n + 2, 2):
+            for c in range(n % 2, n + 1, 2):
+                rest = 4 * n + 2 - a * a - b * b - c * c
+                if rest < c * c:
+                    break
+                d = int(round(rest ** 0.5))
+                if d * d == rest and d >= c and (d - n) % 2 == 0:
+                    out.append((a, b, c, d))
+    return out
+
+
+def run_first_hit(seconds, cpu_seconds=10.0, with_cpu=True):
+    """One production lane (orbit canon + quad switch + Q-prune, ORDER=3; budget 2^22,
+    BUF_CAP 500,000, DRAIN_TOP 50,000) over raw cells [s, s+4096) of n = 36, sig (5,11,0,0),
+    s drawn from the seed; stopped between cells after `seconds`. Reports the completer's
+    A,B nodes/s (the reference's node definition) on the device and through the API, the
+    stream's DFS nodes/s, and the oracle completer on the same candidates on one host core."""
+    import numpy as np
+    import torch
+    from bs45_quantum_explorer_gb300.complete import flat_topk
+    from bs45_quantum_explorer_gb300.hall import Context
+    from bs45_quantum_explorer_gb300.serve import serving_list
+    from bs45_quantum_explorer_gb300.lane import run_lane
+    from bs45_quantum_explorer_gb300.stream import cd_stream
+    t0 = time.perf_counter()
+    listing = serving_list(FH_N, FH_SIG)
+    list_s = time.perf_counter() - t0
+    cells, kept, digest, m = listing
+    rng = np.random.default_rng(SEED)
+    s = int(rng.integers(0, len(kept) - 4096))
+    ctx = Context(FH_N, FH_SIG)
+    kw = dict(budget=1 << 22, buf_cap=500000, drain_top=50000, listing=listing)
+    run_lane(ctx, FH_N, FH_SIG, skip=s, end=s + 1, **kw)  # warm-up: buffers, first cell
+    torch.cuda.synchronize()
+    res = run_lane(ctx, FH_N, FH_SIG, skip=s, end=s + 4096, max_seconds=seconds, **kw)
+    out = {"workload": f"first-hit lane, n={FH_N} sig={FH_SIG}, raw cells [{s}, {s + 4096}) of the "
+                       f"ORDER=3 list (digest {digest}, {int(kept[s:s + 4096].sum())} kept cells), "
+                       "budget 2^22, BUF_CAP 500000, DRAIN_TOP 50000",
+           "bounded_seconds": seconds, "list_build_s": round(list_s, 2),
+           "cells_done": res.cells_done, "cells_orbit_dup": res.cells_orbit_dup,
+           "cells_prof_dead": res.cells_prof_dead, "completions": res.completions,
+           "ab_nodes": res.total_ab_nodes, "budget_aborted": res.budget_aborted,
+           "completer_device_s": res.complete_device_ms * 1e-3, "completer_api_s": res.complete_s,
+           "ab_nodes_per_s_device": res.total_ab_nodes / (res.complete_device_ms * 1e-3)
+           if res.complete_device_ms > 0 else None,
+           "ab_nodes_per_s_api": res.total_ab_nodes / res.complete_s if res.complete_s > 0 else None,
+           "dfs_nodes": res.dfs_nodes, "stream_s": res.stream_s,
+           "dfs_nodes_per_s": res.dfs_nodes / res.stream_s if res.stream_s > 0 else None,
+           "wall_s": res.timings.get("wall_s"), "found": res.found}
+    if res.found:
+        out["hit"] = {"idx": res.hit_idx, "profile_rank": res.profile_rank,
+                      "quad": [list(map(int, x)) for x in res.quad]}
+    if with_cpu:
+        # the oracle completer on the first drained candidates of the window's first kept cell
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import pyoracle
+        from bs45_quantum_explorer_gb300.cells import ab_rows
+        from bs45_quantum_explorer_gb300.hall import unpack
+        pi = next(i for i in range(s, s + 4096) if kept[i])
+        c = cells[pi]
+        rows, off, nr = ab_rows(FH_N, FH_SIG, m, [c])
+        surv, _, _ = cd_stream(ctx, [(list(c.tx[:m]), list(c.ty[:m]))], m=m, as_words=True, limit=500000)
+        order, _ = flat_topk(ctx, surv, len(surv), 50000)
+        cand = unpack(surv[order], FH_N)
+        r = rows[off[0]:off[0] + nr[0]] if 0 < nr[0] <= 20000 else None
+        nodes, done, t1 = 0, 0, time.perf_counter()
+        while done < len(cand) and time.perf_counter() - t1 < cpu_seconds:
+            _, nd, _, _ = pyoracle.complete_ab(FH_N, FH_SIG[0], FH_SIG[1], cand[done, 0], cand[done, 1],
+                                               1 << 22, rows=r, m=m)
+            nodes += nd
+            done += 1
+        dt = time.perf_counter() - t1
+        out["cpu_baseline"] = {"value": nodes / dt, "unit": "A,B nodes/s", "cores": 1, "kind": "port",
+                               "sample": f"the oracle completer on the first {done} drained candidates "
+                                         f"of raw cell {pi} ({dt:.1f} s, budget 2^22); the reference "
+                                         "runs one lane per core"}
+    ctx.close()
+    return out
+
+
+def run_serving(n_jobs=12, tail=2, rate=2.0, slots=4, max_cells=64):
+    """C5: a seeded Poisson stream of first-hit jobs, n uniform in 20..42 with a signature from
+    classes(n) and a contiguous ORDER=3 range of 1..max_cells raw cells, plus `tail` n = 42
+    ranges; per-job budget 2^16, BUF_CAP 2000, DRAIN_TOP 64 (reduced from the production lane
+    so the mix finishes in about a minute). Lists are built before the clock starts, in
+    parallel (a service keeps them). Reports cells/s, nodes/s and p50/p99 job latency."""
+    import concurrent.futures as cf
+    from bs45_quantum_explorer_gb300.serve import Server, poisson_trace, serving_list
+    plan = poisson_trace(nj=n_jobs, rate=rate, seed=SEED, n_range=(20, 42), max_cells=max_cells,
+                         tail_n42=tail, classes=_classes, ncells_of=lambda n, sg: 1 << 30)
+    t0 = time.perf_counter()
+    keys = sorted({(j.n, j.sig) for j in plan})
+    with cf.ThreadPoolExecutor(max_workers=min(16, len(keys))) as ex:
+        lists = dict(zip(keys, ex.map(lambda k: serving_list(*k), keys)))
+    list_s = time.perf_counter() - t0
+    jobs = poisson_trace(nj=n_jobs, rate=rate, seed=SEED, n_range=(20, 42), max_cells=max_cells,
+                         tail_n42=tail, classes=_classes, ncells_of=lambda n, sg: len(lists[(n, sg)][1]),
+                         budget=1 << 16, buf_cap=2000, drain_top=64)
+    srv = Server(slots=slots)
+    out, st = srv.run_trace(jobs)
+    d = st.as_dict()
+    d.update({"workload": f"{len(jobs)} jobs ({tail} of them n=42), Poisson rate {rate}/s, seed {SEED:#x}, "
+                          f"{slots} slots; ranges of 1..{max_cells} raw cells; budget 2^16, BUF_CAP 2000, "
+                          "DRAIN_TOP 64", "lists_prebuilt_s": round(list_s, 2),
+              "errors": sum(1 for j in out if j.error), "found": sum(1 for j in out if j.result and j.result.found),
+              "peak_hbm_admitted_bytes": srv.peak_in_use})
+    return d
 
 
 def main():
@@ -217,8 +335,15 @@ def main():
     ap.add_argument("--mode", default="tc_fp16", choices=["tc_fp16", "tc_bf16x2", "fp64"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true")
+    ap.add_argument("--limit", type=int, default=None,
+                    help="with --stream-only: stop after this many survivors (0: whole cell)")
     ap.add_argument("--stream-only", choices=["n30", "n42"], default=None,
                     help="stream one built-in cell only (a small case for profiling)")
+    ap.add_argument("--first-hit", type=float, default=None, metavar="SECONDS",
+                    help="run only the n=36 first-hit lane for about SECONDS and print its line")
+    ap.add_argument("--serve", action="store_true", help="run only the serving mix and print its line")
+    ap.add_argument("--fh-seconds", type=float, default=30.0,
+                    help="bound on the first-hit lane inside the default run")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     rank = env_int("RANK", 0)
@@ -230,6 +355,14 @@ def main():
         return
     if args.stream_only:
         run_stream_only(args)
+        return
+    if args.first_hit is not None or args.serve:
+        from bs45_quantum_explorer_gb300 import build_library
+        build_library()
+        if args.first_hit is not None:
+            print(json.dumps(run_first_hit(args.first_hit)), flush=True)
+        if args.serve:
+            print(json.dumps(run_serving()), flush=True)
         return
 
     import numpy as np
@@ -402,24 +535,39 @@ def main():
         # ---- search nodes/s: the C,D stream of one n = 42 cell (DFS + Hall + order) ----
         from bs45_quantum_explorer_gb300.stream import cd_stream
         cell42 = ([-1, -1, 1, 1, 1, -1], [-1, -3, 1, 1, 3, -1])  # ORDER=3 raw cell 3056, sig (7,11,0,0)
-        cd_stream(ctx, [cell42], m=6, as_words=True)  # warm-up (frontier, buffers)
+        SEARCH_LIMIT = 50000  # the cell holds > 10^13 nodes: stream its first survivors
+        cd_stream(ctx, [cell42], m=6, as_words=True, limit=100)  # warm-up (frontier, buffers)
         torch.cuda.synchronize()
         ctx.timing(True)
         t0 = time.perf_counter()
-        surv, _, sst = cd_stream(ctx, [cell42], m=6, as_words=True)
+        surv, _, sst = cd_stream(ctx, [cell42], m=6, as_words=True, limit=SEARCH_LIMIT)
         dt = time.perf_counter() - t0
         dfs_ms, dfs_launches, _ = ctx.timing_read()
         ctx.timing(False)
         nodes = sst[0]["nodes"]
+        # the same search with the FP64-only Hall form on the leaves
+        t1 = time.perf_counter()
+        surv64, _, sst64 = cd_stream(ctx, [cell42], m=6, as_words=True, limit=SEARCH_LIMIT,
+                                     hall_mode="fp64")
+        dt64 = time.perf_counter() - t1
         line["search"] = {
             "workload": "C,D stream of the n=42 cell px=(-1,-1,1,1,1,-1) py=(-1,-3,1,1,3,-1) "
-                        "(ORDER=3 raw cell 3056 of sig (7,11,0,0)), whole cell",
+                        "(ORDER=3 raw cell 3056 of sig (7,11,0,0)), its first 50,000 survivors "
+                        "in stream order (the lane's front-only cut)",
             "dfs_nodes": nodes, "leaves": sst[0]["leaves"], "survivors": int(len(surv)),
             "seconds": dt, "nodes_per_s": nodes / dt, "leaves_per_s": sst[0]["leaves"] / dt,
             "device_kernel_ms": dfs_ms, "timed_launches": dfs_launches,
             "device_nodes_per_s": nodes / (dfs_ms * 1e-3) if dfs_ms > 0 else None,
+            "filtered_cands_per_s": sst[0]["leaves"] / dt,
+            "fp64_hall_form": {"seconds": dt64, "nodes_per_s": sst64[0]["nodes"] / dt64,
+                               "filtered_cands_per_s": sst64[0]["leaves"] / dt64,
+                               "tc_speedup": dt64 / dt,
+                               "survivors_identical": bool(np.array_equal(surv64, surv))},
             "reference_single_core": "14,736,335,258 nodes, 448,271,835 leaves, 5,613 survivors "
                                      "in 348.9 s (42.2 M nodes/s, one Xeon core; run interrupted)"}
+        # ---- the n = 36 first-hit lane (bounded) and the serving mix ----
+        line["first_hit"] = run_first_hit(args.fh_seconds, with_cpu=not args.no_cpu_baseline)
+        line["serving"] = run_serving()
         if not args.no_cpu_baseline:
             rate, samp, thr, dt = cpu_hall_rate(os.cpu_count() or 1)
             line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": thr, "kind": "port",

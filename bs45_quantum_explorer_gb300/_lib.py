@@ -41,7 +41,7 @@ class StreamOpts(C.Structure):
     _fields_ = [("m", C.c_int32), ("rev", C.c_int32), ("endpos", C.c_int32),
                 ("cd_prune", C.c_int32), ("hall_mode", C.c_int32), ("ab_side", C.c_int32),
                 ("target_prefixes", C.c_longlong), ("leaf_chunk", C.c_longlong),
-                ("survivor_cap", C.c_longlong)]
+                ("survivor_cap", C.c_longlong), ("limit", C.c_longlong)]
 
 
 class CellStats(C.Structure):
@@ -72,6 +72,7 @@ SIGNATURES = {
     "bs_strerror": (C.c_char_p, [C.c_int]),
     "bs_ctx_create": (C.c_int, [C.c_int] * 6 + [C.POINTER(C.c_void_p)]),
     "bs_ctx_destroy": (None, [C.c_void_p]),
+    "bs_ctx_retarget": (C.c_int, [C.c_void_p] + [C.c_int] * 5),
     "bs_ctx_set_stream": (C.c_int, [C.c_void_p, C.c_void_p]),
     "bs_ctx_device_status": (C.c_int, [C.c_void_p]),
     "bs_hall_filter_batch": (C.c_int, [C.c_void_p, C.c_void_p, C.c_longlong, C.c_int, C.c_void_p,

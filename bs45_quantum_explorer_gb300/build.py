@@ -1,4 +1,4 @@
-"""In-tree build of libbsfh.so (sm_103a) and of the C++ host driver.
+"""In-tree build of libbsfh.so (sm_103a) and of the C++ lane binary.
 
 Each .cu translation unit is compiled in parallel with
 `nvcc -gencode arch=compute_103a,code=sm_103a -O3 -lineinfo`, then linked as a shared

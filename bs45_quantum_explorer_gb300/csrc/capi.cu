@@ -132,7 +132,7 @@ static int build_tc_form(bs_ctx *ctx, const double *ct, const double *st, int mo
     }
   }
   e = e * (1.0 + 1e-9) + 1e-12;
-  // Certified thresholds on the fp32 pair PSD pf_c (derivation in the design doc):
+  // Certified thresholds on the fp32 pair PSD pf_c:
   //   |pf_exact - pf_q| <= 4 e sqrt(pf_q) + 4 e^2, |pf_c - pf_q| <= rho pf_q (kappa = 1+4 rho),
   //   |pf_ref - pf_exact| <= eps64 (FP64 rounding of the reference and twin-angle spread).
   const double eps64 = 1e-9, rho = ldexp(1.0, -20), kappa = 1.0 + 4.0 * rho;
@@ -149,35 +149,24 @@ static int build_tc_form(bs_ctx *ctx, const double *ct, const double *st, int mo
   F.quant_err = e;
   F.pass_below = pbf;
   F.reject_above = raf;
-  cudaError_t ce = cudaMalloc(&F.d_image, bytes);
-  if (ce != cudaSuccess) { free(img); return bs_cuda_fail(ce); }
-  ce = cudaMemcpy(F.d_image, img, bytes, cudaMemcpyHostToDevice);
+  cudaError_t ce = cudaSuccess;
+  if (!F.d_image) ce = cudaMalloc(&F.d_image, bytes);  // one size per form: kept on retarget
+  if (ce == cudaSuccess) ce = cudaMemcpyAsync(F.d_image, img, bytes, cudaMemcpyHostToDevice, ctx->stream);
+  if (ce == cudaSuccess) ce = cudaStreamSynchronize(ctx->stream);
   free(img);
   if (ce != cudaSuccess) return bs_cuda_fail(ce);
   return BS_OK;
 }
 
-extern "C" int bs_ctx_create(int n, int a, int b, int c, int d, int device, bs_ctx **out) {
-  if (!out) return BS_ERR_ARG;
-  *out = nullptr;
-  if (n < 4 || n + 1 > BS_MAXL) return BS_ERR_ARG;
-  if (a * a + b * b + c * c + d * d != 4 * n + 2) return BS_ERR_ARG;
-  int ndev = 0;
-  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= device || device < 0) return BS_ERR_NODEV;
-  cudaDeviceProp prop;
-  CK(cudaGetDeviceProperties(&prop, device));
-  if (prop.major != 10 || prop.minor != 3) return BS_ERR_NODEV;
-  CK(cudaSetDevice(device));
-  bs_ctx *ctx = (bs_ctx *)calloc(1, sizeof(bs_ctx));
-  if (!ctx) return BS_ERR_NOMEM;
+// Loads the tables of BS(n+1,n) into a context whose stream and buffers exist: host tables
+// exactly as init_hall_tables builds them (wz_match.cpp:106-114), their FP64 copies and the
+// tensor-core images for both sequence lengths (C,D: n; A,B: n+1).
+static int load_tables(bs_ctx *ctx, int n, int a, int b, int c, int d) {
   ctx->n = n; ctx->n1 = n + 1;
   ctx->sig[0] = a; ctx->sig[1] = b; ctx->sig[2] = c; ctx->sig[3] = d;
-  ctx->device = device;
-  ctx->num_sms = prop.multiProcessorCount;
   ctx->lim = (4.0 * n + 2.0) + 0.5;
   int rc = BS_OK;
-  // Host tables exactly as init_hall_tables builds them (wz_match.cpp:106-114).
-  int w = n + 1;
+  const int w = n + 1;
   double *ct = (double *)calloc((size_t)201 * w, sizeof(double));
   double *st = (double *)calloc((size_t)201 * w, sizeof(double));
   double *gc = (double *)calloc((size_t)200 * BS_MAXL, sizeof(double));
@@ -193,27 +182,61 @@ extern "C" int bs_ctx_create(int n, int a, int b, int c, int d, int device, bs_c
         gs[(size_t)(j - 1) * BS_MAXL + i] = st[(size_t)j * w + i];
       }
     }
-    cudaError_t e1 = cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking);
-    ctx->stream = ctx->own_stream;
-    if (e1 == cudaSuccess) e1 = cudaMalloc(&ctx->d_cos, sizeof(double) * 200 * BS_MAXL);
-    if (e1 == cudaSuccess) e1 = cudaMalloc(&ctx->d_sin, sizeof(double) * 200 * BS_MAXL);
-    if (e1 == cudaSuccess) e1 = cudaMemcpy(ctx->d_cos, gc, sizeof(double) * 200 * BS_MAXL, cudaMemcpyHostToDevice);
-    if (e1 == cudaSuccess) e1 = cudaMemcpy(ctx->d_sin, gs, sizeof(double) * 200 * BS_MAXL, cudaMemcpyHostToDevice);
-    if (e1 == cudaSuccess) e1 = cudaMalloc(&ctx->d_status, sizeof(int));
-    if (e1 == cudaSuccess) e1 = cudaMemset(ctx->d_status, 0, sizeof(int));
-    if (e1 == cudaSuccess) e1 = cudaMalloc(&ctx->d_count, sizeof(unsigned long long) * 8);
+    cudaError_t e1 = cudaMemcpyAsync(ctx->d_cos, gc, sizeof(double) * 200 * BS_MAXL, cudaMemcpyHostToDevice, ctx->stream);
+    if (e1 == cudaSuccess) e1 = cudaMemcpyAsync(ctx->d_sin, gs, sizeof(double) * 200 * BS_MAXL, cudaMemcpyHostToDevice, ctx->stream);
+    if (e1 == cudaSuccess) e1 = cudaStreamSynchronize(ctx->stream);
     if (e1 != cudaSuccess) rc = bs_cuda_fail(e1);
   }
-  // both sequence lengths: C,D (n) and A,B (n+1)
   if (rc == BS_OK) rc = build_tc_form(ctx, ct, st, BS_HALL_TC_FP16, n, ctx->tc[BS_HALL_TC_FP16]);
   if (rc == BS_OK) rc = build_tc_form(ctx, ct, st, BS_HALL_TC_BF16X2, n, ctx->tc[BS_HALL_TC_BF16X2]);
   if (rc == BS_OK) rc = build_tc_form(ctx, ct, st, BS_HALL_TC_FP16, n + 1, ctx->tc_ab[BS_HALL_TC_FP16]);
   if (rc == BS_OK)
     rc = build_tc_form(ctx, ct, st, BS_HALL_TC_BF16X2, n + 1, ctx->tc_ab[BS_HALL_TC_BF16X2]);
   free(ct); free(st); free(gc); free(gs);
+  return rc;
+}
+
+extern "C" int bs_ctx_create(int n, int a, int b, int c, int d, int device, bs_ctx **out) {
+  if (!out) return BS_ERR_ARG;
+  *out = nullptr;
+  if (n < 4 || n + 1 > BS_MAXL) return BS_ERR_ARG;
+  if (a * a + b * b + c * c + d * d != 4 * n + 2) return BS_ERR_ARG;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= device || device < 0) return BS_ERR_NODEV;
+  cudaDeviceProp prop;
+  CK(cudaGetDeviceProperties(&prop, device));
+  if (prop.major != 10 || prop.minor != 3) return BS_ERR_NODEV;
+  CK(cudaSetDevice(device));
+  bs_ctx *ctx = (bs_ctx *)calloc(1, sizeof(bs_ctx));
+  if (!ctx) return BS_ERR_NOMEM;
+  ctx->device = device;
+  ctx->num_sms = prop.multiProcessorCount;
+  int rc = BS_OK;
+  cudaError_t e1 = cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking);
+  ctx->stream = ctx->own_stream;
+  if (e1 == cudaSuccess) e1 = cudaMalloc(&ctx->d_cos, sizeof(double) * 200 * BS_MAXL);
+  if (e1 == cudaSuccess) e1 = cudaMalloc(&ctx->d_sin, sizeof(double) * 200 * BS_MAXL);
+  if (e1 == cudaSuccess) e1 = cudaMalloc(&ctx->d_status, sizeof(int));
+  if (e1 == cudaSuccess) e1 = cudaMemset(ctx->d_status, 0, sizeof(int));
+  if (e1 == cudaSuccess) e1 = cudaMalloc(&ctx->d_count, sizeof(unsigned long long) * 8);
+  if (e1 != cudaSuccess) rc = bs_cuda_fail(e1);
+  if (rc == BS_OK) rc = load_tables(ctx, n, a, b, c, d);
   if (rc != BS_OK) { bs_ctx_destroy(ctx); return rc; }
   *out = ctx;
   return BS_OK;
+}
+
+extern "C" int bs_ctx_retarget(bs_ctx *ctx, int n, int a, int b, int c, int d) {
+  if (!ctx) return BS_ERR_ARG;
+  if (n < 4 || n + 1 > BS_MAXL) return BS_ERR_ARG;
+  if (a * a + b * b + c * c + d * d != 4 * n + 2) return BS_ERR_ARG;
+  CK(cudaSetDevice(ctx->device));
+  CK(cudaStreamSynchronize(ctx->stream));  // earlier work may still read the old tables
+  if (n == ctx->n) {
+    ctx->sig[0] = a; ctx->sig[1] = b; ctx->sig[2] = c; ctx->sig[3] = d;
+    return BS_OK;
+  }
+  return load_tables(ctx, n, a, b, c, d);
 }
 
 extern "C" void bs_ctx_destroy(bs_ctx *ctx) {

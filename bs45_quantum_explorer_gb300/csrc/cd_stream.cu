@@ -17,6 +17,9 @@
 #include <string.h>
 
 #include <algorithm>
+#include <cstdio>
+#include <chrono>
+#include <cmath>
 #include <vector>
 
 #include "bsfh_internal.cuh"
@@ -40,7 +43,7 @@ struct Saved {
   uint32_t prefix;
   uint32_t seq;        // leaves emitted so far inside this prefix
   uint16_t d, kk;
-  uint16_t pending;    // 1: child kk of node d is a leaf that was not yet written
+  uint16_t owed;       // leaf children of node d (bit k = child k) not yet written
   uint16_t pad;
   uint64_t dig[2];     // digits of depths 0..d-1 (4 bits each, depths 0-15 and 16-31)
 };
@@ -69,12 +72,16 @@ struct CdParams {
 };
 
 
-__device__ __forceinline__ int getdig(const uint64_t dig[2], int d) {
-  return (int)((dig[d >> 4] >> (4 * (d & 15))) & 15);
+// The digits of a walk live in two registers (depths 0-15 and 16-31); selecting between
+// them, rather than indexing an array, keeps them out of local memory.
+__device__ __forceinline__ int getdig(uint64_t d0, uint64_t d1, int d) {
+  const uint64_t w = (d < 16) ? d0 : d1;
+  return (int)((w >> (4 * (d & 15))) & 15);
 }
-__device__ __forceinline__ void setdig(uint64_t dig[2], int d, int v) {
-  int w = d >> 4, s = 4 * (d & 15);
-  dig[w] = (dig[w] & ~(15ULL << s)) | ((uint64_t)v << s);
+__device__ __forceinline__ void setdig(uint64_t &d0, uint64_t &d1, int d, int v) {
+  const int s = 4 * (d & 15);
+  if (d < 16) d0 = (d0 & ~(15ULL << s)) | ((uint64_t)v << s);
+  else d1 = (d1 & ~(15ULL << s)) | ((uint64_t)v << s);
 }
 
 // Per-class feasibility as four "slack" words: for each class c (byte c, bias 64)
@@ -137,7 +144,11 @@ __device__ __forceinline__ void middle_bits(const Walk &w, int half, int cm, uin
   if (dy > 0) ly |= 1ULL << half;
 }
 
-__global__ void __launch_bounds__(256) cd_dfs_kernel(CdParams P) {
+// MINB: the blocks of 256 threads the register budget is set for (4: 64 registers, no spill;
+// 6: 40 registers with a few spills on the rare paths). The launch sizes the grid to the
+// blocks that are resident at once, so saved walks never wait for a block to be scheduled.
+template <int MINB>
+__global__ void __launch_bounds__(256, MINB) cd_dfs_kernel(CdParams P) {
   __shared__ QuadFx fx[32][16];
   __shared__ uint64_t posm[32];
   for (int t = threadIdx.x; t < 32 * 16; t += blockDim.x)
@@ -151,10 +162,10 @@ __global__ void __launch_bounds__(256) cd_dfs_kernel(CdParams P) {
   bool have = false;
   uint32_t prefix = 0, cell = 0, seq = 0;
   int D = 0, d = 0, kk = 0;
-  uint64_t dig[2] = {0, 0};
+  uint64_t dig0 = 0, dig1 = 0;
   Walk w;
   unsigned long long nodes = 0, leaves = 0;
-  bool pending = false;
+  uint32_t owed = 0;  // leaf children (bit k = child k) of the node at depth d not yet written
   int saved_slot = (int)(blockIdx.x * blockDim.x + threadIdx.x);
   unsigned iter = 0;
 
@@ -171,9 +182,9 @@ __global__ void __launch_bounds__(256) cd_dfs_kernel(CdParams P) {
         d = sv.d;
         kk = sv.kk;
         seq = sv.seq;
-        dig[0] = sv.dig[0];
-        dig[1] = sv.dig[1];
-        pending = sv.pending != 0;
+        dig0 = sv.dig[0];
+        dig1 = sv.dig[1];
+        owed = sv.owed;
       } else {
         if (*(volatile int *)P.full_flag) break;
         unsigned long long p = atomicAdd(P.next_prefix, 1ULL);
@@ -185,85 +196,102 @@ __global__ void __launch_bounds__(256) cd_dfs_kernel(CdParams P) {
         d = D;
         kk = 0;
         seq = 0;
-        dig[0] = pf.digits;
-        dig[1] = 0;
-        pending = false;
+        dig0 = pf.digits;
+        dig1 = 0;
+        owed = 0;
       }
       init_walk(w, P.cells[cell], L, m);
-      for (int t = 0; t < d; t++) place(w, fx[t][getdig(dig, t)]);
+      for (int t = 0; t < d; t++) place(w, fx[t][getdig(dig0, dig1, t)]);
       have = true;
     }
 
     // ---- one tree step ----
-    bool emit = false, finished = false;
-    uint64_t lx = 0, ly = 0;
-    if (pending) {
-      // the leaf that could not be written last time (its node is already counted)
-      const QuadFx &f = fx[d][kk];
-      place(w, f);
-      lx = w.X;
-      ly = w.Y;
-      if (L & 1) middle_bits(w, half, cm, lx, ly);
-      unplace(w, f, posm[d]);
-      emit = true;
-    } else if (kk == 8) {
-      if (d == D) {
-        finished = true;
-      } else {
-        d--;
-        kk = getdig(dig, d);
-        unplace(w, fx[d][kk], posm[d]);
-        kk++;
-      }
-    } else {
-      const QuadFx &f = fx[d][kk];
-      place(w, f);
-      nodes++;
-      if (!feasible(w, M)) {
-        unplace(w, f, posm[d]);
-        kk++;
+    bool finished = false;
+    if (owed == 0) {
+      if (kk == 8) {
+        if (d == D) {
+          finished = true;
+        } else {
+          d--;
+          kk = getdig(dig0, dig1, d);
+          unplace(w, fx[d][kk], posm[d]);
+          kk++;
+        }
       } else if (d + 1 == half) {
-        lx = w.X;
-        ly = w.Y;
-        if (L & 1) middle_bits(w, half, cm, lx, ly);
-        unplace(w, f, posm[d]);
-        emit = true;
+        // the children are leaves: test the remaining ones together (each is one node, as
+        // the reference counts them), then write the class-exact ones below
+        uint32_t lm = 0;
+        for (int k = kk; k < 8; k++) {
+          const QuadFx &f = fx[d][k];
+          const uint64_t a0 = w.s0 + (uint64_t)f.ds[0], a1 = w.s1 + (uint64_t)f.ds[1];
+          const uint64_t a2 = w.s2 + (uint64_t)f.ds[2], a3 = w.s3 + (uint64_t)f.ds[3];
+          if (((a0 & a1 & a2 & a3) & M) == M) lm |= 1u << k;
+        }
+        nodes += 8 - kk;
+        owed = lm;
+        kk = 8;
       } else {
-        setdig(dig, d, kk);
-        d++;
-        kk = 0;
-      }
-    }
-
-    // ---- warp-aggregated leaf append ----
-    const unsigned act = __activemask();
-    const unsigned ball = __ballot_sync(act, emit);
-    if (ball) {
-      const int leader = __ffs(ball) - 1;
-      unsigned long long base = 0;
-      if (lane == leader) base = atomicAdd(P.leaf_count, (unsigned long long)__popc(ball));
-      base = __shfl_sync(act, base, leader);
-      if (emit) {
-        const unsigned long long slot = base + __popc(ball & ((1u << lane) - 1u));
-        if (slot < P.leaf_cap) {
-          P.leaf_words[2 * slot] = lx;
-          P.leaf_words[2 * slot + 1] = ly;
-          P.leaf_keys[slot] = ((unsigned long long)prefix << 32) | seq;
-          seq++;
-          leaves++;
-          pending = false;
+        const QuadFx &f = fx[d][kk];
+        place(w, f);
+        nodes++;
+        if (!feasible(w, M)) {
+          unplace(w, f, posm[d]);
           kk++;
         } else {
-          pending = true;  // suspend below with this leaf still owed
-          atomicExch(P.full_flag, 1);
+          setdig(dig0, dig1, d, kk);
+          d++;
+          kk = 0;
         }
       }
     }
 
-    // ---- suspend after an unwritten leaf, or at a clean point once the buffer is full ----
+    // ---- warp-aggregated append of the owed leaves, in child order ----
+    // Each lane owes at most 8 leaves; four ballots of the count's bits give every lane its
+    // exclusive prefix and the warp total, so one atomic reserves the warp's slots.
+    const unsigned act = __activemask();
+    const unsigned cnt = (unsigned)__popc(owed);
+    const unsigned b0 = __ballot_sync(act, cnt & 1u), b1 = __ballot_sync(act, cnt & 2u);
+    const unsigned b2 = __ballot_sync(act, cnt & 4u), b3 = __ballot_sync(act, cnt & 8u);
+    const unsigned total = __popc(b0) + 2u * __popc(b1) + 4u * __popc(b2) + 8u * __popc(b3);
+    if (total) {
+      const unsigned lt = (1u << lane) - 1u;
+      const unsigned before = __popc(b0 & lt) + 2u * __popc(b1 & lt) + 4u * __popc(b2 & lt) +
+                              8u * __popc(b3 & lt);
+      const int leader = __ffs(act) - 1;
+      unsigned long long base = 0;
+      if (lane == leader) base = atomicAdd(P.leaf_count, (unsigned long long)total);
+      base = __shfl_sync(act, base, leader);
+      unsigned long long slot = base + before;
+      while (owed) {
+        if (slot >= P.leaf_cap) {
+          atomicExch(P.full_flag, 1);  // the rest stays owed: suspend below
+          break;
+        }
+        const int k = __ffs(owed) - 1;
+        const QuadFx &f = fx[d][k];
+        uint64_t lx = w.X | f.bx, ly = w.Y | f.by;
+        if (L & 1) {
+          Walk t;
+          t.s0 = w.s0 + (uint64_t)f.ds[0];
+          t.s1 = w.s1 + (uint64_t)f.ds[1];
+          t.s2 = w.s2 + (uint64_t)f.ds[2];
+          t.s3 = w.s3 + (uint64_t)f.ds[3];
+          middle_bits(t, half, cm, lx, ly);
+        }
+        P.leaf_words[2 * slot] = lx;
+        P.leaf_words[2 * slot + 1] = ly;
+        P.leaf_keys[slot] = ((unsigned long long)prefix << 32) | seq;
+        seq++;
+        leaves++;
+        slot++;
+        owed &= owed - 1;
+      }
+    }
+
+    // ---- suspend with leaves still owed, or at a clean point once the buffer is full ----
     iter++;
     const bool suspend = !finished &&
-                         (pending || ((iter & 255) == 0 && *(volatile int *)P.full_flag));
+                         (owed != 0 || ((iter & 255) == 0 && *(volatile int *)P.full_flag));
     if (suspend) {
       const unsigned k = atomicAdd(P.nsaved_out, 1u);
       if ((int)k < P.saved_cap) {
@@ -272,10 +300,10 @@ __global__ void __launch_bounds__(256) cd_dfs_kernel(CdParams P) {
         sv.seq = seq;
         sv.d = (uint16_t)d;
         sv.kk = (uint16_t)kk;
-        sv.pending = pending ? 1 : 0;
+        sv.owed = (uint16_t)owed;
         sv.pad = 0;
-        sv.dig[0] = dig[0];
-        sv.dig[1] = dig[1];
+        sv.dig[0] = dig0;
+        sv.dig[1] = dig1;
         P.saved_out[k] = sv;
       } else {
         atomicCAS(P.status, 0, BS_ERR_INTERNAL);
@@ -287,7 +315,7 @@ __global__ void __launch_bounds__(256) cd_dfs_kernel(CdParams P) {
       nodes = 0;
       leaves = 0;
       have = false;
-      pending = false;
+      owed = 0;
       if (suspend) break;
     }
   }
@@ -442,44 +470,73 @@ extern "C" int bs_cd_stream(bs_ctx *ctx, const bs_cell *cells, int ncells, const
   StreamBufs *B = bufs_of(ctx);
   const int half = L / 2;
 
-  // ---- frontier on the host ----
+  // ---- coarse frontier of each cell on the host, in the reference's order ----
+  // A Prefix holds the digits of 16 depths, so no prefix is deeper than that.
   static const HostQuads Q;
-  std::vector<Prefix> prefixes;
+  const int max_depth = std::min(half - 1, 16);
+  std::vector<Frontier> F(ncells);
+  std::vector<Prefix> coarse;
   std::vector<long long> host_nodes(ncells, 0);
   long long target = opt->target_prefixes > 0 ? opt->target_prefixes : 262144;
   long long per_cell_target = std::max<long long>(64, target / ncells);
+  int deepest = 1;
   for (int ci = 0; ci < ncells; ci++) {
     const bs_cell &c = cells[ci];
-    Frontier F;
-    F.L = L; F.m = m; F.half = half; F.rev = opt->rev; F.root = root_kind;
-    F.pinX = c.pinX; F.pinY = c.pinY;
-    F.ns0 = root_kind == 0 ? 16 : 8;
+    Frontier &f = F[ci];
+    f.L = L; f.m = m; f.half = half; f.rev = opt->rev; f.root = root_kind;
+    f.pinX = c.pinX; f.pinY = c.pinY;
+    f.ns0 = root_kind == 0 ? 16 : 8;
     for (int k = 0; k < m; k++) {
-      F.tot[k] = 0;
-      for (int p = k; p < L; p += m) F.tot[k]++;
+      f.tot[k] = 0;
+      for (int p = k; p < L; p += m) f.tot[k]++;
     }
-    F.tx = c.tx; F.ty = c.ty; F.Q = &Q; F.cell = (uint32_t)ci;
-    // deepen until the cell has enough prefixes or the split reaches depth half-1
+    f.tx = c.tx; f.ty = c.ty; f.Q = &Q; f.cell = (uint32_t)ci;
+    // deepen until the cell has enough prefixes or the split reaches the deepest prefix depth
     std::vector<Prefix> mine;
     int D = 1;
     for (;;) {
       mine.clear();
-      memset(F.px, 0, sizeof F.px); memset(F.py, 0, sizeof F.py); memset(F.placed, 0, sizeof F.placed);
-      F.D = D; F.nodes = 0; F.out = &mine;
-      F.rec(0, 0);
-      if ((long long)mine.size() >= per_cell_target || D >= half - 1 || mine.empty()) break;
+      memset(f.px, 0, sizeof f.px); memset(f.py, 0, sizeof f.py); memset(f.placed, 0, sizeof f.placed);
+      f.D = D; f.nodes = 0; f.out = &mine;
+      f.rec(0, 0);
+      if ((long long)mine.size() >= per_cell_target || D >= max_depth || mine.empty()) break;
       D++;
     }
-    host_nodes[ci] = F.nodes;
-    prefixes.insert(prefixes.end(), mine.begin(), mine.end());
+    deepest = std::max(deepest, D);
+    host_nodes[ci] = f.nodes;
+    coarse.insert(coarse.end(), mine.begin(), mine.end());
   }
-  const long long nprefix = (long long)prefixes.size();
-  if (nprefix >= (1LL << 32)) return BS_ERR_CAP;
+  const long long ncoarse = (long long)coarse.size();
+
+  // The subtrees of coarse prefix p, refined by k more levels: the fine prefixes of its
+  // subtree at depth p.depth + k, in stream order. Returns the host nodes it adds (the coarse
+  // node itself was counted when the frontier was built).
+  auto refine = [&](const Prefix &p, int k, std::vector<Prefix> &out) -> long long {
+    if (k <= 0) {
+      out.push_back(p);
+      return 0;
+    }
+    Frontier &f = F[p.cell];
+    memset(f.px, 0, sizeof f.px); memset(f.py, 0, sizeof f.py); memset(f.placed, 0, sizeof f.placed);
+    for (int t = 0; t < (int)p.depth; t++) {
+      const int(*S)[4] = (t == 0) ? (f.root == 2 ? Q.neg : (f.root == 1 ? Q.pos : Q.all)) : Q.pos;
+      const int ns = (t == 0) ? f.ns0 : 8;
+      const int kk = (int)((p.digits >> (4 * t)) & 15);
+      const int q = f.rev ? ns - 1 - kk : kk;
+      const int c1 = t % m, c2 = (L - 1 - t) % m;
+      f.px[c1] += S[q][0]; f.py[c1] += S[q][1]; f.px[c2] += S[q][2]; f.py[c2] += S[q][3];
+      f.placed[c1]++; f.placed[c2]++;
+    }
+    f.D = (int)p.depth + k;
+    f.out = &out;
+    const long long before = f.nodes;
+    f.rec((int)p.depth, p.digits);
+    return f.nodes - before - 1;
+  };
 
   // ---- device buffers ----
   int rc = bs_ensure_dev((void **)&B->cells, &B->cells_cap, ncells, sizeof(CellDev));
   if (!rc) rc = bs_ensure_dev((void **)&B->cell_stats, &B->cell_stats_cap, 3LL * ncells, sizeof(unsigned long long));
-  if (!rc && nprefix) rc = bs_ensure_dev((void **)&B->prefixes, &B->prefix_cap, nprefix, sizeof(Prefix));
   long long leaf_cap = opt->leaf_chunk > 0 ? opt->leaf_chunk : (1LL << 24);
   if (!rc) {
     long long c0 = B->leaf_cap;
@@ -492,7 +549,17 @@ extern "C" int bs_cd_stream(bs_ctx *ctx, const bs_cell *cells, int ncells, const
   }
   if (!rc) rc = bs_ensure_dev((void **)&B->leaf_pass, &B->pass_cap, leaf_cap, 1);
   const int block = 256;
-  const int grid = ctx->num_sms * 6;
+  // register budget variant (BS_DFS_BLOCKS=6 selects the 40-register one) and the grid of
+  // exactly the blocks that fit at once
+  static const int dfs_blocks = [] {
+    const char *e = getenv("BS_DFS_BLOCKS");
+    return (e && atoi(e) == 6) ? 6 : 4;
+  }();
+  auto dfs_kernel = dfs_blocks == 6 ? cd_dfs_kernel<6> : cd_dfs_kernel<4>;
+  int per_sm = 0;
+  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, dfs_kernel, block, 0));
+  if (per_sm < 1) per_sm = 1;
+  const int grid = ctx->num_sms * per_sm;
   const int saved_cap = grid * block;
   if (!rc && B->saved_cap < saved_cap) {
     cudaFree(B->saved[0]); cudaFree(B->saved[1]);
@@ -555,96 +622,164 @@ extern "C" int bs_cd_stream(bs_ctx *ctx, const bs_cell *cells, int ncells, const
   CK(cudaMemcpyAsync(B->fx, fxh.data(), sizeof(QuadFx) * fxh.size(), cudaMemcpyHostToDevice, s));
   CK(cudaMemcpyAsync(B->posm, posm.data(), sizeof(uint64_t) * 32, cudaMemcpyHostToDevice, s));
   CK(cudaMemcpyAsync(B->cells, hc.data(), sizeof(CellDev) * ncells, cudaMemcpyHostToDevice, s));
-  if (nprefix)
-    CK(cudaMemcpyAsync(B->prefixes, prefixes.data(), sizeof(Prefix) * nprefix, cudaMemcpyHostToDevice, s));
   CK(cudaMemsetAsync(B->cell_stats, 0, sizeof(unsigned long long) * 3 * ncells, s));
-  CK(cudaMemsetAsync(B->counters, 0, sizeof(unsigned long long) * 8, s));
-  // counters: [0] next prefix, [1] leaf count, [2] survivor count
+  // counters: [0] next prefix of the wave, [1] leaf count of the round, [2] survivors of the wave
   unsigned long long *cell_nodes = B->cell_stats, *cell_leaves = B->cell_stats + ncells,
                      *cell_ok = B->cell_stats + 2 * ncells;
 
-  int nsaved = 0, cur = 0;
-  long long rounds = 0;
-  while (nprefix > 0) {
-    CK(cudaMemsetAsync(B->nsaved, 0, sizeof(unsigned), s));
-    CK(cudaMemsetAsync(B->full, 0, sizeof(int), s));
-    CK(cudaMemsetAsync(B->counters + 1, 0, sizeof(unsigned long long), s));
-    CdParams P;
-    P.L = L; P.m = m; P.half = half;
-    P.feas_mask = feas;
-    P.fx = B->fx;
-    P.posmask = B->posm;
-    P.cells = B->cells; P.prefixes = B->prefixes; P.nprefix = nprefix;
-    P.next_prefix = B->counters;
-    P.saved_in = B->saved[cur]; P.nsaved_in = nsaved;
-    P.saved_out = B->saved[cur ^ 1]; P.nsaved_out = B->nsaved; P.saved_cap = saved_cap;
-    P.leaf_words = B->leaf_words; P.leaf_keys = B->leaf_keys;
-    P.leaf_count = B->counters + 1; P.leaf_cap = (unsigned long long)leaf_cap;
-    P.cell_nodes = cell_nodes; P.cell_leaves = cell_leaves;
-    P.full_flag = B->full; P.status = ctx->d_status;
-    bs_timed_begin(ctx);
-    cd_dfs_kernel<<<grid, block, 0, s>>>(P);
-    bs_timed_end(ctx);
-    CK(cudaGetLastError());
-    unsigned long long leaf_count = 0;
-    unsigned nsv = 0;
-    CK(cudaMemcpyAsync(&leaf_count, B->counters + 1, sizeof leaf_count, cudaMemcpyDeviceToHost, s));
-    CK(cudaMemcpyAsync(&nsv, B->nsaved, sizeof nsv, cudaMemcpyDeviceToHost, s));
-    CK(cudaStreamSynchronize(s));
-    if ((int)nsv > saved_cap) return BS_ERR_INTERNAL;
-    long long nleaf = (long long)std::min<unsigned long long>(leaf_count, (unsigned long long)leaf_cap);
-    if (nleaf > 0) {
-      int r2 = bs_hall_dev_len(ctx, B->leaf_words, nleaf, hall_mode, B->leaf_pass, L);
-      if (r2) return r2;
-      ctx->launches++;
-      compact_kernel<<<bs_grid_for(nleaf, 256, 8 * ctx->num_sms), 256, 0, s>>>(
-          B->leaf_words, B->leaf_keys, B->leaf_pass, nleaf, B->prefixes, B->surv_words, B->surv_keys,
-          B->counters + 2, (unsigned long long)surv_cap, cell_ok);
+  // ---- waves: runs of coarse prefixes, in stream order, refined to fill the GPU ----
+  // A wave's survivors all precede the next wave's, so each wave is ordered on its own and
+  // appended. The width (coarse prefixes per wave) and the refinement depth adapt to the
+  // nodes per coarse prefix seen so far: fine subtrees of ~FINE_NODES nodes, waves of
+  // ~WAVE_NODES nodes, and under `limit` no wider than the survivors still owed suggest.
+  const long long limit = opt->limit > 0 ? opt->limit : 0;
+  const double FINE_NODES = 2e4, WAVE_NODES = 8e9, NOMINAL_RATE = 2e10;
+  const long long threads = (long long)grid * block;
+  std::vector<uint64_t> res_words;
+  std::vector<uint32_t> res_cell;
+  std::vector<Prefix> fine;
+  std::vector<uint64_t> wkeys, wwords;
+  std::vector<unsigned long long> cs_prev(3 * (size_t)ncells, 0), cs(3 * (size_t)ncells, 0);
+  long long pos = 0, wave_width = std::min<long long>(ncoarse, 1024);
+  int k_refine = (half - deepest >= 6) ? 2 : 0;
+  long long have = 0;
+  static const bool trace = getenv("BS_STREAM_TRACE") != nullptr;  // per-wave figures on stderr
+  while (pos < ncoarse && !(limit && have >= limit)) {
+    const long long take = std::min<long long>(std::max<long long>(1, wave_width), ncoarse - pos);
+    fine.clear();
+    for (long long i = pos; i < pos + take; i++) {
+      const int k = std::min(k_refine, max_depth - (int)coarse[i].depth);
+      host_nodes[coarse[i].cell] += refine(coarse[i], k, fine);
+    }
+    pos += take;
+    const long long nprefix = (long long)fine.size();
+    if (nprefix == 0) continue;  // the refinement pruned the whole run
+    if (nprefix >= (1LL << 32)) return BS_ERR_CAP;
+    rc = bs_ensure_dev((void **)&B->prefixes, &B->prefix_cap, nprefix, sizeof(Prefix));
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(B->prefixes, fine.data(), sizeof(Prefix) * nprefix, cudaMemcpyHostToDevice, s));
+    CK(cudaMemsetAsync(B->counters, 0, sizeof(unsigned long long) * 8, s));
+    const auto t_wave = std::chrono::steady_clock::now();
+
+    int nsaved = 0, cur = 0;
+    for (;;) {
+      CK(cudaMemsetAsync(B->nsaved, 0, sizeof(unsigned), s));
+      CK(cudaMemsetAsync(B->full, 0, sizeof(int), s));
+      CK(cudaMemsetAsync(B->counters + 1, 0, sizeof(unsigned long long), s));
+      CdParams P;
+      P.L = L; P.m = m; P.half = half;
+      P.feas_mask = feas;
+      P.fx = B->fx;
+      P.posmask = B->posm;
+      P.cells = B->cells; P.prefixes = B->prefixes; P.nprefix = nprefix;
+      P.next_prefix = B->counters;
+      P.saved_in = B->saved[cur]; P.nsaved_in = nsaved;
+      P.saved_out = B->saved[cur ^ 1]; P.nsaved_out = B->nsaved; P.saved_cap = saved_cap;
+      P.leaf_words = B->leaf_words; P.leaf_keys = B->leaf_keys;
+      P.leaf_count = B->counters + 1; P.leaf_cap = (unsigned long long)leaf_cap;
+      P.cell_nodes = cell_nodes; P.cell_leaves = cell_leaves;
+      P.full_flag = B->full; P.status = ctx->d_status;
+      bs_timed_begin(ctx);
+      dfs_kernel<<<grid, block, 0, s>>>(P);
+      bs_timed_end(ctx);
       CK(cudaGetLastError());
-    }
-    rounds++;
-    nsaved = (int)nsv;
-    cur ^= 1;
-    if (nsaved == 0) {
-      unsigned long long nextp = 0;
-      CK(cudaMemcpyAsync(&nextp, B->counters, sizeof nextp, cudaMemcpyDeviceToHost, s));
+      unsigned long long leaf_count = 0;
+      unsigned nsv = 0;
+      CK(cudaMemcpyAsync(&leaf_count, B->counters + 1, sizeof leaf_count, cudaMemcpyDeviceToHost, s));
+      CK(cudaMemcpyAsync(&nsv, B->nsaved, sizeof nsv, cudaMemcpyDeviceToHost, s));
       CK(cudaStreamSynchronize(s));
-      if (nextp >= (unsigned long long)nprefix) break;
+      if ((int)nsv > saved_cap) return BS_ERR_INTERNAL;
+      long long nleaf = (long long)std::min<unsigned long long>(leaf_count, (unsigned long long)leaf_cap);
+      if (nleaf > 0) {
+        int r2 = bs_hall_dev_len(ctx, B->leaf_words, nleaf, hall_mode, B->leaf_pass, L);
+        if (r2) return r2;
+        ctx->launches++;
+        compact_kernel<<<bs_grid_for(nleaf, 256, 8 * ctx->num_sms), 256, 0, s>>>(
+            B->leaf_words, B->leaf_keys, B->leaf_pass, nleaf, B->prefixes, B->surv_words, B->surv_keys,
+            B->counters + 2, (unsigned long long)surv_cap, cell_ok);
+        CK(cudaGetLastError());
+      }
+      nsaved = (int)nsv;
+      cur ^= 1;
+      if (nsaved == 0) {
+        unsigned long long nextp = 0;
+        CK(cudaMemcpyAsync(&nextp, B->counters, sizeof nextp, cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        if (nextp >= (unsigned long long)nprefix) break;
+      }
     }
+
+    // ---- the wave's survivors, in stream order ----
+    unsigned long long nsurv = 0;
+    int status = 0;
+    CK(cudaMemcpyAsync(&nsurv, B->counters + 2, sizeof nsurv, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(&status, ctx->d_status, sizeof status, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(cs.data(), B->cell_stats, sizeof(unsigned long long) * 3 * ncells, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    if (status) {
+      cudaMemsetAsync(ctx->d_status, 0, sizeof(int), s);
+      return status;
+    }
+    if ((long long)nsurv > surv_cap) {
+      // one wave found more survivors than the device buffer holds: report the size to retry
+      // with (as survivor_cap; the output needs at least as much)
+      *nout = have + (long long)nsurv;
+      return BS_ERR_CAP;
+    }
+    if (nsurv > 0) {
+      wkeys.resize(nsurv);
+      wwords.resize(2 * nsurv);
+      CK(cudaMemcpyAsync(wkeys.data(), B->surv_keys, sizeof(uint64_t) * nsurv, cudaMemcpyDeviceToHost, s));
+      CK(cudaMemcpyAsync(wwords.data(), B->surv_words, sizeof(uint64_t) * 2 * nsurv, cudaMemcpyDeviceToHost, s));
+      CK(cudaStreamSynchronize(s));
+      std::vector<uint32_t> order(nsurv);
+      for (uint32_t i = 0; i < (uint32_t)nsurv; i++) order[i] = i;
+      std::sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) { return wkeys[a] < wkeys[b]; });
+      long long keep = (long long)nsurv;
+      if (limit) keep = std::min(keep, limit - have);
+      for (long long i = 0; i < keep; i++) {
+        res_words.push_back(wwords[2 * order[i]]);
+        res_words.push_back(wwords[2 * order[i] + 1]);
+        res_cell.push_back(fine[wkeys[order[i]] >> 32].cell);
+      }
+      have += keep;
+    }
+
+    // ---- size the next wave from what this one cost ----
+    const double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_wave).count();
+    unsigned long long wave_nodes = 0;
+    for (int ci = 0; ci < ncells; ci++) wave_nodes += cs[ci] - cs_prev[ci];
+    cs_prev = cs;
+    const double per_coarse = std::max(1.0, (double)wave_nodes / (double)take);
+    const double rate = std::max(NOMINAL_RATE, secs > 0 ? (double)wave_nodes / secs : 0.0);
+    k_refine = 0;
+    while (k_refine < 16 && per_coarse / std::pow(8.0, k_refine) > FINE_NODES) k_refine++;
+    double width = std::max(WAVE_NODES, rate * 0.25) / per_coarse;
+    // enough fine prefixes for every thread, twice over
+    width = std::max(width, 2.0 * (double)threads / std::pow(8.0, k_refine));
+    if (limit && nsurv > 0) {
+      const double per_coarse_surv = (double)nsurv / (double)take;
+      width = std::min(width, std::max(64.0, 1.5 * (double)(limit - have) / per_coarse_surv));
+    }
+    wave_width = (long long)std::min<double>(width, (double)(1LL << 40));
+    if (trace)
+      fprintf(stderr, "[bs_cd_stream] wave coarse=%lld fine=%lld nodes=%llu surv=%llu have=%lld "
+                      "secs=%.4f next_width=%lld next_k=%d pos=%lld/%lld\n",
+              take, nprefix, wave_nodes, nsurv, have, secs, wave_width, k_refine, pos, ncoarse);
   }
 
   // ---- results ----
-  unsigned long long nsurv = 0;
-  int status = 0;
-  CK(cudaMemcpyAsync(&nsurv, B->counters + 2, sizeof nsurv, cudaMemcpyDeviceToHost, s));
-  CK(cudaMemcpyAsync(&status, ctx->d_status, sizeof status, cudaMemcpyDeviceToHost, s));
-  std::vector<unsigned long long> cs(3 * (size_t)ncells);
-  CK(cudaMemcpyAsync(cs.data(), B->cell_stats, sizeof(unsigned long long) * 3 * ncells, cudaMemcpyDeviceToHost, s));
-  CK(cudaStreamSynchronize(s));
-  if (status) {
-    cudaMemsetAsync(ctx->d_status, 0, sizeof(int), s);
-    return status;
-  }
   if (stats)
     for (int ci = 0; ci < ncells; ci++) {
-      stats[ci].nodes = host_nodes[ci] + (long long)cs[ci];
-      stats[ci].leaves = (long long)cs[ncells + ci];
-      stats[ci].ok = (long long)cs[2 * ncells + ci];
+      stats[ci].nodes = host_nodes[ci] + (long long)cs_prev[ci];
+      stats[ci].leaves = (long long)cs_prev[ncells + ci];
+      stats[ci].ok = (long long)cs_prev[2 * ncells + ci];
     }
-  *nout = (long long)nsurv;
-  if ((long long)nsurv > surv_cap || (long long)nsurv > out_cap) return BS_ERR_CAP;
-  if (nsurv == 0) return BS_OK;
-  std::vector<uint64_t> keys(nsurv), words(2 * nsurv);
-  CK(cudaMemcpyAsync(keys.data(), B->surv_keys, sizeof(uint64_t) * nsurv, cudaMemcpyDeviceToHost, s));
-  CK(cudaMemcpyAsync(words.data(), B->surv_words, sizeof(uint64_t) * 2 * nsurv, cudaMemcpyDeviceToHost, s));
-  CK(cudaStreamSynchronize(s));
-  std::vector<uint32_t> order(nsurv);
-  for (uint32_t i = 0; i < (uint32_t)nsurv; i++) order[i] = i;
-  std::sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) { return keys[a] < keys[b]; });
-  for (unsigned long long i = 0; i < nsurv; i++) {
-    out_words[2 * i] = words[2 * order[i]];
-    out_words[2 * i + 1] = words[2 * order[i] + 1];
-    if (out_cell) out_cell[i] = prefixes[keys[order[i]] >> 32].cell;
+  *nout = have;
+  if (have > out_cap) return BS_ERR_CAP;
+  if (have > 0) {
+    memcpy(out_words, res_words.data(), sizeof(uint64_t) * 2 * have);
+    if (out_cell) memcpy(out_cell, res_cell.data(), sizeof(uint32_t) * have);
   }
   return BS_OK;
 }

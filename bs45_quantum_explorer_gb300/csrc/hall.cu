@@ -401,14 +401,23 @@ __global__ void __launch_bounds__(TC_THREADS, 1) hall_tc_kernel(TcParams P) {
       const uint32_t t0 = tmem + lane_off + (uint32_t)(b * 256);
       float mx = 0.0f;
       float *dump = P.dump ? P.dump + (size_t)(tile * 128 + row) * BS_TC_COLS : nullptr;
+      // A pair's rows sit in adjacent lanes (C even, D odd). Each lane forms its own row's
+      // PSD at every angle; for each angle one lane adds its partner's: the even lane the
+      // first half of a load round's angles, the odd lane the second half. One shuffle then
+      // carries two angles (each lane sends the half its partner sums), and the two running
+      // maxima combine at the end. Every sum is fC + fD of the same operands as before.
+      const bool odd = lane & 1;
+      float mx1 = 0.0f;
       {  // angles 0..63: Re columns 0..63 and Im columns 104..167 in one load round
         float v[128];
         tmem_ld_64_64(t0, t0 + BS_TC_IM0, v);
 #pragma unroll
-        for (int k = 0; k < 64; k++) {
-          float f = fmaf(v[k], v[k], v[64 + k] * v[64 + k]);
-          float g = __shfl_xor_sync(FULL_MASK, f, 1);
-          mx = fmaxf(mx, f + g);
+        for (int k = 0; k < 32; k++) {
+          const float fa = fmaf(v[k], v[k], v[64 + k] * v[64 + k]);
+          const float fb = fmaf(v[32 + k], v[32 + k], v[96 + k] * v[96 + k]);
+          const float got = __shfl_xor_sync(FULL_MASK, odd ? fa : fb, 1);
+          if (k & 1) mx1 = fmaxf(mx1, (odd ? fb : fa) + got);
+          else mx = fmaxf(mx, (odd ? fb : fa) + got);
         }
         if (dump)
           for (int k = 0; k < 64; k++) { dump[k] = v[k]; dump[BS_TC_IM0 + k] = v[64 + k]; }
@@ -417,14 +426,18 @@ __global__ void __launch_bounds__(TC_THREADS, 1) hall_tc_kernel(TcParams P) {
         float v[80];
         tmem_ld_32_8_32_8(t0 + 64, t0 + 96, t0 + BS_TC_IM0 + 64, t0 + BS_TC_IM0 + 96, v);
 #pragma unroll
-        for (int k = 0; k < 40; k++) {
-          float f = fmaf(v[k], v[k], v[40 + k] * v[40 + k]);
-          float g = __shfl_xor_sync(FULL_MASK, f, 1);
-          mx = fmaxf(mx, f + g);
+        for (int k = 0; k < 20; k++) {
+          const float fa = fmaf(v[k], v[k], v[40 + k] * v[40 + k]);
+          const float fb = fmaf(v[20 + k], v[20 + k], v[60 + k] * v[60 + k]);
+          const float got = __shfl_xor_sync(FULL_MASK, odd ? fa : fb, 1);
+          if (k & 1) mx1 = fmaxf(mx1, (odd ? fb : fa) + got);
+          else mx = fmaxf(mx, (odd ? fb : fa) + got);
         }
         if (dump)
           for (int k = 0; k < 40; k++) { dump[64 + k] = v[k]; dump[BS_TC_IM0 + 64 + k] = v[40 + k]; }
       }
+      mx = fmaxf(mx, mx1);
+      mx = fmaxf(mx, __shfl_xor_sync(FULL_MASK, mx, 1));
       tc_fence_before();
       __syncwarp();
       if (lane == 0) mbar_arrive(tempty0 + 8 * b);

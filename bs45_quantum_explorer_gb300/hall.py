@@ -58,6 +58,12 @@ class Context:
     def set_stream(self, stream_handle):
         check(lib().bs_ctx_set_stream(self.h, C.c_void_p(stream_handle)), "bs_ctx_set_stream")
 
+    def retarget(self, n, sig):
+        """Point the context at another (n, signature), keeping its stream and buffers."""
+        a, b, c, d = sig
+        check(lib().bs_ctx_retarget(self.h, n, a, b, c, d), "bs_ctx_retarget")
+        self.n, self.sig = n, tuple(sig)
+
     # ---- Hall filter ----
     def hall_filter(self, XY, mode="tc_fp16"):
         """XY: int8 [npairs, 2, n] (C, D). Returns (pass uint8 [npairs], stats dict)."""

@@ -3,7 +3,7 @@
 // 1343-1391 and 1544-2891), with the C,D stream, the Hall test, the per-cell flattest-k keep
 // and the A,B completion running on the GPU through libbsfh.so (include/bsfh.h).
 //
-// Same argv, same WZ_* environment, same stdout tokens the lane driver greps, same
+// Same argv, same WZ_* environment, same stdout tokens the reference's lane script greps, same
 // checkpoint file (CFGSIG line and resume fields) and the same exit codes:
 //   0 FOUND, 3 no hit / range exhausted / interrupted, 2 refusal, 1 usage, 5 internal error.
 // Not carried over (measurement-only instruments of the reference): FH_TELEM telemetry,
@@ -409,6 +409,11 @@ int main(int argc, char **argv) {
   so.endpos = endpos ? 1 : 0;
   so.cd_prune = 0;
   so.hall_mode = hall_mode;
+  // Front-only lanes use only a cell's first DRAIN_BATCHES x BUF_CAP survivors (the reference
+  // stops the cell's DFS there); the device stream stops there too. Score filtering and the
+  // unbuffered order see further into the stream, so they stream whole cells.
+  if (cell_order && drain_top > 0 && score_max == 0 && cellsize == 0)
+    so.limit = drain_batches * buf_cap;
   std::vector<uint64_t> surv;
   std::vector<int32_t> surv_score;
   std::vector<int8_t> empty_rows;
@@ -451,12 +456,13 @@ int main(int argc, char **argv) {
     cell.pinY = pinD;
     bs_cell_stats cst;
     long long nout = 0;
-    if (surv.size() < 2 * 65536) surv.resize(2 * 65536);
+    if (surv.size() < 2 * (size_t)(1 << 20)) surv.resize(2 * (size_t)(1 << 20));
     rc = bs_cd_stream(ctx, &cell, 1, &so, surv.data(), nullptr, (long long)surv.size() / 2, &nout, &cst);
-    if (rc == BS_ERR_CAP) {
-      surv.resize(2 * (size_t)nout);
+    for (int retry = 0; rc == BS_ERR_CAP && retry < 3; retry++) {
+      // the output or the device survivor buffer was short: grow to the reported size
+      surv.resize(std::max(surv.size(), 2 * (size_t)nout));
       so.survivor_cap = std::max(so.survivor_cap, nout);
-      rc = bs_cd_stream(ctx, &cell, 1, &so, surv.data(), nullptr, nout, &nout, &cst);
+      rc = bs_cd_stream(ctx, &cell, 1, &so, surv.data(), nullptr, (long long)surv.size() / 2, &nout, &cst);
     }
     if (rc) return fail_gpu(rc, "bs_cd_stream");
     // flat scores of every survivor (stream order), computed on the GPU

@@ -1,0 +1,180 @@
+"""One first-hit lane over a window of raw cells, as a library call.
+
+The reference runs this loop as a process (`WZ_FIRSTHIT=1 wz_match n a b c d`,
+src/solver/wz_match.cpp:2101-2891); bin/bs_firsthit is the drop-in for that process. run_lane()
+is the same search for callers that hold a GPU context and want a result object instead of a
+stdout protocol: a scheduler serving many jobs, or a benchmark. For each raw cell pi of the
+window that the arm owns (pi = shard + k*nshard, WZ_FH_PROF_SKIP <= k < WZ_FH_PROF_END) it
+  - skips orbit duplicates (orbit canon) and cells whose allowed A,B row list is empty,
+  - streams the cell on the GPU in the reference's DFS order (bs_cd_stream),
+  - buffers survivors in batches of buf_cap, orders each batch by flat score (bs_flat_topk),
+    completes the first drain_top of the first drain_batches batches (front-only cut;
+    drain_top = 0 completes every survivor) with budgeted A,B search (bs_complete_ab_batch),
+  - stops at the first hit.
+Counts follow the reference's summary line (candidates_streamed, clean_no_AB, budget_aborted,
+total_AB_nodes, cells_done, ...), so a run equals the lane's under the same settings.
+Not carried over: checkpoints, SIGTERM handling and the stdout protocol (bs_firsthit has them),
+WZ_FH_SCORE_MAX / WZ_FH_MAX_CAND and the unbuffered order (cell_order = 0).
+"""
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from .cells import ab_rows, cell_list
+from .complete import complete_ab, flat_topk
+from .hall import unpack
+from .stream import cd_stream
+
+
+@dataclass
+class LaneResult:
+    found: bool = False
+    hit_idx: int = -1              # candidates_streamed when the hit's batch was drained
+    profile_rank: int = -1         # raw cell index of the hit
+    quad: tuple = None             # (A, B, C, D) int8 arrays on a hit
+    nodes_this_cand: int = 0
+    candidates_streamed: int = 0
+    pre_filter_rejected: int = 0
+    clean_no_ab: int = 0
+    budget_aborted: int = 0
+    total_ab_nodes: int = 0
+    backtracks_entered: int = 0
+    cells_done: int = 0
+    cells_orbit_dup: int = 0
+    cells_prof_dead: int = 0
+    cells_prof_uncap: int = 0
+    cells_empty: int = 0
+    cells_capped: int = 0
+    dfs_nodes: int = 0
+    completions: int = 0
+    stream_s: float = 0.0
+    complete_s: float = 0.0
+    complete_device_ms: float = 0.0
+    timings: dict = field(default_factory=dict)
+
+
+_LIST_CACHE = {}
+
+
+def lane_list(n, sig, m6=None, thm211b=None, thm212=None, endpos=False, orbit_canon=True,
+              orbit_q=1, qprune=True, prof_order=3):
+    """The lane's cell list (bs_cell_list), cached per settings."""
+    key = (n, tuple(sig), m6, thm211b, thm212, endpos, orbit_canon, orbit_q, qprune, prof_order)
+    if key not in _LIST_CACHE:
+        _LIST_CACHE[key] = cell_list(n, sig, m6=m6, thm211b=thm211b, thm212=thm212, endpos=endpos,
+                                     orbit_canon=orbit_canon, orbit_q=orbit_q if orbit_canon else 0,
+                                     qprune=qprune, prof_order=prof_order)
+    return _LIST_CACHE[key]
+
+
+def run_lane(ctx, n, sig, skip=0, end=0, shard=0, nshard=1, budget=200000, buf_cap=500000,
+             drain_top=0, drain_batches=1, endpos=False, orbit_canon=True, orbit_q=1, qprune=True,
+             prof_order=3, m6=None, thm211b=None, thm212=None, abp_cap=20000, outer_k=3,
+             early=True, canon=True, rev=False, hall_mode="tc_fp16", chunk=65536,
+             max_seconds=0.0, listing=None):
+    """Runs the lane over raw cells [skip, end) of its shard (end = 0: to the list's end).
+    The list options are the lane's WZ_FH_* list settings (cells.cell_list); the cells must
+    be mod-6 cells (the lane's buffered order). max_seconds > 0 stops between cells once
+    exceeded (the result then says found=False and its counts cover the cells done).
+    listing: a cell_list() result to reuse."""
+    cells, kept, _, m = listing if listing is not None else lane_list(
+        n, sig, m6, thm211b, thm212, endpos, orbit_canon, orbit_q, qprune, prof_order)
+    if m != 6:
+        raise ValueError("run_lane runs the buffered (mod-6 cell) order only")
+    ncells = len(kept)
+    stop = min(ncells, shard + end * nshard) if end > 0 else ncells
+    owned = list(range(shard + skip * nshard, stop, nshard))
+    res = LaneResult()
+    t_start = time.perf_counter()
+    live = [pi for pi in owned if kept[pi]]
+    # allowed A,B rows of every owned kept cell (the reference's abpMap), one host call
+    rows, row_off, nrows = ab_rows(n, sig, m, [cells[pi] for pi in live]) if live else (None, [], [])
+    slot = {pi: j for j, pi in enumerate(live)}
+    cand = 0
+    for pi in owned:
+        if max_seconds > 0 and time.perf_counter() - t_start > max_seconds:
+            break
+        if not kept[pi]:
+            res.cells_orbit_dup += 1
+            continue
+        j = slot[pi]
+        nr = int(nrows[j])
+        if nr == 0:
+            res.cells_prof_dead += 1
+            res.cells_done += 1
+            continue
+        cell_rows = rows[row_off[j]:row_off[j] + nr] if nr <= abp_cap else None
+        if cell_rows is None:
+            res.cells_prof_uncap += 1
+        c = cells[pi]
+        t0 = time.perf_counter()
+        surv, _, st = cd_stream(ctx, [(list(c.tx[:m]), list(c.ty[:m]))], m=m,
+                                pins=[(c.pinX, c.pinY)], rev=rev, endpos=endpos,
+                                hall_mode=hall_mode, as_words=True,
+                                limit=drain_batches * buf_cap if drain_top > 0 else 0)
+        res.stream_s += time.perf_counter() - t0
+        res.dfs_nodes += st[0]["nodes"]
+        nout = len(surv)
+        cs_start = cand
+        nb = (nout + buf_cap - 1) // buf_cap
+        if drain_top > 0:
+            nb = min(nb, drain_batches)
+        found = False
+        for b in range(nb):
+            lo, hi = b * buf_cap, min(nout, (b + 1) * buf_cap)
+            cand = cs_start + hi          # survivors counted when this batch is drained
+            keep = min(hi - lo, drain_top) if drain_top > 0 else hi - lo
+            order, _ = flat_topk(ctx, surv[lo:hi], hi - lo, keep)
+            for c0 in range(0, len(order), chunk):
+                idx = lo + order[c0:c0 + chunk]
+                t1 = time.perf_counter()
+                ctx.timing(True)
+                v, nd, A, B = complete_ab(ctx, surv[idx], budget,
+                                          rows_per_cand=None if cell_rows is None else [cell_rows] * len(idx),
+                                          m=m, outer_k=outer_k, early=early, canon=canon,
+                                          first_hit=True)
+                ms, _, _ = ctx.timing_read()
+                ctx.timing(False)
+                res.complete_s += time.perf_counter() - t1
+                res.complete_device_ms += ms
+                for t in range(len(idx)):
+                    r = int(v[t])
+                    if r < 0:
+                        raise RuntimeError(f"candidate {t} of a batch was not completed ({r})")
+                    if r == 4:
+                        raise RuntimeError("completer found a quad whose NPAF recheck failed")
+                    res.completions += 1
+                    res.total_ab_nodes += int(nd[t])
+                    if r >= 2 or r == 0:  # the summary counts the hit as entered too
+                        res.backtracks_entered += 1
+                    if r == 1:
+                        res.pre_filter_rejected += 1
+                    elif r == 2:
+                        res.clean_no_ab += 1
+                    elif r == 3:
+                        res.budget_aborted += 1
+                    elif r == 0:
+                        cw = unpack(surv[idx[t]:idx[t] + 1], n)[0]
+                        res.found, res.hit_idx, res.profile_rank = True, cand, pi
+                        res.quad = (A[t].copy(), B[t].copy(), cw[0].copy(), cw[1].copy())
+                        res.nodes_this_cand = int(nd[t])
+                        found = True
+                        break
+                if found:
+                    break
+            if found:
+                break
+        if found:
+            res.candidates_streamed = cand
+            break
+        # the lane counts a cell as capped once it has drained its last allowed batch
+        if drain_top > 0 and nout > 0 and -(-nout // buf_cap) >= drain_batches:
+            res.cells_capped += 1
+        res.candidates_streamed = cand = cs_start + (min(nout, drain_batches * buf_cap)
+                                                     if drain_top > 0 else nout)
+        res.cells_done += 1
+        if nout == 0:
+            res.cells_empty += 1
+    res.timings["wall_s"] = time.perf_counter() - t_start
+    return res

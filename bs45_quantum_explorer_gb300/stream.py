@@ -26,30 +26,31 @@ def make_cells(cells, m, pins=None):
 
 def cd_stream(ctx, cells, m=6, pins=None, rev=False, endpos=False, hall_mode="tc_fp16",
               target_prefixes=0, leaf_chunk=0, survivor_cap=0, cap=None, as_words=False,
-              ab_side=False):
+              ab_side=False, limit=0):
     """cells: list of (tx, ty). Returns (survivors, cell index per survivor, per-cell stats).
 
     survivors: int8 [k, 2, L] (or uint64 words [k, 2] with as_words) in stream order, L = n
     (C,D) or n+1 with ab_side (the reference's abSide stream of A,B pairs).
     stats: list of dicts {nodes, leaves, ok} per cell (the reference's CDSTAT dfs_nodes and
-    CELLSIZE leaves / hall_ok)."""
+    CELLSIZE leaves / hall_ok; with limit > 0, of the part explored).
+    limit > 0 returns only the first `limit` survivors and stops the search there."""
     ncells = len(cells)
     arr = make_cells(cells, m, pins)
     opt = StreamOpts(m=m, rev=int(rev), endpos=int(endpos), cd_prune=0,
                      hall_mode=MODES[hall_mode], ab_side=int(ab_side),
                      target_prefixes=target_prefixes, leaf_chunk=leaf_chunk,
-                     survivor_cap=survivor_cap)
+                     survivor_cap=survivor_cap, limit=limit)
     stats = (CellStats * ncells)()
     nout = C.c_longlong(0)
-    cap = cap if cap is not None else (1 << 20)
-    for _ in range(2):
+    cap = cap if cap is not None else (min(1 << 20, limit) if limit > 0 else 1 << 20)
+    for _ in range(4):
         words = np.zeros((max(1, cap), 2), np.uint64)
         cidx = np.zeros(max(1, cap), np.uint32)
         rc = lib().bs_cd_stream(ctx.h, arr, ncells, C.byref(opt), words.ctypes.data,
                                 cidx.ctypes.data, cap, C.byref(nout), stats)
-        if rc == -6 and nout.value > cap:  # BS_ERR_CAP: retry with the size it reported
-            cap = nout.value
-            opt.survivor_cap = max(opt.survivor_cap, cap)
+        if rc == -6:  # BS_ERR_CAP: retry with the sizes it reported
+            cap = max(cap, nout.value)
+            opt.survivor_cap = max(opt.survivor_cap, nout.value)
             continue
         check(rc, "bs_cd_stream")
         break

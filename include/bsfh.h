@@ -57,6 +57,11 @@ const char *bs_strerror(int code);
  * (src/solver/wz_match.cpp:106-114) and uploads them. 4 <= n <= 63. */
 int bs_ctx_create(int n, int a, int b, int c, int d, int device, bs_ctx **out);
 void bs_ctx_destroy(bs_ctx *ctx);
+/* Point an existing context at another BS(n+1,n) and signature, keeping its stream and every
+ * device buffer (a serving slot reuses one context across jobs instead of allocating, and so
+ * synchronising the device, per job). Waits for the context's queued work first. No
+ * counterpart in the reference (one process per lane there). */
+int bs_ctx_retarget(bs_ctx *ctx, int n, int a, int b, int c, int d);
 /* Use a caller-owned CUDA stream (cudaStream_t) for every later call; NULL = the context's own. */
 int bs_ctx_set_stream(bs_ctx *ctx, void *cuda_stream);
 /* Last error recorded by the device (timeouts), cleared on read. */
@@ -110,7 +115,9 @@ int bs_hall_tc_dump_dev(bs_ctx *ctx, const uint64_t *d_bits, long long npairs, i
  * Thm 2.2 mirror-quad (C,D) whose class sums equal the cell's targets and that passes the
  * Thm 2.4 test, in the reference's emission order (cells in the given order, then DFS
  * order), with per-cell counts equal to the reference's CDSTAT dfs_nodes, leaves and
- * hall_ok (CELLSIZE) figures. */
+ * hall_ok (CELLSIZE) figures. The subtrees are explored in waves, in stream order: each
+ * wave refines the next run of the cell's frontier to as many subtrees as keep the GPU
+ * busy, so cells of 10^13 nodes (n = 42) stream at full speed and `limit` stops early. */
 typedef struct {
   int8_t tx[8], ty[8];  /* class-sum targets of C and D at modulus m (entries >= m unused) */
   int32_t pinX, pinY;   /* zero-sum pins: C[0] = +1 / D[0] = +1 (wz_match.cpp:1526-1527) */
@@ -126,6 +133,11 @@ typedef struct {
   long long target_prefixes; /* subtrees to split the batch into (0 = 262144) */
   long long leaf_chunk;      /* leaves buffered per round (0 = 2^24) */
   long long survivor_cap;    /* device survivor buffer (0 = 2^22) */
+  long long limit;           /* > 0: stop once the first `limit` survivors of the batch (in
+                                stream order) are known and return only those -- the lane's
+                                front-only cut (BUF_CAP x DRAIN_BATCHES survivors per cell,
+                                wz_match.cpp:2656-2714, 2782-2790), which stops the
+                                reference's DFS; the stats then cover the part explored */
 } bs_stream_opts;
 
 typedef struct { long long nodes, leaves, ok; } bs_cell_stats;
@@ -166,7 +178,9 @@ int bs_ab_rows(int n, int a, int b, int m, const bs_cell *cells, long long ncell
                long long rows_cap, long long *row_off, int32_t *nrows, long long *nrows_total);
 
 /* out_words: 2 words (C, D) per survivor, out_cell (may be NULL): the survivor's cell index.
- * *nout always receives the survivor count; BS_ERR_CAP when it exceeds out_cap. */
+ * *nout always receives the survivor count; BS_ERR_CAP when it exceeds out_cap, or when one
+ * wave's survivors exceed survivor_cap (then *nout is a lower bound: retry with both at
+ * least *nout). */
 int bs_cd_stream(bs_ctx *ctx, const bs_cell *cells, int ncells, const bs_stream_opts *opt,
                  uint64_t *out_words, uint32_t *out_cell, long long out_cap, long long *nout,
                  bs_cell_stats *stats);

@@ -74,3 +74,70 @@ def test_lane_checkpoint_resume_matches_reference(gpu):
             assert (rc1, semantic(out1), ckpt1) == (c["rc"], c["semantic"], c["ckpt"]), ctx
             assert (rc2, semantic(out2), ckpt2) == (c["rc2"], c["semantic2"], c["ckpt2"]), ctx
             assert (dh, dl) == (c["dump_sha256"], c["dump_len"]), ctx
+
+
+# ---- the library form of the lane (lane.run_lane) against the same reference runs ----
+
+_SUMMARY_KEYS = {"candidates_streamed": "candidates_streamed", "backtracks_entered": "backtracks_entered",
+                 "clean_no_AB": "clean_no_ab", "budget_aborted": "budget_aborted",
+                 "total_AB_nodes": "total_ab_nodes", "cells_done": "cells_done",
+                 "cells_prof_dead": "cells_prof_dead", "cells_prof_uncap": "cells_prof_uncap",
+                 "cells_orbit_dup": "cells_orbit_dup", "cells_empty": "cells_empty",
+                 "cells_capped": "cells_capped", "pre_filter_rejected": "pre_filter_rejected"}
+
+
+def summary_of(semantic_lines):
+    """The reference summary's counts, the FIRSTHIT fields and the quad, from semantic lines."""
+    import re
+    out = {}
+    for line in semantic_lines:
+        for k, v in re.findall(r"(\w+)=(-?\d+)", line):
+            if k in _SUMMARY_KEYS:
+                out[_SUMMARY_KEYS[k]] = int(v)
+        m = re.match(r"FIRSTHIT: idx=(\d+) profile_rank=(\d+) nodes_this_cand=(\d+)", line)
+        if m:
+            out["hit"] = tuple(int(x) for x in m.groups())
+        m = re.match(r"([ABCD]) = \{(.*)\};", line)
+        if m:
+            out[m.group(1)] = [int(x) for x in m.group(2).split(",")]
+    return out
+
+
+def lane_kwargs(st):
+    """run_lane arguments for a lane's WZ_* settings (buffered mod-6 order only)."""
+    return dict(budget=int(st.get("WZ_FH_AB_BUDGET", 200000)), buf_cap=int(st.get("WZ_FH_BUF_CAP", 500000)),
+                drain_top=int(st.get("WZ_FH_DRAIN_TOP", 0)), drain_batches=int(st.get("WZ_FH_DRAIN_BATCHES", 1)),
+                skip=int(st.get("WZ_FH_PROF_SKIP", 0)), end=int(st.get("WZ_FH_PROF_END", 0)),
+                rev=bool(int(st.get("WZ_FH_STREAM_REV", 0))), endpos=bool(int(st.get("WZ_FH_ENDPOS", 0))),
+                orbit_canon=bool(int(st.get("WZ_FH_ORBIT_CANON", 0))), orbit_q=int(st.get("WZ_FH_ORBIT_Q", 0)),
+                qprune=bool(int(st.get("WZ_FH_ORBIT_QPRUNE", 0))), prof_order=int(st.get("WZ_FH_PROF_ORDER", 0)),
+                outer_k=int(st.get("WZ_FH_OUTER_K", 3)), early=int(st.get("WZ_FH_EARLY_CHECK", 1)) != 0,
+                canon="WZ_FH_NO_CANON" not in st, m6=True, thm211b=True, thm212=True)
+
+
+def check_run_lane(res, want, ctx):
+    got = {v: getattr(res, v) for v in _SUMMARY_KEYS.values() if v in want}
+    assert got == {k: want[k] for k in got}, ctx
+    if "hit" in want:
+        assert res.found and (res.hit_idx, res.profile_rank, res.nodes_this_cand) == want["hit"], ctx
+        A, B, C, D = res.quad
+        assert [list(map(int, x)) for x in (A, B, C, D)] == [want[k] for k in "ABCD"], ctx
+    else:
+        assert not res.found, ctx
+
+
+def test_run_lane_matches_reference_runs(gpu):
+    from bs45_quantum_explorer_gb300.hall import Context
+    from bs45_quantum_explorer_gb300.lane import run_lane
+    cases = [c for c in _cases() if not c.get("resume") and c["settings"].get("WZ_FH_M6") == 1
+             and not any(k in c["settings"] for k in ("WZ_FH_CELLSIZE", "WZ_FH_SCORE_MAX"))]
+    assert len(cases) >= 100
+    ctxs = {}
+    for c in cases:
+        key = (c["n"], tuple(c["sig"]))
+        if key not in ctxs:
+            ctxs[key] = Context(c["n"], tuple(c["sig"]))
+        res = run_lane(ctxs[key], c["n"], tuple(c["sig"]), **lane_kwargs(c["settings"]))
+        check_run_lane(res, summary_of(c["semantic"]), (c["n"], c["sig"], c["settings"]))
+    for x in ctxs.values():
+        x.close()

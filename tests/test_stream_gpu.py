@@ -129,3 +129,40 @@ def test_stream_golden_reference(gpu):
             assert st[0]["nodes"] == nodes
         else:
             assert st[0]["nodes"] >= nodes
+
+
+def test_stream_limit_returns_the_stream_prefix(gpu, oracle):
+    """limit = L returns exactly the first L survivors of the batch, in order (the lane's
+    front-only cut), for limits inside one cell, across cells and past the end."""
+    from bs45_quantum_explorer_gb300.hall import Context
+    from bs45_quantum_explorer_gb300.stream import cd_stream
+    n = 22
+    sig = _classes(n)[0]
+    ctx = Context(n, sig)
+    rng = np.random.default_rng(7)
+    cells = [(x, y) for x in _cells(n, sig[2], 6) for y in _cells(n, sig[3], 6)]
+    cells = [cells[i] for i in rng.permutation(len(cells))[:40]]
+    pins = [(0, 0)] * len(cells)
+    ref, ridx, _ = _oracle_batch(oracle, n, cells, 6, pins, 0, 0)
+    total = len(ref)
+    assert total > 200
+    for L in (1, 5, 100, total // 2, total - 1, total, total + 3):
+        got, gidx, _ = cd_stream(ctx, cells, m=6, pins=pins, limit=L)
+        k = min(L, total)
+        assert got.shape[0] == k, (L, got.shape)
+        assert (got == ref[:k]).all() and (gidx == ridx[:k]).all(), L
+    ctx.close()
+
+
+def test_stream_limit_on_a_large_cell(gpu):
+    """n = 30, the 176,414-survivor cell: the limited stream is the full stream's prefix."""
+    from bs45_quantum_explorer_gb300.hall import Context
+    from bs45_quantum_explorer_gb300.stream import cd_stream
+    ctx = Context(30, (1, 7, 6, 6))
+    cell = ([-1, 1, 1, 1, 1, 3], [-1, 1, 1, 1, 5, -1])
+    full, _, st = cd_stream(ctx, [cell], m=6, as_words=True)
+    assert len(full) == 176414 and st[0]["nodes"] == 599381729
+    for L in (1000, 50000, 176414):
+        got, _, _ = cd_stream(ctx, [cell], m=6, as_words=True, limit=L)
+        assert np.array_equal(got, full[:L]), L
+    ctx.close()
