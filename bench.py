@@ -227,7 +227,7 @@ def _classes(n):
     return out
 
 
-def run_first_hit(seconds, cpu_seconds=10.0, with_cpu=True):
+def run_first_hit(seconds, cpu_seconds=10.0, with_cpu=True, drain_top=50000):
     """One production lane (orbit canon + quad switch + Q-prune, ORDER=3; budget 2^22,
     BUF_CAP 500,000, DRAIN_TOP 50,000) over raw cells [s, s+4096) of n = 36, sig (5,11,0,0),
     s drawn from the seed; stopped between cells after `seconds`. Reports the completer's
@@ -247,13 +247,13 @@ def run_first_hit(seconds, cpu_seconds=10.0, with_cpu=True):
     rng = np.random.default_rng(SEED)
     s = int(rng.integers(0, len(kept) - 4096))
     ctx = Context(FH_N, FH_SIG)
-    kw = dict(budget=1 << 22, buf_cap=500000, drain_top=50000, listing=listing)
+    kw = dict(budget=1 << 22, buf_cap=500000, drain_top=drain_top, listing=listing)
     run_lane(ctx, FH_N, FH_SIG, skip=s, end=s + 1, **kw)  # warm-up: buffers, first cell
     torch.cuda.synchronize()
     res = run_lane(ctx, FH_N, FH_SIG, skip=s, end=s + 4096, max_seconds=seconds, **kw)
     out = {"workload": f"first-hit lane, n={FH_N} sig={FH_SIG}, raw cells [{s}, {s + 4096}) of the "
                        f"ORDER=3 list (digest {digest}, {int(kept[s:s + 4096].sum())} kept cells), "
-                       "budget 2^22, BUF_CAP 500000, DRAIN_TOP 50000",
+                       f"budget 2^22, BUF_CAP 500000, DRAIN_TOP {drain_top}",
            "bounded_seconds": seconds, "list_build_s": round(list_s, 2),
            "cells_done": res.cells_done, "cells_orbit_dup": res.cells_orbit_dup,
            "cells_prof_dead": res.cells_prof_dead, "completions": res.completions,
@@ -278,7 +278,7 @@ def run_first_hit(seconds, cpu_seconds=10.0, with_cpu=True):
         c = cells[pi]
         rows, off, nr = ab_rows(FH_N, FH_SIG, m, [c])
         surv, _, _ = cd_stream(ctx, [(list(c.tx[:m]), list(c.ty[:m]))], m=m, as_words=True, limit=500000)
-        order, _ = flat_topk(ctx, surv, len(surv), 50000)
+        order, _ = flat_topk(ctx, surv, len(surv), drain_top)
         cand = unpack(surv[order], FH_N)
         r = rows[off[0]:off[0] + nr[0]] if 0 < nr[0] <= 20000 else None
         nodes, done, t1 = 0, 0, time.perf_counter()
@@ -294,6 +294,55 @@ def run_first_hit(seconds, cpu_seconds=10.0, with_cpu=True):
                                          "runs one lane per core"}
     ctx.close()
     return out
+
+
+def run_c3(max_cells=0, batch=16, topk=256):
+    """C3: the full C,D stream at n = 30, sig (1,7,6,6): every kept cell of the ORDER=3 list
+    (2.11b + 2.12, orbit canon with the quad switch: 97,141 cells, 7,987 kept) streamed whole,
+    with its flattest-256 keep. Reports DFS nodes/s and the stream's algorithmic HBM rate:
+    32 B per DFS node (a 16 B frontier record written and read once) + 16 B per leaf handed to
+    the filter + 24 B per survivor (packed C,D, DFS rank, score)."""
+    import numpy as np
+    import torch
+    from bs45_quantum_explorer_gb300.cells import cell_list
+    from bs45_quantum_explorer_gb300.complete import flat_topk
+    from bs45_quantum_explorer_gb300.hall import Context
+    from bs45_quantum_explorer_gb300.stream import cd_stream
+    n, sig = 30, (1, 7, 6, 6)
+    cells, kept, digest, m = cell_list(n, sig, m6=True, thm211b=True, thm212=True, orbit_canon=True,
+                                       orbit_q=1, qprune=False, prof_order=3)
+    live = [i for i in range(len(kept)) if kept[i]]
+    if max_cells:
+        live = live[:max_cells]
+    ctx = Context(n, sig)
+    cd_stream(ctx, [(list(cells[live[0]].tx[:m]), list(cells[live[0]].ty[:m]))], m=m, as_words=True)
+    torch.cuda.synchronize()
+    nodes = leaves = surv_total = kept_total = 0
+    t0 = time.perf_counter()
+    for b in range(0, len(live), batch):
+        group = live[b:b + batch]
+        batch_cells = [(list(cells[i].tx[:m]), list(cells[i].ty[:m])) for i in group]
+        surv, cidx, st = cd_stream(ctx, batch_cells, m=m, as_words=True, cap=1 << 23,
+                                   survivor_cap=1 << 23)
+        nodes += sum(x["nodes"] for x in st)
+        leaves += sum(x["leaves"] for x in st)
+        surv_total += len(surv)
+        # each cell's flattest 256 (one batch covering the whole cell)
+        bounds = np.searchsorted(cidx, np.arange(len(group) + 1))
+        for j in range(len(group)):
+            lo, hi = int(bounds[j]), int(bounds[j + 1])
+            if hi > lo:
+                order, _ = flat_topk(ctx, surv[lo:hi], hi - lo, topk)
+                kept_total += len(order)
+    dt = time.perf_counter() - t0
+    ctx.close()
+    alg = 32 * nodes + 16 * leaves + 24 * surv_total
+    return {"workload": f"C,D stream n={n} sig={sig}: {len(live)} kept cells of the ORDER=3 list "
+                        f"({len(kept)} cells, digest {digest}) streamed whole, flattest-{topk} per cell",
+            "cells": len(live), "dfs_nodes": nodes, "leaves": leaves, "survivors": surv_total,
+            "kept_topk": kept_total, "seconds": dt, "dfs_nodes_per_s": nodes / dt,
+            "filtered_cands_per_s": leaves / dt, "cells_per_s": len(live) / dt,
+            "algorithmic_bytes": alg, "algorithmic_gb_per_s": alg / dt / 1e9}
 
 
 def run_serving(n_jobs=12, tail=2, rate=2.0, slots=4, max_cells=64):
@@ -342,6 +391,10 @@ def main():
     ap.add_argument("--first-hit", type=float, default=None, metavar="SECONDS",
                     help="run only the n=36 first-hit lane for about SECONDS and print its line")
     ap.add_argument("--serve", action="store_true", help="run only the serving mix and print its line")
+    ap.add_argument("--c3", type=int, default=None, metavar="CELLS",
+                    help="run only the n=30 full stream over the first CELLS kept cells (0: all)")
+    ap.add_argument("--fh-drain", type=int, default=50000,
+                    help="DRAIN_TOP of the first-hit lane (a smaller value makes a small profiling case)")
     ap.add_argument("--fh-seconds", type=float, default=30.0,
                     help="bound on the first-hit lane inside the default run")
     args = ap.parse_args()
@@ -356,13 +409,16 @@ def main():
     if args.stream_only:
         run_stream_only(args)
         return
-    if args.first_hit is not None or args.serve:
+    if args.first_hit is not None or args.serve or args.c3 is not None:
         from bs45_quantum_explorer_gb300 import build_library
         build_library()
         if args.first_hit is not None:
-            print(json.dumps(run_first_hit(args.first_hit)), flush=True)
+            print(json.dumps(run_first_hit(args.first_hit, with_cpu=not args.no_cpu_baseline,
+                                           drain_top=args.fh_drain)), flush=True)
         if args.serve:
             print(json.dumps(run_serving()), flush=True)
+        if args.c3 is not None:
+            print(json.dumps(run_c3(args.c3)), flush=True)
         return
 
     import numpy as np
@@ -545,9 +601,14 @@ def main():
         dfs_ms, dfs_launches, _ = ctx.timing_read()
         ctx.timing(False)
         nodes = sst[0]["nodes"]
-        # the same search with the FP64-only Hall form on the leaves
+        # the tensor-core and FP64-only Hall forms on the same shorter search (the FP64 form
+        # filters ~2e7 leaves/s, so the full 50,000-survivor search would take minutes)
+        CMP_LIMIT = 500
         t1 = time.perf_counter()
-        surv64, _, sst64 = cd_stream(ctx, [cell42], m=6, as_words=True, limit=SEARCH_LIMIT,
+        surv_c, _, sst_c = cd_stream(ctx, [cell42], m=6, as_words=True, limit=CMP_LIMIT)
+        dt_c = time.perf_counter() - t1
+        t1 = time.perf_counter()
+        surv64, _, sst64 = cd_stream(ctx, [cell42], m=6, as_words=True, limit=CMP_LIMIT,
                                      hall_mode="fp64")
         dt64 = time.perf_counter() - t1
         line["search"] = {
@@ -559,10 +620,14 @@ def main():
             "device_kernel_ms": dfs_ms, "timed_launches": dfs_launches,
             "device_nodes_per_s": nodes / (dfs_ms * 1e-3) if dfs_ms > 0 else None,
             "filtered_cands_per_s": sst[0]["leaves"] / dt,
-            "fp64_hall_form": {"seconds": dt64, "nodes_per_s": sst64[0]["nodes"] / dt64,
-                               "filtered_cands_per_s": sst64[0]["leaves"] / dt64,
-                               "tc_speedup": dt64 / dt,
-                               "survivors_identical": bool(np.array_equal(surv64, surv))},
+            "hall_forms_on_first_500": {
+                "tc_fp16": {"seconds": dt_c, "nodes_per_s": sst_c[0]["nodes"] / dt_c,
+                            "filtered_cands_per_s": sst_c[0]["leaves"] / dt_c},
+                "fp64": {"seconds": dt64, "nodes_per_s": sst64[0]["nodes"] / dt64,
+                         "filtered_cands_per_s": sst64[0]["leaves"] / dt64},
+                "tc_speedup": dt64 / dt_c,
+                "survivors_identical": bool(np.array_equal(surv64, surv_c)),
+                "same_as_50000_prefix": bool(np.array_equal(surv_c, surv[:CMP_LIMIT]))},
             "reference_single_core": "14,736,335,258 nodes, 448,271,835 leaves, 5,613 survivors "
                                      "in 348.9 s (42.2 M nodes/s, one Xeon core; run interrupted)"}
         # ---- the n = 36 first-hit lane (bounded) and the serving mix ----

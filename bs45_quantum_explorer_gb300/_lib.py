@@ -41,7 +41,8 @@ class StreamOpts(C.Structure):
     _fields_ = [("m", C.c_int32), ("rev", C.c_int32), ("endpos", C.c_int32),
                 ("cd_prune", C.c_int32), ("hall_mode", C.c_int32), ("ab_side", C.c_int32),
                 ("target_prefixes", C.c_longlong), ("leaf_chunk", C.c_longlong),
-                ("survivor_cap", C.c_longlong), ("limit", C.c_longlong)]
+                ("survivor_cap", C.c_longlong), ("limit", C.c_longlong),
+                ("round_us", C.c_longlong)]
 
 
 class CellStats(C.Structure):

@@ -27,29 +27,38 @@ def flat_topk(ctx, words, buf_cap, keep):
     return order[:nk.value], scores[:nk.value]
 
 
+AB_CAND = np.dtype([("c", np.uint64), ("d", np.uint64), ("row_off", np.int64),
+                    ("nrows", np.int32), ("reserved", np.int32)])
+assert AB_CAND.itemsize == C.sizeof(AbCand)
+
+
 def complete_ab(ctx, cands, budget, rows_per_cand=None, m=6, outer_k=3, early=True, canon=True,
-                first_hit=False, max_seconds=0.0):
-    """cands: int8 [k, 2, n] (C, D) or uint64 words [k, 2]. rows_per_cand: None or a list of
-    int8 [r, 16] arrays (the cell's allowed rows; empty = unconstrained).
+                first_hit=False, max_seconds=0.0, rows=None):
+    """cands: int8 [k, 2, n] (C, D) or uint64 words [k, 2]. Allowed A,B rows (int8 [r, 16]):
+    `rows` shared by every candidate (one cell's list), or rows_per_cand, a list of arrays
+    (empty = unconstrained); neither: unconstrained.
     Returns (verdict int32 [k], nodes int64 [k], A int8 [k, n+1], B int8 [k, n+1])."""
     cands = np.asarray(cands)
     words = cands if cands.dtype == np.uint64 else pack(cands)
     words = np.ascontiguousarray(words.reshape(-1, 2), np.uint64)
     k = words.shape[0]
-    arr = (AbCand * max(1, k))()
-    all_rows = []
-    off = 0
-    for i in range(k):
-        arr[i].c, arr[i].d = int(words[i, 0]), int(words[i, 1])
-        r = None if rows_per_cand is None else rows_per_cand[i]
-        if r is not None and len(r):
-            r = np.ascontiguousarray(r, np.int8).reshape(-1, 16)
-            arr[i].row_off, arr[i].nrows = off, r.shape[0]
-            all_rows.append(r)
-            off += r.shape[0]
-        else:
-            arr[i].row_off, arr[i].nrows = 0, 0
-    rows = np.ascontiguousarray(np.concatenate(all_rows) if all_rows else np.zeros((1, 16), np.int8))
+    arr = np.zeros(max(1, k), AB_CAND)
+    arr["c"][:k], arr["d"][:k] = words[:, 0], words[:, 1]
+    if rows is not None and len(rows):
+        all_rows = np.ascontiguousarray(rows, np.int8).reshape(-1, 16)
+        arr["nrows"][:k] = all_rows.shape[0]
+        off = all_rows.shape[0]
+    else:
+        parts, off = [], 0
+        for i in range(k):
+            r = None if rows_per_cand is None else rows_per_cand[i]
+            if r is not None and len(r):
+                r = np.ascontiguousarray(r, np.int8).reshape(-1, 16)
+                arr["row_off"][i], arr["nrows"][i] = off, r.shape[0]
+                parts.append(r)
+                off += r.shape[0]
+        all_rows = np.concatenate(parts) if parts else np.zeros((1, 16), np.int8)
+    all_rows = np.ascontiguousarray(all_rows)
     opt = AbOpts(budget=budget, outer_k=outer_k, early=int(early), canon=int(canon), m=m,
                  first_hit=int(first_hit), reserved=0, max_seconds=max_seconds)
     n1 = ctx.n + 1
@@ -57,7 +66,8 @@ def complete_ab(ctx, cands, budget, rows_per_cand=None, m=6, outer_k=3, early=Tr
     nodes = np.zeros(max(1, k), np.int64)
     A = np.zeros((max(1, k), n1), np.int8)
     B = np.zeros((max(1, k), n1), np.int8)
-    check(lib().bs_complete_ab_batch(ctx.h, arr, k, rows.ctypes.data, off, C.byref(opt),
-                                     verdict.ctypes.data, nodes.ctypes.data, A.ctypes.data,
-                                     B.ctypes.data), "bs_complete_ab_batch")
+    check(lib().bs_complete_ab_batch(ctx.h, C.cast(arr.ctypes.data, C.POINTER(AbCand)), k,
+                                     all_rows.ctypes.data, off, C.byref(opt), verdict.ctypes.data,
+                                     nodes.ctypes.data, A.ctypes.data, B.ctypes.data),
+          "bs_complete_ab_batch")
     return verdict[:k], nodes[:k], A[:k], B[:k]

@@ -3,15 +3,16 @@
 //
 // Structure:
 //   1. Host: each cell's DFS tree is expanded to a split depth D in the reference's branch
-//      order (quad index order, reversed under STREAM_REV), giving prefixes in DFS order.
-//      Nodes above D are counted here exactly as the reference counts rec() calls.
-//   2. Device, cd_dfs_kernel: persistent threads take prefixes from a queue and walk the
-//      subtree below each one iteratively, one tree step per loop iteration (so a warp's lanes
-//      stay busy on different subtrees). A class-exact leaf is appended to the leaf buffer with
-//      key (prefix index << 32 | leaf sequence inside the prefix). When the buffer is full a
-//      thread saves its position and stops; the next launch resumes it.
+//      order (quad index order, reversed under STREAM_REV), giving coarse prefixes in DFS
+//      order. Nodes above D are counted here exactly as the reference counts rec() calls.
+//   2. Waves: runs of coarse prefixes, in order, refined on the host to enough subtree roots
+//      to fill the GPU. Device, cd_dfs_kernel: groups of eight lanes take roots from a queue
+//      and walk each subtree iteratively; the eight lanes test a node's eight children in
+//      one step. A class-exact leaf is appended with its branch path as key. A launch stops
+//      when the leaf buffer is full or its time is up; suspended walks resume in the next
+//      launch, and when few remain the host splits them into their remaining subtrees.
 //   3. Device: the Hall filter (tensor-core form by default) decides every leaf; survivors are
-//      compacted with their keys; sorting by key restores the reference's stream order.
+//      compacted with their keys; sorting by (cell, path) restores the reference's order.
 #include <stdint.h>
 #include <stdlib.h>
 #include <string.h>
@@ -32,20 +33,21 @@ struct CellDev {
   int8_t tx[8], ty[8];
 };
 
+// A subtree root handed to the device: the node reached by the branch indices of depths
+// 0..depth-1 (4 bits per depth; depths 0-15 in dig0, 16-31 in dig1).
 struct Prefix {
   uint32_t cell;
-  uint32_t depth;   // D: quads placed at depths 0..D-1
-  uint64_t digits;  // 4 bits per depth: the loop index kk chosen at that depth
+  uint32_t depth;
+  uint64_t dig0, dig1;
 };
 
-// A suspended subtree walk: the node at depth d with its next child index kk.
+// A suspended walk: the subtree of root depth D, now at the node of depth d with next child
+// kk, and the leaf children of that node (bit k = child k) not yet written.
 struct Saved {
-  uint32_t prefix;
-  uint32_t seq;        // leaves emitted so far inside this prefix
-  uint16_t d, kk;
-  uint16_t owed;       // leaf children of node d (bit k = child k) not yet written
-  uint16_t pad;
-  uint64_t dig[2];     // digits of depths 0..d-1 (4 bits each, depths 0-15 and 16-31)
+  uint32_t cell;
+  uint16_t D, d, kk, owed;
+  uint32_t pad;
+  uint64_t dig0, dig1;  // branch indices of depths 0..d-1
 };
 
 struct CdParams {
@@ -62,12 +64,14 @@ struct CdParams {
   Saved *saved_out;
   unsigned *nsaved_out;
   int saved_cap;
-  uint64_t *leaf_words;  // [cap][2]
-  uint64_t *leaf_keys;   // [cap]
+  uint64_t *leaf_words;  // [cap][2]: C, D
+  uint64_t *leaf_keys;   // [cap][2]: the leaf's path key (see path_key)
+  uint32_t *leaf_cell;   // [cap]
   unsigned long long *leaf_count;
   unsigned long long leaf_cap;
   unsigned long long *cell_nodes, *cell_leaves;
-  int *full_flag;
+  int *stop_flag;         // set when the leaf buffer is full or the round's time is up
+  unsigned long long round_ns;  // > 0: suspend every walk after about this long
   int *status;
 };
 
@@ -119,9 +123,6 @@ __device__ __forceinline__ void unplace(Walk &w, const QuadFx &f, uint64_t posma
   w.X &= ~posmask;
   w.Y &= ~posmask;
 }
-__device__ __forceinline__ bool feasible(const Walk &w, uint64_t M) {
-  return ((w.s0 & w.s1 & w.s2 & w.s3) & M) == M;
-}
 
 __device__ __forceinline__ void init_walk(Walk &w, const CellDev &cell, int L, int m) {
   w.s0 = w.s1 = w.s2 = w.s3 = 0x4040404040404040ULL;
@@ -144,9 +145,32 @@ __device__ __forceinline__ void middle_bits(const Walk &w, int half, int cm, uin
   if (dy > 0) ly |= 1ULL << half;
 }
 
+// The order key of a leaf: its branch index at every depth, depth 0 most significant (the
+// reference's DFS visits leaves in exactly this lexicographic order). The digit words hold
+// depth t at bits 4t..4t+3, so the key is each word with its 16 nibbles reversed.
+__device__ __forceinline__ uint64_t nibble_reverse(uint64_t x) {
+  x = ((x & 0x0F0F0F0F0F0F0F0FULL) << 4) | ((x >> 4) & 0x0F0F0F0F0F0F0F0FULL);
+  const uint32_t lo = (uint32_t)x, hi = (uint32_t)(x >> 32);
+  return ((uint64_t)__byte_perm(lo, 0, 0x0123) << 32) | (uint64_t)__byte_perm(hi, 0, 0x0123);
+}
+
+__device__ __forceinline__ unsigned long long globaltimer() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
 // MINB: the blocks of 256 threads the register budget is set for (4: 64 registers, no spill;
 // 6: 40 registers with a few spills on the rare paths). The launch sizes the grid to the
 // blocks that are resident at once, so saved walks never wait for a block to be scheduled.
+//
+// Eight lanes walk one subtree together: lane j of a group tests child j of the group's
+// current node, so a node's eight children take one step instead of eight, and the lanes of
+// a group never diverge. A step then descends into the first feasible untried child (the
+// children before it count as nodes, as the reference counts them when it tries them), or,
+// when none is left, returns to the parent; at the leaf level all feasible children are
+// written at once. A warp holds four walks; warp-wide collectives run every step in every
+// lane, walks that have ended idle until the whole warp has.
 template <int MINB>
 __global__ void __launch_bounds__(256, MINB) cd_dfs_kernel(CdParams P) {
   __shared__ QuadFx fx[32][16];
@@ -156,176 +180,196 @@ __global__ void __launch_bounds__(256, MINB) cd_dfs_kernel(CdParams P) {
   if (threadIdx.x < 32) posm[threadIdx.x] = P.posmask[threadIdx.x];
   __syncthreads();
   const int lane = threadIdx.x & 31;
+  const int j = lane & 7;               // the child this lane tests
+  const int g = lane >> 3;              // the walk of this lane within the warp
+  const unsigned gmask = 0xFFu << (8 * g);
+  const int leader = 8 * g;             // lane 0 of the group
   const int L = P.L, m = P.m, half = P.half;
   const uint64_t M = P.feas_mask;
   const int cm = half % m;
-  bool have = false;
-  uint32_t prefix = 0, cell = 0, seq = 0;
+  const unsigned long long t_start = globaltimer();
+  bool have = false, done = false;
+  uint32_t cell = 0;
   int D = 0, d = 0, kk = 0;
   uint64_t dig0 = 0, dig1 = 0;
   Walk w;
-  unsigned long long nodes = 0, leaves = 0;
+  unsigned long long nodes = 0, leaves = 0;  // kept by the group's lane 0
   uint32_t owed = 0;  // leaf children (bit k = child k) of the node at depth d not yet written
-  int saved_slot = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+  const int gid = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 3);
+  int saved_slot = gid;
   unsigned iter = 0;
 
   while (true) {
-    // ---- acquire work: this thread's saved walk first, then fresh prefixes ----
-    if (!have) {
+    // ---- acquire work (group-uniform): this group's saved walk first, then prefixes ----
+    if (!have && !done) {
       if (saved_slot < P.nsaved_in) {
         const Saved sv = P.saved_in[saved_slot];
-        saved_slot = P.nsaved_in;  // at most one saved walk per thread
-        prefix = sv.prefix;
-        const Prefix pf = P.prefixes[prefix];
-        cell = pf.cell;
-        D = (int)pf.depth;
+        saved_slot = P.nsaved_in;  // at most one saved walk per group
+        cell = sv.cell;
+        D = sv.D;
         d = sv.d;
         kk = sv.kk;
-        seq = sv.seq;
-        dig0 = sv.dig[0];
-        dig1 = sv.dig[1];
         owed = sv.owed;
+        dig0 = sv.dig0;
+        dig1 = sv.dig1;
+        have = true;
       } else {
-        if (*(volatile int *)P.full_flag) break;
-        unsigned long long p = atomicAdd(P.next_prefix, 1ULL);
-        if (p >= (unsigned long long)P.nprefix) break;
-        prefix = (uint32_t)p;
-        const Prefix pf = P.prefixes[p];
-        cell = pf.cell;
-        D = (int)pf.depth;
-        d = D;
-        kk = 0;
-        seq = 0;
-        dig0 = pf.digits;
-        dig1 = 0;
-        owed = 0;
+        unsigned long long p = ~0ULL;
+        if (j == 0 && !*(volatile int *)P.stop_flag) p = atomicAdd(P.next_prefix, 1ULL);
+        p = __shfl_sync(gmask, p, leader);
+        if (p >= (unsigned long long)P.nprefix) {
+          done = true;
+        } else {
+          const Prefix pf = P.prefixes[p];
+          cell = pf.cell;
+          D = (int)pf.depth;
+          d = D;
+          kk = 0;
+          owed = 0;
+          dig0 = pf.dig0;
+          dig1 = pf.dig1;
+          have = true;
+        }
       }
-      init_walk(w, P.cells[cell], L, m);
-      for (int t = 0; t < d; t++) place(w, fx[t][getdig(dig0, dig1, t)]);
-      have = true;
+      if (have) {
+        init_walk(w, P.cells[cell], L, m);
+        for (int t = 0; t < d; t++) place(w, fx[t][getdig(dig0, dig1, t)]);
+      }
     }
+    if (__all_sync(FULL_MASK, done)) break;
 
-    // ---- one tree step ----
+    // ---- test the children (one per lane) ----
+    const bool leaf_level = have && d + 1 == half;
+    bool ok = false;
+    if (have && owed == 0 && j >= kk) {
+      const QuadFx &f = fx[d][j];
+      const uint64_t a0 = w.s0 + (uint64_t)f.ds[0], a1 = w.s1 + (uint64_t)f.ds[1];
+      const uint64_t a2 = w.s2 + (uint64_t)f.ds[2], a3 = w.s3 + (uint64_t)f.ds[3];
+      ok = ((a0 & a1 & a2 & a3) & M) == M;
+    }
+    const unsigned gm = (__ballot_sync(FULL_MASK, ok) >> (8 * g)) & 0xFFu;
+
+    // ---- leaves: a leaf-level node's feasible children, or leaves owed from before ----
+    bool emit = false;
+    if (have) {
+      if (owed) emit = (owed >> j) & 1u;
+      else if (leaf_level) emit = ok;
+    }
+    const unsigned eb = __ballot_sync(FULL_MASK, emit);
+    bool written = false;
+    if (eb) {
+      unsigned long long base = 0;
+      const int first = __ffs(eb) - 1;
+      if (lane == first) base = atomicAdd(P.leaf_count, (unsigned long long)__popc(eb));
+      base = __shfl_sync(FULL_MASK, base, first);
+      if (emit) {
+        const unsigned long long slot = base + __popc(eb & ((1u << lane) - 1u));
+        if (slot < P.leaf_cap) {
+          const QuadFx &f = fx[d][j];
+          uint64_t lx = w.X | f.bx, ly = w.Y | f.by;
+          if (L & 1) {
+            Walk t;
+            t.s0 = w.s0 + (uint64_t)f.ds[0];
+            t.s1 = w.s1 + (uint64_t)f.ds[1];
+            t.s2 = w.s2 + (uint64_t)f.ds[2];
+            t.s3 = w.s3 + (uint64_t)f.ds[3];
+            middle_bits(t, half, cm, lx, ly);
+          }
+          uint64_t p0 = dig0, p1 = dig1;
+          setdig(p0, p1, d, j);
+          P.leaf_words[2 * slot] = lx;
+          P.leaf_words[2 * slot + 1] = ly;
+          P.leaf_keys[2 * slot] = nibble_reverse(p0);
+          P.leaf_keys[2 * slot + 1] = nibble_reverse(p1);
+          P.leaf_cell[slot] = cell;
+          written = true;
+        } else {
+          atomicExch(P.stop_flag, 1);  // buffer full: the rest stays owed, the walk suspends
+        }
+      }
+    }
+    const unsigned gw = (__ballot_sync(FULL_MASK, written) >> (8 * g)) & 0xFFu;
+    const unsigned gunw = (__ballot_sync(FULL_MASK, emit && !written) >> (8 * g)) & 0xFFu;
+
+    // ---- move the walk (group-uniform) ----
     bool finished = false;
-    if (owed == 0) {
-      if (kk == 8) {
+    if (have) {
+      if (j == 0) leaves += __popc(gw);
+      if (owed || leaf_level) {
+        if (!owed && j == 0) nodes += 8 - kk;  // every child of a leaf-level node is a node
+        owed = gunw;
+        kk = 8;
+      } else if (gm) {
+        const int c = __ffs(gm) - 1;  // the first feasible untried child
+        if (j == 0) nodes += c - kk + 1;
+        setdig(dig0, dig1, d, c);
+        place(w, fx[d][c]);
+        d++;
+        kk = 0;
+      } else {
+        if (j == 0) nodes += 8 - kk;
+        kk = 8;
+      }
+      if (kk == 8 && owed == 0) {  // the node is done: back to its parent
         if (d == D) {
           finished = true;
         } else {
           d--;
-          kk = getdig(dig0, dig1, d);
-          unplace(w, fx[d][kk], posm[d]);
-          kk++;
-        }
-      } else if (d + 1 == half) {
-        // the children are leaves: test the remaining ones together (each is one node, as
-        // the reference counts them), then write the class-exact ones below
-        uint32_t lm = 0;
-        for (int k = kk; k < 8; k++) {
-          const QuadFx &f = fx[d][k];
-          const uint64_t a0 = w.s0 + (uint64_t)f.ds[0], a1 = w.s1 + (uint64_t)f.ds[1];
-          const uint64_t a2 = w.s2 + (uint64_t)f.ds[2], a3 = w.s3 + (uint64_t)f.ds[3];
-          if (((a0 & a1 & a2 & a3) & M) == M) lm |= 1u << k;
-        }
-        nodes += 8 - kk;
-        owed = lm;
-        kk = 8;
-      } else {
-        const QuadFx &f = fx[d][kk];
-        place(w, f);
-        nodes++;
-        if (!feasible(w, M)) {
-          unplace(w, f, posm[d]);
-          kk++;
-        } else {
-          setdig(dig0, dig1, d, kk);
-          d++;
-          kk = 0;
+          const int c = getdig(dig0, dig1, d);
+          unplace(w, fx[d][c], posm[d]);
+          kk = c + 1;
         }
       }
     }
 
-    // ---- warp-aggregated append of the owed leaves, in child order ----
-    // Each lane owes at most 8 leaves; four ballots of the count's bits give every lane its
-    // exclusive prefix and the warp total, so one atomic reserves the warp's slots.
-    const unsigned act = __activemask();
-    const unsigned cnt = (unsigned)__popc(owed);
-    const unsigned b0 = __ballot_sync(act, cnt & 1u), b1 = __ballot_sync(act, cnt & 2u);
-    const unsigned b2 = __ballot_sync(act, cnt & 4u), b3 = __ballot_sync(act, cnt & 8u);
-    const unsigned total = __popc(b0) + 2u * __popc(b1) + 4u * __popc(b2) + 8u * __popc(b3);
-    if (total) {
-      const unsigned lt = (1u << lane) - 1u;
-      const unsigned before = __popc(b0 & lt) + 2u * __popc(b1 & lt) + 4u * __popc(b2 & lt) +
-                              8u * __popc(b3 & lt);
-      const int leader = __ffs(act) - 1;
-      unsigned long long base = 0;
-      if (lane == leader) base = atomicAdd(P.leaf_count, (unsigned long long)total);
-      base = __shfl_sync(act, base, leader);
-      unsigned long long slot = base + before;
-      while (owed) {
-        if (slot >= P.leaf_cap) {
-          atomicExch(P.full_flag, 1);  // the rest stays owed: suspend below
-          break;
-        }
-        const int k = __ffs(owed) - 1;
-        const QuadFx &f = fx[d][k];
-        uint64_t lx = w.X | f.bx, ly = w.Y | f.by;
-        if (L & 1) {
-          Walk t;
-          t.s0 = w.s0 + (uint64_t)f.ds[0];
-          t.s1 = w.s1 + (uint64_t)f.ds[1];
-          t.s2 = w.s2 + (uint64_t)f.ds[2];
-          t.s3 = w.s3 + (uint64_t)f.ds[3];
-          middle_bits(t, half, cm, lx, ly);
-        }
-        P.leaf_words[2 * slot] = lx;
-        P.leaf_words[2 * slot + 1] = ly;
-        P.leaf_keys[slot] = ((unsigned long long)prefix << 32) | seq;
-        seq++;
-        leaves++;
-        slot++;
-        owed &= owed - 1;
-      }
-    }
-
-    // ---- suspend with leaves still owed, or at a clean point once the buffer is full ----
+    // ---- suspend with leaves still owed, or at a clean point once asked to stop ----
     iter++;
-    const bool suspend = !finished &&
-                         (owed != 0 || ((iter & 255) == 0 && *(volatile int *)P.full_flag));
-    if (suspend) {
+    bool suspend = have && !finished && owed != 0;
+    if (have && !finished && !suspend && (iter & 255) == 0) {
+      int st = 0;
+      if (j == 0) {
+        if (*(volatile int *)P.stop_flag) st = 1;
+        else if (P.round_ns && globaltimer() - t_start > P.round_ns) { atomicExch(P.stop_flag, 1); st = 1; }
+      }
+      suspend = __shfl_sync(gmask, st, leader) != 0;
+    }
+    if (suspend && j == 0) {
       const unsigned k = atomicAdd(P.nsaved_out, 1u);
       if ((int)k < P.saved_cap) {
         Saved sv;
-        sv.prefix = prefix;
-        sv.seq = seq;
+        sv.cell = cell;
+        sv.D = (uint16_t)D;
         sv.d = (uint16_t)d;
         sv.kk = (uint16_t)kk;
         sv.owed = (uint16_t)owed;
         sv.pad = 0;
-        sv.dig[0] = dig0;
-        sv.dig[1] = dig1;
+        sv.dig0 = dig0;
+        sv.dig1 = dig1;
         P.saved_out[k] = sv;
       } else {
         atomicCAS(P.status, 0, BS_ERR_INTERNAL);
       }
     }
     if (finished || suspend) {
-      if (nodes) atomicAdd(P.cell_nodes + cell, nodes);
-      if (leaves) atomicAdd(P.cell_leaves + cell, leaves);
+      if (j == 0) {
+        if (nodes) atomicAdd(P.cell_nodes + cell, nodes);
+        if (leaves) atomicAdd(P.cell_leaves + cell, leaves);
+      }
       nodes = 0;
       leaves = 0;
       have = false;
       owed = 0;
-      if (suspend) break;
+      if (suspend) done = true;
     }
   }
 }
 
-// Compact the leaves that passed the Hall filter (with their keys), count passes per cell.
+// Compact the leaves that passed the Hall filter (with their keys and cells), count passes
+// per cell.
 __global__ void compact_kernel(const uint64_t *__restrict__ words, const uint64_t *__restrict__ keys,
-                               const uint8_t *__restrict__ pass, long long count,
-                               const Prefix *__restrict__ prefixes, uint64_t *out_words,
-                               uint64_t *out_keys, unsigned long long *out_count,
+                               const uint32_t *__restrict__ lcell, const uint8_t *__restrict__ pass,
+                               long long count, uint64_t *out_words, uint64_t *out_keys,
+                               uint32_t *out_cell, unsigned long long *out_count,
                                unsigned long long out_cap, unsigned long long *cell_ok) {
   const int lane = threadIdx.x & 31;
   for (long long base = (long long)blockIdx.x * blockDim.x; base < count;
@@ -340,13 +384,15 @@ __global__ void compact_kernel(const uint64_t *__restrict__ words, const uint64_
     o = __shfl_sync(FULL_MASK, o, leader);
     if (p) {
       unsigned long long slot = o + __popc(ball & ((1u << lane) - 1u));
-      uint64_t k = keys[i];
+      const uint32_t c = lcell[i];
       if (slot < out_cap) {
         out_words[2 * slot] = words[2 * i];
         out_words[2 * slot + 1] = words[2 * i + 1];
-        out_keys[slot] = k;
+        out_keys[2 * slot] = keys[2 * i];
+        out_keys[2 * slot + 1] = keys[2 * i + 1];
+        out_cell[slot] = c;
       }
-      atomicAdd(cell_ok + prefixes[k >> 32].cell, 1ULL);
+      atomicAdd(cell_ok + c, 1ULL);
     }
   }
 }
@@ -390,7 +436,7 @@ struct Frontier {
     nodes++;
     if (!check()) return;
     if (d == D) {
-      out->push_back(Prefix{cell, (uint32_t)D, digits});
+      out->push_back(Prefix{cell, (uint32_t)D, digits, 0});
       return;
     }
     const int i1 = d, i2 = L - 1 - d, c1 = i1 % m, c2 = i2 % m;
@@ -425,12 +471,14 @@ struct StreamBufs {
   Prefix *prefixes = nullptr; long long prefix_cap = 0;
   Saved *saved[2] = {nullptr, nullptr}; long long saved_cap = 0;
   uint64_t *leaf_words = nullptr, *leaf_keys = nullptr; long long leaf_cap = 0;
+  uint32_t *leaf_cell = nullptr;
   uint8_t *leaf_pass = nullptr; long long pass_cap = 0;
   uint64_t *surv_words = nullptr, *surv_keys = nullptr; long long surv_cap = 0;
+  uint32_t *surv_cell = nullptr;
   unsigned long long *counters = nullptr;  // see below
   unsigned long long *cell_stats = nullptr; long long cell_stats_cap = 0;
   unsigned *nsaved = nullptr;
-  int *full = nullptr;
+  int *stop = nullptr;
   QuadFx *fx = nullptr;      // [32][16] branch effects
   uint64_t *posm = nullptr;  // [32] position masks
 };
@@ -444,12 +492,26 @@ void bs_stream_free(bs_ctx *ctx) {
   StreamBufs *b = (StreamBufs *)ctx->stream_bufs;
   if (!b) return;
   cudaFree(b->cells); cudaFree(b->prefixes); cudaFree(b->saved[0]); cudaFree(b->saved[1]);
-  cudaFree(b->leaf_words); cudaFree(b->leaf_keys); cudaFree(b->leaf_pass);
-  cudaFree(b->surv_words); cudaFree(b->surv_keys); cudaFree(b->counters);
-  cudaFree(b->cell_stats); cudaFree(b->nsaved); cudaFree(b->full); cudaFree(b->fx);
+  cudaFree(b->leaf_words); cudaFree(b->leaf_keys); cudaFree(b->leaf_cell); cudaFree(b->leaf_pass);
+  cudaFree(b->surv_words); cudaFree(b->surv_keys); cudaFree(b->surv_cell); cudaFree(b->counters);
+  cudaFree(b->cell_stats); cudaFree(b->nsaved); cudaFree(b->stop); cudaFree(b->fx);
   cudaFree(b->posm);
   delete b;
   ctx->stream_bufs = nullptr;
+}
+
+// Grows a leaf or survivor store (words and keys: 2 words each; cells) to at least `want`.
+static int ensure_store(uint64_t **words, uint64_t **keys, uint32_t **cellv, long long *cap,
+                        long long want) {
+  if (*cap >= want && *words) return BS_OK;
+  cudaFree(*words); cudaFree(*keys); cudaFree(*cellv);
+  *words = nullptr; *keys = nullptr; *cellv = nullptr; *cap = 0;
+  cudaError_t e = cudaMalloc(words, sizeof(uint64_t) * 2 * want);
+  if (e == cudaSuccess) e = cudaMalloc(keys, sizeof(uint64_t) * 2 * want);
+  if (e == cudaSuccess) e = cudaMalloc(cellv, sizeof(uint32_t) * want);
+  if (e != cudaSuccess) return bs_cuda_fail(e);
+  *cap = want;
+  return BS_OK;
 }
 
 extern "C" int bs_cd_stream(bs_ctx *ctx, const bs_cell *cells, int ncells, const bs_stream_opts *opt,
@@ -471,7 +533,7 @@ extern "C" int bs_cd_stream(bs_ctx *ctx, const bs_cell *cells, int ncells, const
   const int half = L / 2;
 
   // ---- coarse frontier of each cell on the host, in the reference's order ----
-  // A Prefix holds the digits of 16 depths, so no prefix is deeper than that.
+  // The first split stops at depth 16 (one digit word); later splits go deeper.
   static const HostQuads Q;
   const int max_depth = std::min(half - 1, 16);
   std::vector<Frontier> F(ncells);
@@ -508,6 +570,23 @@ extern "C" int bs_cd_stream(bs_ctx *ctx, const bs_cell *cells, int ncells, const
   }
   const long long ncoarse = (long long)coarse.size();
 
+  // Places (sign +1) or removes (-1) branch k of depth t on a cell's host walker.
+  auto apply = [&](Frontier &f, int t, int k, int sign) {
+    const int(*S)[4] = (t == 0) ? (f.root == 2 ? Q.neg : (f.root == 1 ? Q.pos : Q.all)) : Q.pos;
+    const int ns = (t == 0) ? f.ns0 : 8;
+    const int q = f.rev ? ns - 1 - k : k;
+    const int c1 = t % m, c2 = (L - 1 - t) % m;
+    f.px[c1] += sign * S[q][0]; f.py[c1] += sign * S[q][1];
+    f.px[c2] += sign * S[q][2]; f.py[c2] += sign * S[q][3];
+    f.placed[c1] += sign; f.placed[c2] += sign;
+  };
+  auto digit = [](uint64_t d0, uint64_t d1, int t) {
+    return (int)((((t < 16) ? d0 : d1) >> (4 * (t & 15))) & 15);
+  };
+  auto reset = [](Frontier &f) {
+    memset(f.px, 0, sizeof f.px); memset(f.py, 0, sizeof f.py); memset(f.placed, 0, sizeof f.placed);
+  };
+
   // The subtrees of coarse prefix p, refined by k more levels: the fine prefixes of its
   // subtree at depth p.depth + k, in stream order. Returns the host nodes it adds (the coarse
   // node itself was counted when the frontier was built).
@@ -517,36 +596,64 @@ extern "C" int bs_cd_stream(bs_ctx *ctx, const bs_cell *cells, int ncells, const
       return 0;
     }
     Frontier &f = F[p.cell];
-    memset(f.px, 0, sizeof f.px); memset(f.py, 0, sizeof f.py); memset(f.placed, 0, sizeof f.placed);
-    for (int t = 0; t < (int)p.depth; t++) {
-      const int(*S)[4] = (t == 0) ? (f.root == 2 ? Q.neg : (f.root == 1 ? Q.pos : Q.all)) : Q.pos;
-      const int ns = (t == 0) ? f.ns0 : 8;
-      const int kk = (int)((p.digits >> (4 * t)) & 15);
-      const int q = f.rev ? ns - 1 - kk : kk;
-      const int c1 = t % m, c2 = (L - 1 - t) % m;
-      f.px[c1] += S[q][0]; f.py[c1] += S[q][1]; f.px[c2] += S[q][2]; f.py[c2] += S[q][3];
-      f.placed[c1]++; f.placed[c2]++;
-    }
+    reset(f);
+    for (int t = 0; t < (int)p.depth; t++) apply(f, t, digit(p.dig0, p.dig1, t), +1);
     f.D = (int)p.depth + k;
     f.out = &out;
     const long long before = f.nodes;
-    f.rec((int)p.depth, p.digits);
+    f.rec((int)p.depth, p.dig0);
     return f.nodes - before - 1;
+  };
+
+  // A suspended walk's remaining work as subtree roots: its node at depth d itself if none
+  // of its children was tried yet, else the children kk.. of that node; then the later
+  // siblings of each node on its path up to its root depth D. Each sibling is a node the
+  // device would have counted on placing it; infeasible ones end there.
+  auto split_walk = [&](const Saved &w, std::vector<Prefix> &out) -> long long {
+    Frontier &f = F[w.cell];
+    reset(f);
+    for (int t = 0; t < (int)w.d; t++) apply(f, t, digit(w.dig0, w.dig1, t), +1);
+    long long added = 0;
+    for (int t = (int)w.d; t >= (int)w.D; t--) {
+      if (t < (int)w.d) apply(f, t, digit(w.dig0, w.dig1, t), -1);
+      // the path's digits above depth t
+      uint64_t p0 = w.dig0, p1 = w.dig1;
+      for (int u = t; u < 32; u++) {
+        const int s = 4 * (u & 15);
+        if (u < 16) p0 &= ~(15ULL << s);
+        else p1 &= ~(15ULL << s);
+      }
+      int first;
+      if (t == (int)w.d) {
+        if (w.kk == 0) {  // untouched below (already counted): it is a subtree root as it is
+          out.push_back(Prefix{w.cell, (uint32_t)t, p0, p1});
+          continue;
+        }
+        if (t + 1 >= half) continue;  // a leaf-level node: its children were tested together
+        first = (int)w.kk;
+      } else {
+        first = digit(w.dig0, w.dig1, t) + 1;
+      }
+      for (int k = first; k < 8; k++) {
+        apply(f, t, k, +1);
+        added++;
+        if (f.check()) {
+          uint64_t q0 = p0, q1 = p1;
+          if (t < 16) q0 |= (uint64_t)k << (4 * t);
+          else q1 |= (uint64_t)k << (4 * (t - 16));
+          out.push_back(Prefix{w.cell, (uint32_t)(t + 1), q0, q1});
+        }
+        apply(f, t, k, -1);
+      }
+    }
+    return added;
   };
 
   // ---- device buffers ----
   int rc = bs_ensure_dev((void **)&B->cells, &B->cells_cap, ncells, sizeof(CellDev));
   if (!rc) rc = bs_ensure_dev((void **)&B->cell_stats, &B->cell_stats_cap, 3LL * ncells, sizeof(unsigned long long));
   long long leaf_cap = opt->leaf_chunk > 0 ? opt->leaf_chunk : (1LL << 24);
-  if (!rc) {
-    long long c0 = B->leaf_cap;
-    rc = bs_ensure_dev((void **)&B->leaf_keys, &B->leaf_cap, leaf_cap, sizeof(uint64_t));
-    if (!rc && (B->leaf_cap != c0 || !B->leaf_words)) {
-      cudaFree(B->leaf_words);
-      B->leaf_words = nullptr;
-      CK(cudaMalloc(&B->leaf_words, sizeof(uint64_t) * 2 * B->leaf_cap));
-    }
-  }
+  if (!rc) rc = ensure_store(&B->leaf_words, &B->leaf_keys, &B->leaf_cell, &B->leaf_cap, leaf_cap);
   if (!rc) rc = bs_ensure_dev((void **)&B->leaf_pass, &B->pass_cap, leaf_cap, 1);
   const int block = 256;
   // register budget variant (BS_DFS_BLOCKS=6 selects the 40-register one) and the grid of
@@ -570,20 +677,12 @@ extern "C" int bs_cd_stream(bs_ctx *ctx, const bs_cell *cells, int ncells, const
   if (!rc && !B->counters) {
     CK(cudaMalloc(&B->counters, sizeof(unsigned long long) * 8));
     CK(cudaMalloc(&B->nsaved, sizeof(unsigned) * 2));
-    CK(cudaMalloc(&B->full, sizeof(int)));
+    CK(cudaMalloc(&B->stop, sizeof(int)));
     CK(cudaMalloc(&B->fx, sizeof(QuadFx) * 32 * 16));
     CK(cudaMalloc(&B->posm, sizeof(uint64_t) * 32));
   }
   long long surv_cap = opt->survivor_cap > 0 ? opt->survivor_cap : (1LL << 22);
-  if (!rc) {
-    long long c0 = B->surv_cap;
-    rc = bs_ensure_dev((void **)&B->surv_keys, &B->surv_cap, surv_cap, sizeof(uint64_t));
-    if (!rc && (B->surv_cap != c0 || !B->surv_words)) {
-      cudaFree(B->surv_words);
-      B->surv_words = nullptr;
-      CK(cudaMalloc(&B->surv_words, sizeof(uint64_t) * 2 * B->surv_cap));
-    }
-  }
+  if (!rc) rc = ensure_store(&B->surv_words, &B->surv_keys, &B->surv_cell, &B->surv_cap, surv_cap);
   if (rc) return rc;
   surv_cap = B->surv_cap;
   leaf_cap = B->leaf_cap;
@@ -623,24 +722,34 @@ extern "C" int bs_cd_stream(bs_ctx *ctx, const bs_cell *cells, int ncells, const
   CK(cudaMemcpyAsync(B->posm, posm.data(), sizeof(uint64_t) * 32, cudaMemcpyHostToDevice, s));
   CK(cudaMemcpyAsync(B->cells, hc.data(), sizeof(CellDev) * ncells, cudaMemcpyHostToDevice, s));
   CK(cudaMemsetAsync(B->cell_stats, 0, sizeof(unsigned long long) * 3 * ncells, s));
-  // counters: [0] next prefix of the wave, [1] leaf count of the round, [2] survivors of the wave
+  // counters: [0] next prefix of the queue, [1] leaf count of the round, [2] survivors of the wave
   unsigned long long *cell_nodes = B->cell_stats, *cell_leaves = B->cell_stats + ncells,
                      *cell_ok = B->cell_stats + 2 * ncells;
 
   // ---- waves: runs of coarse prefixes, in stream order, refined to fill the GPU ----
-  // A wave's survivors all precede the next wave's, so each wave is ordered on its own and
-  // appended. The width (coarse prefixes per wave) and the refinement depth adapt to the
-  // nodes per coarse prefix seen so far: fine subtrees of ~FINE_NODES nodes, waves of
+  // A leaf's key is its branch path, so survivors sort into stream order however the work
+  // was divided; a wave's survivors all precede the next wave's, so each wave is ordered on
+  // its own and appended. The width (coarse prefixes per wave) and the refinement depth adapt
+  // to the nodes per coarse prefix seen so far: fine subtrees of ~FINE_NODES nodes, waves of
   // ~WAVE_NODES nodes, and under `limit` no wider than the survivors still owed suggest.
+  // Inside a wave, a launch lasts at most ROUND_NS; when the queue is empty and fewer walks
+  // than walkers remain, the suspended walks are split into their remaining subtrees, so one
+  // large subtree never holds the GPU with a few walkers.
   const long long limit = opt->limit > 0 ? opt->limit : 0;
   const double FINE_NODES = 2e4, WAVE_NODES = 8e9, NOMINAL_RATE = 2e10;
-  const long long threads = (long long)grid * block;
+  const unsigned long long ROUND_NS = opt->round_us > 0 ? (unsigned long long)opt->round_us * 1000ULL
+                                                        : 25000000ULL;
+  const long long walkers = (long long)grid * block / 8;  // eight lanes walk one subtree
   std::vector<uint64_t> res_words;
   std::vector<uint32_t> res_cell;
-  std::vector<Prefix> fine;
+  std::vector<Prefix> fine, pieces;
+  std::vector<Saved> walks, keep_walks;
   std::vector<uint64_t> wkeys, wwords;
+  std::vector<uint32_t> wcell;
   std::vector<unsigned long long> cs_prev(3 * (size_t)ncells, 0), cs(3 * (size_t)ncells, 0);
-  long long pos = 0, wave_width = std::min<long long>(ncoarse, 1024);
+  // the first wave is a probe: small under `limit` (a few coarse prefixes can hold far more
+  // survivors than asked for), wider otherwise; later waves grow at most 4x at a time
+  long long pos = 0, wave_width = std::min<long long>(ncoarse, limit ? 8 : 256);
   int k_refine = (half - deepest >= 6) ? 2 : 0;
   long long have = 0;
   static const bool trace = getenv("BS_STREAM_TRACE") != nullptr;  // per-wave figures on stderr
@@ -652,19 +761,17 @@ extern "C" int bs_cd_stream(bs_ctx *ctx, const bs_cell *cells, int ncells, const
       host_nodes[coarse[i].cell] += refine(coarse[i], k, fine);
     }
     pos += take;
-    const long long nprefix = (long long)fine.size();
+    long long nprefix = (long long)fine.size();
     if (nprefix == 0) continue;  // the refinement pruned the whole run
-    if (nprefix >= (1LL << 32)) return BS_ERR_CAP;
     rc = bs_ensure_dev((void **)&B->prefixes, &B->prefix_cap, nprefix, sizeof(Prefix));
     if (rc) return rc;
     CK(cudaMemcpyAsync(B->prefixes, fine.data(), sizeof(Prefix) * nprefix, cudaMemcpyHostToDevice, s));
     CK(cudaMemsetAsync(B->counters, 0, sizeof(unsigned long long) * 8, s));
     const auto t_wave = std::chrono::steady_clock::now();
-
-    int nsaved = 0, cur = 0;
+    int nsaved = 0, cur = 0, rounds = 0, splits = 0;
     for (;;) {
       CK(cudaMemsetAsync(B->nsaved, 0, sizeof(unsigned), s));
-      CK(cudaMemsetAsync(B->full, 0, sizeof(int), s));
+      CK(cudaMemsetAsync(B->stop, 0, sizeof(int), s));
       CK(cudaMemsetAsync(B->counters + 1, 0, sizeof(unsigned long long), s));
       CdParams P;
       P.L = L; P.m = m; P.half = half;
@@ -675,19 +782,21 @@ extern "C" int bs_cd_stream(bs_ctx *ctx, const bs_cell *cells, int ncells, const
       P.next_prefix = B->counters;
       P.saved_in = B->saved[cur]; P.nsaved_in = nsaved;
       P.saved_out = B->saved[cur ^ 1]; P.nsaved_out = B->nsaved; P.saved_cap = saved_cap;
-      P.leaf_words = B->leaf_words; P.leaf_keys = B->leaf_keys;
+      P.leaf_words = B->leaf_words; P.leaf_keys = B->leaf_keys; P.leaf_cell = B->leaf_cell;
       P.leaf_count = B->counters + 1; P.leaf_cap = (unsigned long long)leaf_cap;
       P.cell_nodes = cell_nodes; P.cell_leaves = cell_leaves;
-      P.full_flag = B->full; P.status = ctx->d_status;
+      P.stop_flag = B->stop; P.round_ns = ROUND_NS; P.status = ctx->d_status;
       bs_timed_begin(ctx);
       dfs_kernel<<<grid, block, 0, s>>>(P);
       bs_timed_end(ctx);
       CK(cudaGetLastError());
-      unsigned long long leaf_count = 0;
+      unsigned long long leaf_count = 0, nextp = 0;
       unsigned nsv = 0;
       CK(cudaMemcpyAsync(&leaf_count, B->counters + 1, sizeof leaf_count, cudaMemcpyDeviceToHost, s));
+      CK(cudaMemcpyAsync(&nextp, B->counters, sizeof nextp, cudaMemcpyDeviceToHost, s));
       CK(cudaMemcpyAsync(&nsv, B->nsaved, sizeof nsv, cudaMemcpyDeviceToHost, s));
       CK(cudaStreamSynchronize(s));
+      rounds++;
       if ((int)nsv > saved_cap) return BS_ERR_INTERNAL;
       long long nleaf = (long long)std::min<unsigned long long>(leaf_count, (unsigned long long)leaf_cap);
       if (nleaf > 0) {
@@ -695,17 +804,38 @@ extern "C" int bs_cd_stream(bs_ctx *ctx, const bs_cell *cells, int ncells, const
         if (r2) return r2;
         ctx->launches++;
         compact_kernel<<<bs_grid_for(nleaf, 256, 8 * ctx->num_sms), 256, 0, s>>>(
-            B->leaf_words, B->leaf_keys, B->leaf_pass, nleaf, B->prefixes, B->surv_words, B->surv_keys,
-            B->counters + 2, (unsigned long long)surv_cap, cell_ok);
+            B->leaf_words, B->leaf_keys, B->leaf_cell, B->leaf_pass, nleaf, B->surv_words,
+            B->surv_keys, B->surv_cell, B->counters + 2, (unsigned long long)surv_cap, cell_ok);
         CK(cudaGetLastError());
       }
       nsaved = (int)nsv;
       cur ^= 1;
-      if (nsaved == 0) {
-        unsigned long long nextp = 0;
-        CK(cudaMemcpyAsync(&nextp, B->counters, sizeof nextp, cudaMemcpyDeviceToHost, s));
+      const bool queue_empty = nextp >= (unsigned long long)nprefix;
+      if (nsaved == 0 && queue_empty) break;
+      // few walks left and nothing queued: split the walks into their remaining subtrees
+      if (queue_empty && nsaved > 0 && (long long)nsaved * 4 < walkers * 3 && leaf_count < (unsigned long long)leaf_cap) {
+        walks.resize(nsaved);
+        CK(cudaMemcpyAsync(walks.data(), B->saved[cur], sizeof(Saved) * nsaved, cudaMemcpyDeviceToHost, s));
         CK(cudaStreamSynchronize(s));
-        if (nextp >= (unsigned long long)nprefix) break;
+        pieces.clear();
+        keep_walks.clear();
+        for (const Saved &w : walks) {
+          if (w.owed) keep_walks.push_back(w);  // leaves still to write: resume as is
+          else host_nodes[w.cell] += split_walk(w, pieces);
+        }
+        nprefix = (long long)pieces.size();
+        if (nprefix >= (1LL << 40)) return BS_ERR_CAP;
+        if (nprefix > 0) {
+          rc = bs_ensure_dev((void **)&B->prefixes, &B->prefix_cap, nprefix, sizeof(Prefix));
+          if (rc) return rc;
+          CK(cudaMemcpyAsync(B->prefixes, pieces.data(), sizeof(Prefix) * nprefix, cudaMemcpyHostToDevice, s));
+        }
+        nsaved = (int)keep_walks.size();
+        if (nsaved > 0)
+          CK(cudaMemcpyAsync(B->saved[cur], keep_walks.data(), sizeof(Saved) * nsaved, cudaMemcpyHostToDevice, s));
+        CK(cudaMemsetAsync(B->counters, 0, sizeof(unsigned long long), s));
+        splits++;
+        if (nsaved == 0 && nprefix == 0) break;
       }
     }
 
@@ -727,20 +857,26 @@ extern "C" int bs_cd_stream(bs_ctx *ctx, const bs_cell *cells, int ncells, const
       return BS_ERR_CAP;
     }
     if (nsurv > 0) {
-      wkeys.resize(nsurv);
+      wkeys.resize(2 * nsurv);
       wwords.resize(2 * nsurv);
-      CK(cudaMemcpyAsync(wkeys.data(), B->surv_keys, sizeof(uint64_t) * nsurv, cudaMemcpyDeviceToHost, s));
+      wcell.resize(nsurv);
+      CK(cudaMemcpyAsync(wkeys.data(), B->surv_keys, sizeof(uint64_t) * 2 * nsurv, cudaMemcpyDeviceToHost, s));
       CK(cudaMemcpyAsync(wwords.data(), B->surv_words, sizeof(uint64_t) * 2 * nsurv, cudaMemcpyDeviceToHost, s));
+      CK(cudaMemcpyAsync(wcell.data(), B->surv_cell, sizeof(uint32_t) * nsurv, cudaMemcpyDeviceToHost, s));
       CK(cudaStreamSynchronize(s));
       std::vector<uint32_t> order(nsurv);
       for (uint32_t i = 0; i < (uint32_t)nsurv; i++) order[i] = i;
-      std::sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) { return wkeys[a] < wkeys[b]; });
+      std::sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) {
+        if (wcell[a] != wcell[b]) return wcell[a] < wcell[b];
+        if (wkeys[2 * a] != wkeys[2 * b]) return wkeys[2 * a] < wkeys[2 * b];
+        return wkeys[2 * a + 1] < wkeys[2 * b + 1];
+      });
       long long keep = (long long)nsurv;
       if (limit) keep = std::min(keep, limit - have);
       for (long long i = 0; i < keep; i++) {
         res_words.push_back(wwords[2 * order[i]]);
         res_words.push_back(wwords[2 * order[i] + 1]);
-        res_cell.push_back(fine[wkeys[order[i]] >> 32].cell);
+        res_cell.push_back(wcell[order[i]]);
       }
       have += keep;
     }
@@ -755,17 +891,19 @@ extern "C" int bs_cd_stream(bs_ctx *ctx, const bs_cell *cells, int ncells, const
     k_refine = 0;
     while (k_refine < 16 && per_coarse / std::pow(8.0, k_refine) > FINE_NODES) k_refine++;
     double width = std::max(WAVE_NODES, rate * 0.25) / per_coarse;
-    // enough fine prefixes for every thread, twice over
-    width = std::max(width, 2.0 * (double)threads / std::pow(8.0, k_refine));
+    // enough fine prefixes for every walker, twice over
+    width = std::max(width, 2.0 * (double)walkers / std::pow(8.0, k_refine));
+    width = std::min(width, 4.0 * (double)take);
     if (limit && nsurv > 0) {
       const double per_coarse_surv = (double)nsurv / (double)take;
-      width = std::min(width, std::max(64.0, 1.5 * (double)(limit - have) / per_coarse_surv));
+      width = std::min(width, std::max(8.0, 1.5 * (double)(limit - have) / per_coarse_surv));
     }
     wave_width = (long long)std::min<double>(width, (double)(1LL << 40));
     if (trace)
-      fprintf(stderr, "[bs_cd_stream] wave coarse=%lld fine=%lld nodes=%llu surv=%llu have=%lld "
-                      "secs=%.4f next_width=%lld next_k=%d pos=%lld/%lld\n",
-              take, nprefix, wave_nodes, nsurv, have, secs, wave_width, k_refine, pos, ncoarse);
+      fprintf(stderr, "[bs_cd_stream] wave coarse=%lld fine=%lld rounds=%d splits=%d nodes=%llu "
+                      "surv=%llu have=%lld secs=%.4f next_width=%lld next_k=%d pos=%lld/%lld\n",
+              take, (long long)fine.size(), rounds, splits, wave_nodes, nsurv, have, secs, wave_width,
+              k_refine, pos, ncoarse);
   }
 
   // ---- results ----

@@ -35,7 +35,8 @@ struct AbParams {
   long long max_cycles;
   const AbCandDev *cands;
   long long ncand;
-  const int8_t *rows;
+  const uint64_t *roww;  // allowed rows as 4 words each (see RowBox)
+  uint64_t m7, mb;       // bit 7 / all bits of each used class byte
   uint16_t *stacks;  // per warp slot: levels 1..half, maxrows entries each
   int maxrows;
   const uint8_t *outer2, *outer3;
@@ -181,22 +182,31 @@ __device__ __forceinline__ int next_quad(const AbParams &P, int d, int k, unsign
   return 8;
 }
 
-__device__ __forceinline__ bool row_box(const int8_t *row, const Uni &u, const AbParams &P) {
-  for (int c = 0; c < 6; c++) {
-    if (c >= P.m) break;
-    int rem = P.tic[c] - fld(u.plc, c);
-    int dk = row[c] - fld(u.pa, c), dr = row[8 + c] - fld(u.pb, c);
-    if (dk < -rem || dk > rem || dr < -rem || dr > rem) return false;
-  }
-  return true;
-}
+// An allowed row (k, r) as four words of biased class bytes: k+64, 64-k, r+64, 64-r. A level's
+// box test |k_c - pa_c| <= rem_c, |r_c - pb_c| <= rem_c (wz_match.cpp:1055-1075) then reads
+// k_c - pa_c + rem_c + 128 >= 128 and pa_c - k_c + rem_c + 128 >= 128 (and the same for r) off
+// bit 7 of four byte-wise sums: every byte stays in [84, 194], so no carry crosses a class.
+struct RowBox { uint64_t k1, k2, r1, r2; };
 
-__device__ __forceinline__ bool row_exact(const int8_t *row, const Uni &u, const AbParams &P) {
+__device__ __forceinline__ RowBox row_box_of(const Uni &u, const AbParams &P) {
+  RowBox b = {0, 0, 0, 0};
   for (int c = 0; c < 6; c++) {
     if (c >= P.m) break;
-    if (row[c] != fld(u.pa, c) || row[8 + c] != fld(u.pb, c)) return false;
+    const int rem = P.tic[c] - fld(u.plc, c), pa = fld(u.pa, c), pb = fld(u.pb, c);
+    b.k1 |= (uint64_t)(rem - pa + 64) << (8 * c);
+    b.k2 |= (uint64_t)(rem + pa + 64) << (8 * c);
+    b.r1 |= (uint64_t)(rem - pb + 64) << (8 * c);
+    b.r2 |= (uint64_t)(rem + pb + 64) << (8 * c);
   }
-  return true;
+  return b;
+}
+__device__ __forceinline__ bool row_box(const uint64_t *row, const RowBox &b, const AbParams &P) {
+  const uint64_t t = (row[0] + b.k1) & (row[1] + b.k2) & (row[2] + b.r1) & (row[3] + b.r2);
+  return (t & P.m7) == P.m7;
+}
+// the leaf test of a row: its class sums equal the placed ones (pa, pb hold sum + 64)
+__device__ __forceinline__ bool row_exact(const uint64_t *row, const Uni &u, const AbParams &P) {
+  return ((row[0] ^ u.pa) & P.mb) == 0 && ((row[2] ^ u.pb) & P.mb) == 0;
 }
 
 __global__ void __launch_bounds__(32 * AB_WARPS) ab_kernel(AbParams P) {
@@ -220,7 +230,7 @@ __global__ void __launch_bounds__(32 * AB_WARPS) ab_kernel(AbParams P) {
       continue;
     }
     const AbCandDev cd = P.cands[idx];
-    const int8_t *rows = cd.nrows > 0 ? P.rows + 16 * cd.row_off : nullptr;
+    const uint64_t *rows = cd.nrows > 0 ? P.roww + 4 * (size_t)cd.row_off : nullptr;
     // targets -N_CD(s) and the prefilter of wz_match.cpp:1300-1308
     Lanes v;
     v.s0 = (lane + 1 <= n) ? lane + 1 : 0;
@@ -279,7 +289,7 @@ __global__ void __launch_bounds__(32 * AB_WARPS) ab_kernel(AbParams P) {
             bool any = false;
             for (int base = 0; base < cnt && !any; base += 32) {
               int t = base + lane;
-              bool hit = t < cnt && row_exact(rows + 16 * (size_t)lst[t], u, P);
+              bool hit = t < cnt && row_exact(rows + 4 * (size_t)lst[t], u, P);
               any = __any_sync(FULL_MASK, hit);
             }
             if (!any) return false;
@@ -364,6 +374,7 @@ __global__ void __launch_bounds__(32 * AB_WARPS) ab_kernel(AbParams P) {
         const int srclen = (d == 0) ? cd.nrows : len[d];
         const uint16_t *src = stk + (size_t)(d - 1) * P.maxrows;
         uint16_t *dst = stk + (size_t)d * P.maxrows;
+        const RowBox box = row_box_of(u, P);
         int cnt = 0;
         for (int base = 0; base < srclen; base += 32) {
           int t = base + lane;
@@ -371,7 +382,7 @@ __global__ void __launch_bounds__(32 * AB_WARPS) ab_kernel(AbParams P) {
           bool ok = false;
           if (t < srclen) {
             ri = (d == 0) ? t : src[t];
-            ok = row_box(rows + 16 * (size_t)ri, u, P);
+            ok = row_box(rows + 4 * (size_t)ri, box, P);
           }
           unsigned ball = __ballot_sync(FULL_MASK, ok);
           if (ok) dst[cnt + __popc(ball & ((1u << lane) - 1u))] = (uint16_t)ri;
@@ -498,7 +509,7 @@ struct OuterTables {
 struct AbBufs {
   uint8_t *outer = nullptr;  // o2 then o3
   AbCandDev *cands = nullptr; long long cand_cap = 0;
-  int8_t *rows = nullptr; long long rows_cap = 0;
+  uint64_t *rows = nullptr; long long rows_cap = 0;  // 4 words per row
   uint16_t *stacks = nullptr; long long stack_cap = 0;
   int32_t *verdict = nullptr; long long v_cap = 0;
   long long *nodes = nullptr; long long n_cap = 0;
@@ -571,13 +582,26 @@ extern "C" int bs_complete_ab_batch(bs_ctx *ctx, const bs_ab_cand *cands, long l
   if (!rc) rc = bs_ensure_dev((void **)&Bf->verdict, &Bf->v_cap, ncand, sizeof(int32_t));
   if (!rc) rc = bs_ensure_dev((void **)&Bf->nodes, &Bf->n_cap, ncand, sizeof(long long));
   if (!rc) rc = bs_ensure_dev((void **)&Bf->ab, &Bf->ab_cap, 2 * ncand, sizeof(uint64_t));
-  if (!rc && nrows_total > 0) rc = bs_ensure_dev((void **)&Bf->rows, &Bf->rows_cap, nrows_total * 16, 1);
+  if (!rc && nrows_total > 0)
+    rc = bs_ensure_dev((void **)&Bf->rows, &Bf->rows_cap, nrows_total * 4, sizeof(uint64_t));
   if (!rc) rc = bs_ensure_dev((void **)&Bf->stacks, &Bf->stack_cap, slots * half * (long long)maxrows,
                               sizeof(uint16_t));
   if (rc) return rc;
   CK(cudaMemcpyAsync(Bf->cands, hc.data(), sizeof(AbCandDev) * ncand, cudaMemcpyHostToDevice, s));
-  if (nrows_total > 0)
-    CK(cudaMemcpyAsync(Bf->rows, rows, (size_t)nrows_total * 16, cudaMemcpyHostToDevice, s));
+  std::vector<uint64_t> roww;
+  if (nrows_total > 0) {
+    // each row (k[8], r[8], int8) as four words of biased class bytes: k+64, 64-k, r+64, 64-r
+    roww.assign(4 * (size_t)nrows_total, 0);
+    for (long long r = 0; r < nrows_total; r++)
+      for (int c = 0; c < opt->m; c++) {
+        const int k = rows[16 * r + c], q = rows[16 * r + 8 + c];
+        roww[4 * r + 0] |= (uint64_t)(k + 64) << (8 * c);
+        roww[4 * r + 1] |= (uint64_t)(64 - k) << (8 * c);
+        roww[4 * r + 2] |= (uint64_t)(q + 64) << (8 * c);
+        roww[4 * r + 3] |= (uint64_t)(64 - q) << (8 * c);
+      }
+    CK(cudaMemcpyAsync(Bf->rows, roww.data(), sizeof(uint64_t) * 4 * nrows_total, cudaMemcpyHostToDevice, s));
+  }
   CK(cudaMemsetAsync(Bf->next, 0, sizeof(unsigned long long), s));
   const long long big = 1LL << 62;
   CK(cudaMemcpyAsync(Bf->hit_min, &big, sizeof big, cudaMemcpyHostToDevice, s));
@@ -590,7 +614,9 @@ extern "C" int bs_complete_ab_batch(bs_ctx *ctx, const bs_ab_cand *cands, long l
   P.budget = opt->budget;
   P.max_cycles = opt->max_seconds > 0 ? (long long)(opt->max_seconds * 2.0e9) : 0;
   P.cands = Bf->cands; P.ncand = ncand;
-  P.rows = Bf->rows; P.stacks = Bf->stacks; P.maxrows = maxrows;
+  P.roww = Bf->rows; P.stacks = Bf->stacks; P.maxrows = maxrows;
+  P.m7 = 0; P.mb = 0;
+  for (int c = 0; c < opt->m; c++) { P.m7 |= 0x80ULL << (8 * c); P.mb |= 0xFFULL << (8 * c); }
   P.outer2 = Bf->outer; P.outer3 = Bf->outer + sizeof T.o2;
   P.next = Bf->next; P.hit_min = Bf->hit_min;
   P.verdict = Bf->verdict; P.nodes_out = Bf->nodes; P.ab_out = Bf->ab;

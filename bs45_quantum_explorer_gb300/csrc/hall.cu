@@ -422,7 +422,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1) hall_tc_kernel(TcParams P) {
         if (dump)
           for (int k = 0; k < 64; k++) { dump[k] = v[k]; dump[BS_TC_IM0 + k] = v[64 + k]; }
       }
-      {  // angles 64..103 (101..103 are zero padding)
+      // A pair whose max PSD over the first 64 angles already reaches reject_above is rejected
+      // whatever the other angles hold (the max only grows). When that holds for all 16 pairs
+      // of the warp, the second round is skipped (most leaves of a stream end here).
+      const float m64 = fmaxf(fmaxf(mx, mx1), __shfl_xor_sync(FULL_MASK, fmaxf(mx, mx1), 1));
+      if (!dump && __all_sync(FULL_MASK, m64 >= P.reject_above)) {
+        mx = m64;
+        mx1 = m64;
+      } else {  // angles 64..103 (101..103 are zero padding)
         float v[80];
         tmem_ld_32_8_32_8(t0 + 64, t0 + 96, t0 + BS_TC_IM0 + 64, t0 + BS_TC_IM0 + 96, v);
 #pragma unroll

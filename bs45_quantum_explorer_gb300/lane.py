@@ -72,12 +72,14 @@ def run_lane(ctx, n, sig, skip=0, end=0, shard=0, nshard=1, budget=200000, buf_c
              drain_top=0, drain_batches=1, endpos=False, orbit_canon=True, orbit_q=1, qprune=True,
              prof_order=3, m6=None, thm211b=None, thm212=None, abp_cap=20000, outer_k=3,
              early=True, canon=True, rev=False, hall_mode="tc_fp16", chunk=65536,
-             max_seconds=0.0, listing=None):
+             max_seconds=0.0, listing=None, batch_cells=None):
     """Runs the lane over raw cells [skip, end) of its shard (end = 0: to the list's end).
     The list options are the lane's WZ_FH_* list settings (cells.cell_list); the cells must
     be mod-6 cells (the lane's buffered order). max_seconds > 0 stops between cells once
     exceeded (the result then says found=False and its counts cover the cells done).
-    listing: a cell_list() result to reuse."""
+    listing: a cell_list() result to reuse. batch_cells: cells streamed per device call
+    (default 32 up to n = 30, where cells are small, else 1); a batch is streamed whole and
+    each cell cut to its front-only prefix on the host, which is the same prefix."""
     cells, kept, _, m = listing if listing is not None else lane_list(
         n, sig, m6, thm211b, thm212, endpos, orbit_canon, orbit_q, qprune, prof_order)
     if m != 6:
@@ -91,6 +93,29 @@ def run_lane(ctx, n, sig, skip=0, end=0, shard=0, nshard=1, budget=200000, buf_c
     # allowed A,B rows of every owned kept cell (the reference's abpMap), one host call
     rows, row_off, nrows = ab_rows(n, sig, m, [cells[pi] for pi in live]) if live else (None, [], [])
     slot = {pi: j for j, pi in enumerate(live)}
+    if batch_cells is None:
+        batch_cells = 32 if n <= 30 else 1
+    cut = drain_batches * buf_cap if drain_top > 0 else 0
+    streamed = {}  # raw cell -> (survivors in stream order, stats), filled a batch at a time
+
+    def stream_from(j0):
+        """Streams the live cells live[j0:] with allowed rows, batch_cells at a time."""
+        group = [pi for pi in live[j0:] if int(nrows[slot[pi]]) > 0][:batch_cells]
+        args = [(list(cells[q].tx[:m]), list(cells[q].ty[:m])) for q in group]
+        pins = [(cells[q].pinX, cells[q].pinY) for q in group]
+        t0 = time.perf_counter()
+        surv, cidx, st = cd_stream(ctx, args, m=m, pins=pins, rev=rev, endpos=endpos,
+                                   hall_mode=hall_mode, as_words=True,
+                                   limit=cut if len(group) == 1 else 0)
+        res.stream_s += time.perf_counter() - t0
+        if len(group) == 1:
+            streamed[group[0]] = (surv, st[0])
+            return
+        bounds = np.searchsorted(cidx, np.arange(len(group) + 1))
+        for k, q in enumerate(group):
+            w = surv[int(bounds[k]):int(bounds[k + 1])]
+            streamed[q] = (w[:cut] if cut else w, st[k])
+
     cand = 0
     for pi in owned:
         if max_seconds > 0 and time.perf_counter() - t_start > max_seconds:
@@ -107,14 +132,10 @@ def run_lane(ctx, n, sig, skip=0, end=0, shard=0, nshard=1, budget=200000, buf_c
         cell_rows = rows[row_off[j]:row_off[j] + nr] if nr <= abp_cap else None
         if cell_rows is None:
             res.cells_prof_uncap += 1
-        c = cells[pi]
-        t0 = time.perf_counter()
-        surv, _, st = cd_stream(ctx, [(list(c.tx[:m]), list(c.ty[:m]))], m=m,
-                                pins=[(c.pinX, c.pinY)], rev=rev, endpos=endpos,
-                                hall_mode=hall_mode, as_words=True,
-                                limit=drain_batches * buf_cap if drain_top > 0 else 0)
-        res.stream_s += time.perf_counter() - t0
-        res.dfs_nodes += st[0]["nodes"]
+        if pi not in streamed:
+            stream_from(j)
+        surv, st0 = streamed.pop(pi)
+        res.dfs_nodes += st0["nodes"]
         nout = len(surv)
         cs_start = cand
         nb = (nout + buf_cap - 1) // buf_cap
@@ -130,9 +151,8 @@ def run_lane(ctx, n, sig, skip=0, end=0, shard=0, nshard=1, budget=200000, buf_c
                 idx = lo + order[c0:c0 + chunk]
                 t1 = time.perf_counter()
                 ctx.timing(True)
-                v, nd, A, B = complete_ab(ctx, surv[idx], budget,
-                                          rows_per_cand=None if cell_rows is None else [cell_rows] * len(idx),
-                                          m=m, outer_k=outer_k, early=early, canon=canon,
+                v, nd, A, B = complete_ab(ctx, surv[idx], budget, rows=cell_rows, m=m,
+                                          outer_k=outer_k, early=early, canon=canon,
                                           first_hit=True)
                 ms, _, _ = ctx.timing_read()
                 ctx.timing(False)

@@ -26,7 +26,7 @@ def make_cells(cells, m, pins=None):
 
 def cd_stream(ctx, cells, m=6, pins=None, rev=False, endpos=False, hall_mode="tc_fp16",
               target_prefixes=0, leaf_chunk=0, survivor_cap=0, cap=None, as_words=False,
-              ab_side=False, limit=0):
+              ab_side=False, limit=0, round_us=0):
     """cells: list of (tx, ty). Returns (survivors, cell index per survivor, per-cell stats).
 
     survivors: int8 [k, 2, L] (or uint64 words [k, 2] with as_words) in stream order, L = n
@@ -39,7 +39,7 @@ def cd_stream(ctx, cells, m=6, pins=None, rev=False, endpos=False, hall_mode="tc
     opt = StreamOpts(m=m, rev=int(rev), endpos=int(endpos), cd_prune=0,
                      hall_mode=MODES[hall_mode], ab_side=int(ab_side),
                      target_prefixes=target_prefixes, leaf_chunk=leaf_chunk,
-                     survivor_cap=survivor_cap, limit=limit)
+                     survivor_cap=survivor_cap, limit=limit, round_us=round_us)
     stats = (CellStats * ncells)()
     nout = C.c_longlong(0)
     cap = cap if cap is not None else (min(1 << 20, limit) if limit > 0 else 1 << 20)

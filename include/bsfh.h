@@ -138,6 +138,9 @@ typedef struct {
                                 front-only cut (BUF_CAP x DRAIN_BATCHES survivors per cell,
                                 wz_match.cpp:2656-2714, 2782-2790), which stops the
                                 reference's DFS; the stats then cover the part explored */
+  long long round_us;        /* longest device launch in microseconds (0 = 25,000); walks still
+                                running then suspend, and when few remain the host splits them
+                                into their remaining subtrees (small values exercise that path) */
 } bs_stream_opts;
 
 typedef struct { long long nodes, leaves, ok; } bs_cell_stats;

@@ -89,7 +89,10 @@ def test_stream_resume_and_split_invariance(gpu, oracle):
     cells = [(x, y) for x in _cells(n, sig[2], 6) for y in _cells(n, sig[3], 6)][:200]
     pins = [(0, 0)] * len(cells)
     for kw in (dict(leaf_chunk=64), dict(leaf_chunk=1000, target_prefixes=16),
-               dict(target_prefixes=1 << 20), dict(hall_mode="fp64"), dict(hall_mode="tc_bf16x2")):
+               dict(target_prefixes=1 << 20), dict(hall_mode="fp64"), dict(hall_mode="tc_bf16x2"),
+               # 1 us launches: every walk suspends after 256 steps, so the rounds, the
+               # resumption and the host's splitting of walks all run many times
+               dict(round_us=1), dict(round_us=1, leaf_chunk=64, target_prefixes=16)):
         _compare(ctx, oracle, n, cells, 6, pins, 0, 0, **kw)
 
 
@@ -103,7 +106,14 @@ def test_stream_larger_n(gpu, oracle, n):
     # cells whose class sums are small have the largest streams
     cells.sort(key=lambda c: sum(abs(v) for v in c[0]) + sum(abs(v) for v in c[1]))
     pick = [cells[i] for i in rng.integers(0, min(len(cells), 400), 3)]
-    _compare(ctx, oracle, n, pick, 6, [(0, 0)] * 3, 0, 0)
+    from bs45_quantum_explorer_gb300.stream import cd_stream
+    ref, ridx, rst = _oracle_batch(oracle, n, pick, 6, [(0, 0)] * 3, 0, 0)
+    # default launches, then short ones that force suspension and splitting inside these
+    # large subtrees
+    for kw in (dict(), dict(round_us=300)):
+        got, gidx, gst = cd_stream(ctx, pick, m=6, pins=[(0, 0)] * 3, **kw)
+        assert got.shape == ref.shape and (got == ref).all() and (gidx == ridx).all(), kw
+        assert gst == rst, kw
 
 
 def test_stream_golden_reference(gpu):
@@ -146,8 +156,9 @@ def test_stream_limit_returns_the_stream_prefix(gpu, oracle):
     ref, ridx, _ = _oracle_batch(oracle, n, cells, 6, pins, 0, 0)
     total = len(ref)
     assert total > 200
-    for L in (1, 5, 100, total // 2, total - 1, total, total + 3):
-        got, gidx, _ = cd_stream(ctx, cells, m=6, pins=pins, limit=L)
+    for L, rus in ((1, 0), (5, 0), (100, 0), (total // 2, 0), (total // 2, 1), (total - 1, 0),
+                   (total, 0), (total + 3, 0)):
+        got, gidx, _ = cd_stream(ctx, cells, m=6, pins=pins, limit=L, round_us=rus)
         k = min(L, total)
         assert got.shape[0] == k, (L, got.shape)
         assert (got == ref[:k]).all() and (gidx == ridx[:k]).all(), L
