@@ -26,6 +26,7 @@ class BsError(RuntimeError):
 
 class HallStats(C.Structure):
     _fields_ = [("pairs", C.c_longlong), ("passed", C.c_longlong), ("rechecked", C.c_longlong),
+                ("fp64_rechecked", C.c_longlong),
                 ("pass_below", C.c_double), ("reject_above", C.c_double),
                 ("quant_err", C.c_double), ("mode", C.c_int)]
 

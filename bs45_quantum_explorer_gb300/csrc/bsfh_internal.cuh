@@ -25,6 +25,16 @@ struct bs_hall_tc_form {
   uint8_t *d_image;      // nparts * BS_TC_PART_BYTES
 };
 
+// The Hall tables in fixed point for the margin band's second test: T = round(t * 2^30) for
+// the 101 unique angles, [cos 101 x L][sin 101 x L][row sums cos 101][row sums sin 101] int64,
+// with the certified thresholds of that form (see hall.cu).
+#define BS_FIX_WORDS (2 * BS_TC_NANG * BS_MAXL + 2 * BS_TC_NANG)
+struct bs_hall_fix_form {
+  double err;           // per-sequence bound on |Re - Re_fix|, |Im - Im_fix|
+  double pass_below, reject_above;
+  int64_t *d_tab;       // BS_FIX_WORDS, laid out for length L
+};
+
 struct bs_ctx {
   int n, n1, sig[4], device;
   int num_sms;
@@ -33,13 +43,16 @@ struct bs_ctx {
   double lim;                // 4n + 2 + 0.5
   bs_hall_tc_form tc[3];     // index by mode (0 unused), sequences of length n (C,D)
   bs_hall_tc_form tc_ab[3];  // the same for length n+1 (A,B)
+  bs_hall_fix_form fix[2];   // fixed-point band test, lengths n (0) and n+1 (1)
   int *d_status;             // device-side error word
-  unsigned long long *d_count;  // [0] uncertain count, [1] pass count, [2] overflow flag
+  unsigned long long *d_count;  // [0] band count, [1] pass count, [2] overflow flag,
+                                // [3] pairs left for the FP64 test
   // scratch for the host-buffer entry points
   uint64_t *d_bits; long long bits_cap;   // pairs
   uint8_t *d_pass; long long pass_cap;
   int8_t *d_rows; long long rows_cap;     // int8 staging for packing
-  unsigned *d_unc; long long unc_cap;     // uncertain pair indices
+  unsigned *d_unc; long long unc_cap;     // band pair indices
+  unsigned *d_unc2; long long unc2_cap;   // pairs the fixed-point test leaves undecided
   void *h_pinned; size_t pinned_bytes;
   // kernel timing (bs_ctx_timing): start/stop events around the timed kernel class
   int timing;

@@ -3,7 +3,9 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <algorithm>
 #include <cmath>
+#include <vector>
 
 #include "bsfh_internal.cuh"
 
@@ -158,6 +160,48 @@ static int build_tc_form(bs_ctx *ctx, const double *ct, const double *st, int mo
   return BS_OK;
 }
 
+// The fixed-point Hall form for sequences of length L: every table entry of the 101 unique
+// angles as T = round(t * 2^30) (|T| <= 2^30), so a sequence's Re and Im are exact int64 sums
+// and their error against the FP64 table is at most e1 = max over angles of sum |t - T/2^30|.
+// The pair PSD F' is formed from them in FP64 with relative error below 2^-48 (kappa2); the
+// same argument as the tensor-core form then certifies its thresholds.
+static int build_fix_form(bs_ctx *ctx, const double *ct, const double *st, int L, bs_hall_fix_form &F) {
+  std::vector<int64_t> tab(BS_FIX_WORDS, 0);
+  int64_t *tc = tab.data(), *ts = tc + BS_TC_NANG * L, *sc = tc + 2 * BS_TC_NANG * L, *ss = sc + BS_TC_NANG;
+  double e = 0.0;
+  for (int u = 0; u < BS_TC_NANG; u++) {
+    const int j = angle_of(u);
+    double ec = 0.0, es = 0.0;
+    for (int i = 0; i < L; i++) {
+      const double c = ct[(size_t)j * ctx->n1 + i], s = st[(size_t)j * ctx->n1 + i];
+      const int64_t qc = llrint(ldexp(c, 30)), qs = llrint(ldexp(s, 30));
+      tc[u * L + i] = qc;
+      ts[u * L + i] = qs;
+      sc[u] += qc;
+      ss[u] += qs;
+      ec += fabs(c - ldexp((double)qc, -30));
+      es += fabs(s - ldexp((double)qs, -30));
+    }
+    e = std::max(e, std::max(ec, es));
+  }
+  e = e * (1.0 + 1e-9) + 1e-15;
+  const double eps64 = 1e-9, kappa2 = 1.0 + ldexp(1.0, -48);
+  double pb = sqrt(ctx->lim - eps64) - 2.0 * e;
+  pb = pb * pb / kappa2;
+  double ra = 2.0 * e + sqrt(ctx->lim + 8.0 * e * e + eps64);
+  ra = ra * ra * kappa2;
+  F.err = e;
+  F.pass_below = nextafter(pb, 0.0);
+  F.reject_above = nextafter(ra, 1e300);
+  cudaError_t ce = cudaSuccess;
+  if (!F.d_tab) ce = cudaMalloc(&F.d_tab, sizeof(int64_t) * BS_FIX_WORDS);
+  if (ce == cudaSuccess)
+    ce = cudaMemcpyAsync(F.d_tab, tab.data(), sizeof(int64_t) * BS_FIX_WORDS, cudaMemcpyHostToDevice, ctx->stream);
+  if (ce == cudaSuccess) ce = cudaStreamSynchronize(ctx->stream);
+  if (ce != cudaSuccess) return bs_cuda_fail(ce);
+  return BS_OK;
+}
+
 // Loads the tables of BS(n+1,n) into a context whose stream and buffers exist: host tables
 // exactly as init_hall_tables builds them (wz_match.cpp:106-114), their FP64 copies and the
 // tensor-core images for both sequence lengths (C,D: n; A,B: n+1).
@@ -192,6 +236,8 @@ static int load_tables(bs_ctx *ctx, int n, int a, int b, int c, int d) {
   if (rc == BS_OK) rc = build_tc_form(ctx, ct, st, BS_HALL_TC_FP16, n + 1, ctx->tc_ab[BS_HALL_TC_FP16]);
   if (rc == BS_OK)
     rc = build_tc_form(ctx, ct, st, BS_HALL_TC_BF16X2, n + 1, ctx->tc_ab[BS_HALL_TC_BF16X2]);
+  if (rc == BS_OK) rc = build_fix_form(ctx, ct, st, n, ctx->fix[0]);
+  if (rc == BS_OK) rc = build_fix_form(ctx, ct, st, n + 1, ctx->fix[1]);
   free(ct); free(st); free(gc); free(gs);
   return rc;
 }
@@ -248,8 +294,10 @@ extern "C" void bs_ctx_destroy(bs_ctx *ctx) {
     cudaFree(ctx->tc[m].d_image);
     cudaFree(ctx->tc_ab[m].d_image);
   }
+  cudaFree(ctx->fix[0].d_tab); cudaFree(ctx->fix[1].d_tab);
   cudaFree(ctx->d_status); cudaFree(ctx->d_count);
   cudaFree(ctx->d_bits); cudaFree(ctx->d_pass); cudaFree(ctx->d_rows); cudaFree(ctx->d_unc);
+  cudaFree(ctx->d_unc2);
   bs_stream_free(ctx);
   bs_ab_free(ctx);
   if (ctx->h_pinned) cudaFreeHost(ctx->h_pinned);

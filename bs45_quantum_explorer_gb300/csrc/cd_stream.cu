@@ -514,6 +514,34 @@ static int ensure_store(uint64_t **words, uint64_t **keys, uint32_t **cellv, lon
   return BS_OK;
 }
 
+// Stream order of a wave's survivors: by (cell, path key hi, path key lo), as a stable LSD
+// radix sort over the bytes that vary (a leaf's path occupies only the top 4 x half bits, so
+// most bytes of the low key word, and of the cell index, are skipped).
+static void stream_order(const std::vector<uint64_t> &keys, const std::vector<uint32_t> &cellv, size_t n,
+                         std::vector<uint32_t> &order) {
+  order.resize(n);
+  for (size_t i = 0; i < n; i++) order[i] = (uint32_t)i;
+  std::vector<uint32_t> tmp(n);
+  size_t cnt[256];
+  auto pass = [&](auto byte_of) {
+    memset(cnt, 0, sizeof cnt);
+    for (size_t i = 0; i < n; i++) cnt[byte_of(order[i])]++;
+    for (int b = 0; b < 256; b++)
+      if (cnt[b] == n) return;  // one value: this byte orders nothing
+    size_t run = 0;
+    for (int b = 0; b < 256; b++) {
+      const size_t c = cnt[b];
+      cnt[b] = run;
+      run += c;
+    }
+    for (size_t i = 0; i < n; i++) tmp[cnt[byte_of(order[i])]++] = order[i];
+    order.swap(tmp);
+  };
+  for (int b = 0; b < 8; b++) pass([&](uint32_t i) { return (unsigned)((keys[2 * i + 1] >> (8 * b)) & 255); });
+  for (int b = 0; b < 8; b++) pass([&](uint32_t i) { return (unsigned)((keys[2 * i] >> (8 * b)) & 255); });
+  for (int b = 0; b < 4; b++) pass([&](uint32_t i) { return (unsigned)((cellv[i] >> (8 * b)) & 255); });
+}
+
 extern "C" int bs_cd_stream(bs_ctx *ctx, const bs_cell *cells, int ncells, const bs_stream_opts *opt,
                             uint64_t *out_words, uint32_t *out_cell, long long out_cap,
                             long long *nout, bs_cell_stats *stats) {
@@ -748,7 +776,7 @@ extern "C" int bs_cd_stream(bs_ctx *ctx, const bs_cell *cells, int ncells, const
   std::vector<uint32_t> wcell;
   std::vector<unsigned long long> cs_prev(3 * (size_t)ncells, 0), cs(3 * (size_t)ncells, 0);
   // the first wave is a probe: small under `limit` (a few coarse prefixes can hold far more
-  // survivors than asked for), wider otherwise; later waves grow at most 4x at a time
+  // survivors than asked for; later waves then grow at most 4x at a time), wider otherwise
   long long pos = 0, wave_width = std::min<long long>(ncoarse, limit ? 8 : 256);
   int k_refine = (half - deepest >= 6) ? 2 : 0;
   long long have = 0;
@@ -864,13 +892,8 @@ extern "C" int bs_cd_stream(bs_ctx *ctx, const bs_cell *cells, int ncells, const
       CK(cudaMemcpyAsync(wwords.data(), B->surv_words, sizeof(uint64_t) * 2 * nsurv, cudaMemcpyDeviceToHost, s));
       CK(cudaMemcpyAsync(wcell.data(), B->surv_cell, sizeof(uint32_t) * nsurv, cudaMemcpyDeviceToHost, s));
       CK(cudaStreamSynchronize(s));
-      std::vector<uint32_t> order(nsurv);
-      for (uint32_t i = 0; i < (uint32_t)nsurv; i++) order[i] = i;
-      std::sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) {
-        if (wcell[a] != wcell[b]) return wcell[a] < wcell[b];
-        if (wkeys[2 * a] != wkeys[2 * b]) return wkeys[2 * a] < wkeys[2 * b];
-        return wkeys[2 * a + 1] < wkeys[2 * b + 1];
-      });
+      std::vector<uint32_t> order;
+      stream_order(wkeys, wcell, (size_t)nsurv, order);
       long long keep = (long long)nsurv;
       if (limit) keep = std::min(keep, limit - have);
       for (long long i = 0; i < keep; i++) {
@@ -893,7 +916,7 @@ extern "C" int bs_cd_stream(bs_ctx *ctx, const bs_cell *cells, int ncells, const
     double width = std::max(WAVE_NODES, rate * 0.25) / per_coarse;
     // enough fine prefixes for every walker, twice over
     width = std::max(width, 2.0 * (double)walkers / std::pow(8.0, k_refine));
-    width = std::min(width, 4.0 * (double)take);
+    if (limit) width = std::min(width, 4.0 * (double)take);  // approach the limit gradually
     if (limit && nsurv > 0) {
       const double per_coarse_surv = (double)nsurv / (double)take;
       width = std::min(width, std::max(8.0, 1.5 * (double)(limit - have) / per_coarse_surv));

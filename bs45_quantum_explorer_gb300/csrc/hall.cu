@@ -141,6 +141,72 @@ __global__ void __launch_bounds__(256) hall_fp64_recheck_kernel(
   if (lane == 0 && local) atomicAdd(pass_count, (unsigned long long)local);
 }
 
+// Second test of the margin band, exact up to a tiny certified error: a warp per listed pair,
+// the 101 unique angles over the lanes. Re and Im of each sequence are int64 sums of the
+// fixed-point table T = round(t * 2^30): Re = 2 * (sum of T over the +1 positions) - (row sum).
+// The pair PSD is formed in FP64 from those exact integers and its maximum over the angles is
+// compared with the form's certified thresholds; a pair between them goes on to the FP64 test.
+__global__ void __launch_bounds__(256) hall_fix_band_kernel(
+    const uint64_t *__restrict__ bits, const unsigned *__restrict__ list,
+    const unsigned long long *list_len, unsigned long long list_cap, int L,
+    const int64_t *__restrict__ tab, double pass_below, double reject_above,
+    uint8_t *__restrict__ pass, unsigned long long *pass_count, unsigned *__restrict__ list2,
+    unsigned long long *list2_len, unsigned long long list2_cap) {
+  extern __shared__ int64_t ftab[];
+  const int nt = 2 * BS_TC_NANG * L + 2 * BS_TC_NANG;
+  for (int i = threadIdx.x; i < nt; i += blockDim.x) {
+    // the device table is laid out for its length L: [cos][sin][sums]
+    ftab[i] = tab[i];
+  }
+  __syncthreads();
+  const int64_t *tc = ftab, *ts = ftab + BS_TC_NANG * L;
+  const int64_t *sc = ftab + 2 * BS_TC_NANG * L, *ss = sc + BS_TC_NANG;
+  const unsigned long long n = *list_len;
+  const long long count = (long long)(n < list_cap ? n : list_cap);
+  const int lane = threadIdx.x & 31;
+  const long long w0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+  unsigned local = 0;
+  for (long long t = w0; t < count; t += nw) {
+    const long long p = (long long)list[t];
+    const uint64_t x = bits[2 * p], y = bits[2 * p + 1];
+    double mx = 0.0;
+    for (int u = lane; u < BS_TC_NANG; u += 32) {
+      const int64_t *cr = tc + u * L, *sr = ts + u * L;
+      int64_t rx = 0, ix = 0, ry = 0, iy = 0;
+      for (uint64_t b = x; b; b &= b - 1) {
+        const int i = __ffsll((long long)b) - 1;
+        rx += cr[i];
+        ix += sr[i];
+      }
+      for (uint64_t b = y; b; b &= b - 1) {
+        const int i = __ffsll((long long)b) - 1;
+        ry += cr[i];
+        iy += sr[i];
+      }
+      rx = 2 * rx - sc[u];
+      ix = 2 * ix - ss[u];
+      ry = 2 * ry - sc[u];
+      iy = 2 * iy - ss[u];
+      const double a = (double)rx, b2 = (double)ix, c = (double)ry, d = (double)iy;
+      const double f = __dadd_rn(__dadd_rn(__dmul_rn(a, a), __dmul_rn(b2, b2)),
+                                 __dadd_rn(__dmul_rn(c, c), __dmul_rn(d, d))) * 0x1p-60;
+      mx = fmax(mx, f);
+    }
+    for (int o = 16; o; o >>= 1) mx = fmax(mx, __shfl_xor_sync(FULL_MASK, mx, o));
+    if (lane == 0) {
+      if (mx <= pass_below) {
+        pass[p] = 1;
+        local++;
+      } else if (mx < reject_above) {
+        const unsigned long long k = atomicAdd(list2_len, 1ULL);
+        if (k < list2_cap) list2[k] = (unsigned)p;
+      }  // else rejected: the tensor-core kernel already wrote 0
+    }
+  }
+  if (lane == 0 && local) atomicAdd(pass_count, (unsigned long long)local);
+}
+
 __global__ void pack_kernel(const int8_t *__restrict__ rows, long long nrows, int L,
                             uint64_t *__restrict__ words, int *status) {
   for (long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x; r < nrows;
@@ -553,6 +619,26 @@ static int launch_tc(bs_ctx *ctx, int mode, const uint64_t *d_bits, long long np
   return BS_OK;
 }
 
+// The band's fixed-point test: from the tensor-core list (d_unc, d_count[0]) to the FP64
+// list (d_unc2, d_count[3]).
+static int launch_fix(bs_ctx *ctx, const uint64_t *d_bits, uint8_t *d_pass, int L) {
+  const bs_hall_fix_form &F = ctx->fix[L == ctx->n ? 0 : 1];
+  static bool attr_done = false;
+  if (!attr_done) {
+    CK(cudaFuncSetAttribute(hall_fix_band_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                            (int)(sizeof(int64_t) * BS_FIX_WORDS)));
+    attr_done = true;
+  }
+  const size_t smem = sizeof(int64_t) * (2 * BS_TC_NANG * L + 2 * BS_TC_NANG);
+  ctx->launches++;
+  hall_fix_band_kernel<<<ctx->num_sms, 256, smem, ctx->stream>>>(
+      d_bits, ctx->d_unc, ctx->d_count, (unsigned long long)ctx->unc_cap, L, F.d_tab,
+      F.pass_below, F.reject_above, d_pass, ctx->d_count + 1, ctx->d_unc2, ctx->d_count + 3,
+      (unsigned long long)ctx->unc2_cap);
+  CK(cudaGetLastError());
+  return BS_OK;
+}
+
 static int hall_dev(bs_ctx *ctx, const uint64_t *d_bits, long long npairs, int mode,
                     uint8_t *d_pass, bs_hall_stats *stats, float *d_dump, int L) {
   if (!ctx || (L != ctx->n && L != ctx->n1)) return BS_ERR_ARG;
@@ -567,11 +653,15 @@ static int hall_dev(bs_ctx *ctx, const uint64_t *d_bits, long long npairs, int m
       if (rc) return rc;
     } else {
       int rc = bs_ensure_dev((void **)&ctx->d_unc, &ctx->unc_cap, npairs, sizeof(unsigned));
+      if (!rc) rc = bs_ensure_dev((void **)&ctx->d_unc2, &ctx->unc2_cap, npairs, sizeof(unsigned));
       if (rc) return rc;
       rc = launch_tc(ctx, mode, d_bits, npairs, d_pass, d_dump, L);
       if (rc) return rc;
-      rc = launch_fp64(ctx, d_bits, npairs, ctx->d_unc, ctx->d_count,
-                       (unsigned long long)ctx->unc_cap, d_pass, L);
+      // the margin band: the exact fixed-point test, then FP64 for what it leaves
+      rc = launch_fix(ctx, d_bits, d_pass, L);
+      if (rc) return rc;
+      rc = launch_fp64(ctx, d_bits, npairs, ctx->d_unc2, ctx->d_count + 3,
+                       (unsigned long long)ctx->unc2_cap, d_pass, L);
       if (rc) return rc;
     }
   }
@@ -589,6 +679,7 @@ static int hall_dev(bs_ctx *ctx, const uint64_t *d_bits, long long npairs, int m
     stats->pairs = npairs;
     stats->passed = (long long)cnt[1];
     stats->rechecked = mode == BS_HALL_FP64 ? 0 : (long long)cnt[0];
+    stats->fp64_rechecked = mode == BS_HALL_FP64 ? 0 : (long long)cnt[3];
     stats->mode = mode;
     if (mode == BS_HALL_FP64) {
       stats->pass_below = ctx->lim;

@@ -41,7 +41,10 @@ typedef struct bs_ctx bs_ctx;
 typedef struct {
   long long pairs;          /* pairs tested */
   long long passed;         /* pairs accepted (== the reference's hall_ok_pair_fast count) */
-  long long rechecked;      /* pairs that fell inside the margin band and were rechecked in FP64 */
+  long long rechecked;      /* pairs inside the tensor-core margin band, decided again by the
+                               exact fixed-point test */
+  long long fp64_rechecked; /* of those, pairs within the fixed-point test's own (about 1e-6
+                               wide) band, decided in FP64 */
   double pass_below;        /* max pair PSD at or below which a pair certainly passes */
   double reject_above;      /* max pair PSD at or above which a pair certainly fails */
   double quant_err;         /* per-sequence |Re|,|Im| quantisation bound e of the table */

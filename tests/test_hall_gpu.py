@@ -129,7 +129,9 @@ def test_hall_near_threshold_parity(gpu, oracle):
     ctx = _ctx(n, (7, 11, 0, 0))
     _check_all_modes(ctx, near, ref)
     _, st = ctx.hall_filter_packed(near, "tc_fp16")
-    assert st["rechecked"] > 0  # the band is really used on these inputs
+    assert st["rechecked"] > 0  # the tensor-core band is really used on these inputs
+    # the exact fixed-point test decides nearly all of them; FP64 takes what is left
+    assert 0 <= st["fp64_rechecked"] <= st["rechecked"]
 
 
 def _quantised_tables(n, oracle, mode):
