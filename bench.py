@@ -350,6 +350,55 @@ def run_c3(max_cells=0, batch=16, topk=256):
             "algorithmic_bytes": alg, "algorithmic_gb_per_s": alg / dt / 1e9}
 
 
+def run_join(n=24):
+    """The full-space exact join (the reference's JOIN22 semantics) for one signature of
+    BS(n+1, n): every A,B pair of every mod-3 cell (length n+1) and every C,D pair of every
+    cell (length n), streamed on the GPU, then joined on AB[s] = -CD[s] with every match
+    verified by the exact NPAF. Reports the counts, the stream and join times and the join
+    probe kernel's algorithmic rate (8 B per key inserted + 8 B per probed slot)."""
+    import itertools
+    import numpy as np
+    from bs45_quantum_explorer_gb300.hall import Context
+    from bs45_quantum_explorer_gb300.stream import cd_stream, join_quads
+
+    def cells(L, total, m=6):
+        cnt = [len(range(c, L, m)) for c in range(m)]
+        out = []
+        for v in itertools.product(*[range(-k, k + 1, 2) for k in cnt[:-1]]):
+            last = total - sum(v)
+            if abs(last) <= cnt[-1] and (last + cnt[-1]) % 2 == 0:
+                out.append(list(v) + [last])
+        return out
+
+    sig = _classes(n)[0]
+    ctx = Context(n, sig)
+    # mod-3 cells: every (A,B) and every (C,D) of the signature falls in exactly one
+    ab_cells = [(x, y) for x in cells(n + 1, sig[0], 3) for y in cells(n + 1, sig[1], 3)]
+    cd_cells = [(x, y) for x in cells(n, sig[2], 3) for y in cells(n, sig[3], 3)]
+    t0 = time.perf_counter()
+    ab = np.concatenate([cd_stream(ctx, ab_cells[i:i + 512], m=3, ab_side=True, as_words=True,
+                                   cap=1 << 22)[0] for i in range(0, len(ab_cells), 512)])
+    cd = np.concatenate([cd_stream(ctx, cd_cells[i:i + 512], m=3, as_words=True, cap=1 << 22)[0]
+                         for i in range(0, len(cd_cells), 512)])
+    stream_s = time.perf_counter() - t0
+    ctx.timing(True)
+    t1 = time.perf_counter()
+    quads, hits = join_quads(ctx, cd, ab)
+    join_s = time.perf_counter() - t1
+    probe_ms, _, _ = ctx.timing_read()
+    ctx.close()
+    slots = 1024
+    while slots < 2 * len(cd):
+        slots *= 2
+    alg = 8 * len(cd) + 8 * len(ab)
+    return {"workload": f"full-space join BS({n + 1},{n}) sig={sig}: {len(ab_cells)} A,B cells and "
+                        f"{len(cd_cells)} C,D cells, all pairs passing the Thm 2.2-2.4 stream",
+            "ab_pairs": int(len(ab)), "cd_pairs": int(len(cd)), "table_slots": slots,
+            "key_matches": int(hits), "verified_quads": int(len(quads)),
+            "stream_s": stream_s, "join_s": join_s, "probe_kernel_ms": probe_ms,
+            "probe_algorithmic_gb_per_s": alg / (probe_ms * 1e-3) / 1e9 if probe_ms > 0 else None}
+
+
 def run_serving(n_jobs=12, tail=2, rate=2.0, slots=4, max_cells=64):
     """C5: a seeded Poisson stream of first-hit jobs, n uniform in 20..42 with a signature from
     classes(n) and a contiguous ORDER=3 range of 1..max_cells raw cells, plus `tail` n = 42
@@ -396,6 +445,8 @@ def main():
     ap.add_argument("--first-hit", type=float, default=None, metavar="SECONDS",
                     help="run only the n=36 first-hit lane for about SECONDS and print its line")
     ap.add_argument("--serve", action="store_true", help="run only the serving mix and print its line")
+    ap.add_argument("--join", type=int, default=None, metavar="N",
+                    help="run only the full-space join for BS(N+1, N), one signature")
     ap.add_argument("--c3", type=int, default=None, metavar="CELLS",
                     help="run only the n=30 full stream over the first CELLS kept cells (0: all)")
     ap.add_argument("--fh-drain", type=int, default=50000,
@@ -414,7 +465,7 @@ def main():
     if args.stream_only:
         run_stream_only(args)
         return
-    if args.first_hit is not None or args.serve or args.c3 is not None:
+    if args.first_hit is not None or args.serve or args.c3 is not None or args.join is not None:
         from bs45_quantum_explorer_gb300 import build_library
         build_library()
         if args.first_hit is not None:
@@ -424,6 +475,8 @@ def main():
             print(json.dumps(run_serving()), flush=True)
         if args.c3 is not None:
             print(json.dumps(run_c3(args.c3)), flush=True)
+        if args.join is not None:
+            print(json.dumps(run_join(args.join)), flush=True)
         return
 
     import numpy as np

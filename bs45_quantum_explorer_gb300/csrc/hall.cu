@@ -555,14 +555,17 @@ static int launch_fp64(bs_ctx *ctx, const uint64_t *d_bits, long long npairs,
                        const unsigned *list, const unsigned long long *list_len,
                        unsigned long long list_cap, uint8_t *d_pass, int L) {
   size_t smem = sizeof(double) * 2 * 200 * L;
-  static bool attr_done = false;
-  if (!attr_done) {
-    CK(cudaFuncSetAttribute(hall_fp64_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                            (int)(sizeof(double) * 2 * 200 * BS_MAXL)));
-    CK(cudaFuncSetAttribute(hall_fp64_recheck_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                            (int)(sizeof(double) * 2 * 200 * BS_MAXL)));
-    attr_done = true;
-  }
+  // shared-memory opt-in, once per process (a thread-safe static: serving slots call this
+  // from several host threads)
+  static const cudaError_t attr = [] {
+    cudaError_t e = cudaFuncSetAttribute(hall_fp64_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)(sizeof(double) * 2 * 200 * BS_MAXL));
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(hall_fp64_recheck_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)(sizeof(double) * 2 * 200 * BS_MAXL));
+    return e;
+  }();
+  CK(attr);
   if (list) {  // the margin band after the tensor-core kernel: a warp per pair on every SM
     ctx->launches++;
     hall_fp64_recheck_kernel<<<ctx->num_sms, 256, smem, ctx->stream>>>(
@@ -604,12 +607,9 @@ static int launch_tc(bs_ctx *ctx, int mode, const uint64_t *d_bits, long long np
   P.status = ctx->d_status;
   P.dump = d_dump;
   size_t smem = tc_smem_bytes(F.nparts);
-  static bool attr_done = false;
-  if (!attr_done) {
-    CK(cudaFuncSetAttribute(hall_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                            (int)tc_smem_bytes(2)));
-    attr_done = true;
-  }
+  static const cudaError_t attr = cudaFuncSetAttribute(
+      hall_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc_smem_bytes(2));
+  CK(attr);
   long long grid = P.ntiles < ctx->num_sms ? P.ntiles : ctx->num_sms;
   if (grid < 1) grid = 1;
   bs_timed_begin(ctx);
@@ -623,12 +623,10 @@ static int launch_tc(bs_ctx *ctx, int mode, const uint64_t *d_bits, long long np
 // list (d_unc2, d_count[3]).
 static int launch_fix(bs_ctx *ctx, const uint64_t *d_bits, uint8_t *d_pass, int L) {
   const bs_hall_fix_form &F = ctx->fix[L == ctx->n ? 0 : 1];
-  static bool attr_done = false;
-  if (!attr_done) {
-    CK(cudaFuncSetAttribute(hall_fix_band_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                            (int)(sizeof(int64_t) * BS_FIX_WORDS)));
-    attr_done = true;
-  }
+  static const cudaError_t attr = cudaFuncSetAttribute(
+      hall_fix_band_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+      (int)(sizeof(int64_t) * BS_FIX_WORDS));
+  CK(attr);
   const size_t smem = sizeof(int64_t) * (2 * BS_TC_NANG * L + 2 * BS_TC_NANG);
   ctx->launches++;
   hall_fix_band_kernel<<<ctx->num_sms, 256, smem, ctx->stream>>>(

@@ -119,8 +119,9 @@ int bs_hall_tc_dump_dev(bs_ctx *ctx, const uint64_t *d_bits, long long npairs, i
  * Thm 2.4 test, in the reference's emission order (cells in the given order, then DFS
  * order), with per-cell counts equal to the reference's CDSTAT dfs_nodes, leaves and
  * hall_ok (CELLSIZE) figures. The subtrees are explored in waves, in stream order: each
- * wave refines the next run of the cell's frontier to as many subtrees as keep the GPU
- * busy, so cells of 10^13 nodes (n = 42) stream at full speed and `limit` stops early. */
+ * wave refines the next run of the cell's frontier to as many subtrees as keep the GPU busy,
+ * and walks that run long are split further between launches, so cells of more than 10^13
+ * nodes (n = 42) stream at full speed and `limit` stops early. */
 typedef struct {
   int8_t tx[8], ty[8];  /* class-sum targets of C and D at modulus m (entries >= m unused) */
   int32_t pinX, pinY;   /* zero-sum pins: C[0] = +1 / D[0] = +1 (wz_match.cpp:1526-1527) */
@@ -133,7 +134,8 @@ typedef struct {
   int32_t cd_prune;          /* WZ_FH_CD_PRUNE: only 0 (the optional prunes are host-only) */
   int32_t hall_mode;         /* BS_HALL_* form of the leaf test */
   int32_t ab_side;           /* 1: stream the A,B side (length n+1, negative-product root quads) */
-  long long target_prefixes; /* subtrees to split the batch into (0 = 262144) */
+  long long target_prefixes; /* coarse split of the batch into subtrees (0 = 262144); the
+                                waves refine it further as the measured subtree sizes ask */
   long long leaf_chunk;      /* leaves buffered per round (0 = 2^24) */
   long long survivor_cap;    /* device survivor buffer (0 = 2^22) */
   long long limit;           /* > 0: stop once the first `limit` survivors of the batch (in
