@@ -328,6 +328,17 @@ __device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
   return d;
 }
 
+// Two PSDs re^2 + im^2 at once with the packed f32x2 multiply and FMA: f0, f1 are exactly
+// fmaf(re0, re0, im0 * im0) and fmaf(re1, re1, im1 * im1) (round to nearest per element).
+__device__ __forceinline__ void psd2(float re0, float re1, float im0, float im1, float &f0, float &f1) {
+  uint64_t re, im, r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(re) : "f"(re0), "f"(re1));
+  asm("mov.b64 %0, {%1, %2};" : "=l"(im) : "f"(im0), "f"(im1));
+  asm("mul.rn.f32x2 %0, %1, %1;" : "=l"(r) : "l"(im));
+  asm("fma.rn.f32x2 %0, %1, %1, %0;" : "+l"(r) : "l"(re));
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(f0), "=f"(f1) : "l"(r));
+}
+
 __global__ void __launch_bounds__(TC_THREADS, 1) hall_tc_kernel(TcParams P) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t *base = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -468,21 +479,22 @@ __global__ void __launch_bounds__(TC_THREADS, 1) hall_tc_kernel(TcParams P) {
       float mx = 0.0f;
       float *dump = P.dump ? P.dump + (size_t)(tile * 128 + row) * BS_TC_COLS : nullptr;
       // A pair's rows sit in adjacent lanes (C even, D odd). Each lane forms its own row's
-      // PSD at every angle; for each angle one lane adds its partner's: the even lane the
-      // first half of a load round's angles, the odd lane the second half. One shuffle then
-      // carries two angles (each lane sends the half its partner sums), and the two running
-      // maxima combine at the end. Every sum is fC + fD of the same operands as before.
+      // PSD at every angle, two adjacent angles per packed f32x2 multiply and FMA; for each
+      // angle one lane adds its partner's: the even lane the even angles, the odd lane the odd
+      // ones. One shuffle then carries two angles (each lane sends the one its partner sums),
+      // and the two running maxima combine at the end. Every value is the scalar
+      // fmaf(re, re, im * im) of the same operands, and every sum fC + fD.
       const bool odd = lane & 1;
       float mx1 = 0.0f;
       {  // angles 0..63: Re columns 0..63 and Im columns 104..167 in one load round
         float v[128];
         tmem_ld_64_64(t0, t0 + BS_TC_IM0, v);
 #pragma unroll
-        for (int k = 0; k < 32; k++) {
-          const float fa = fmaf(v[k], v[k], v[64 + k] * v[64 + k]);
-          const float fb = fmaf(v[32 + k], v[32 + k], v[96 + k] * v[96 + k]);
+        for (int k = 0; k < 64; k += 2) {  // adjacent angles k, k+1 in one packed pair
+          float fa, fb;
+          psd2(v[k], v[k + 1], v[64 + k], v[65 + k], fa, fb);
           const float got = __shfl_xor_sync(FULL_MASK, odd ? fa : fb, 1);
-          if (k & 1) mx1 = fmaxf(mx1, (odd ? fb : fa) + got);
+          if (k & 2) mx1 = fmaxf(mx1, (odd ? fb : fa) + got);
           else mx = fmaxf(mx, (odd ? fb : fa) + got);
         }
         if (dump)
@@ -499,11 +511,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1) hall_tc_kernel(TcParams P) {
         float v[80];
         tmem_ld_32_8_32_8(t0 + 64, t0 + 96, t0 + BS_TC_IM0 + 64, t0 + BS_TC_IM0 + 96, v);
 #pragma unroll
-        for (int k = 0; k < 20; k++) {
-          const float fa = fmaf(v[k], v[k], v[40 + k] * v[40 + k]);
-          const float fb = fmaf(v[20 + k], v[20 + k], v[60 + k] * v[60 + k]);
+        for (int k = 0; k < 40; k += 2) {
+          float fa, fb;
+          psd2(v[k], v[k + 1], v[40 + k], v[41 + k], fa, fb);
           const float got = __shfl_xor_sync(FULL_MASK, odd ? fa : fb, 1);
-          if (k & 1) mx1 = fmaxf(mx1, (odd ? fb : fa) + got);
+          if (k & 2) mx1 = fmaxf(mx1, (odd ? fb : fa) + got);
           else mx = fmaxf(mx, (odd ? fb : fa) + got);
         }
         if (dump)
