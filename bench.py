@@ -50,8 +50,8 @@ def load_peaks():
 
 
 def load_traffic():
-    """DRAM bytes per Hall tensor-core launch from the committed ncu summary, if any."""
-    path = os.path.join(ROOT, "profiles", "hall_tc_kernel_n42.md")
+    """DRAM bytes per Hall tensor-core launch from the committed ncu figure, if any."""
+    path = os.path.join(ROOT, "profiles", "hall_tc_kernel_n42_traffic.txt")
     try:
         for line in open(path):
             if line.startswith("traffic_bytes_per_launch:"):
