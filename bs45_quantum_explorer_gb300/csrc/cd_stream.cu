@@ -161,7 +161,7 @@ __device__ __forceinline__ unsigned long long globaltimer() {
 }
 
 // MINB: the blocks of 256 threads the register budget is set for (4: 64 registers, no spill;
-// 6: 40 registers with a few spills on the rare paths). The launch sizes the grid to the
+// 5: 48 registers, 6: 40 registers, both with a few spills). The launch sizes the grid to the
 // blocks that are resident at once, so saved walks never wait for a block to be scheduled.
 //
 // Eight lanes walk one subtree together: lane j of a group tests child j of the group's
@@ -684,13 +684,14 @@ extern "C" int bs_cd_stream(bs_ctx *ctx, const bs_cell *cells, int ncells, const
   if (!rc) rc = ensure_store(&B->leaf_words, &B->leaf_keys, &B->leaf_cell, &B->leaf_cap, leaf_cap);
   if (!rc) rc = bs_ensure_dev((void **)&B->leaf_pass, &B->pass_cap, leaf_cap, 1);
   const int block = 256;
-  // register budget variant (BS_DFS_BLOCKS=6 selects the 40-register one) and the grid of
-  // exactly the blocks that fit at once
+  // register budget variant (BS_DFS_BLOCKS=5 or 6 select the 48- and 40-register builds) and
+  // the grid of exactly the blocks that fit at once
   static const int dfs_blocks = [] {
     const char *e = getenv("BS_DFS_BLOCKS");
-    return (e && atoi(e) == 6) ? 6 : 4;
+    const int b = e ? atoi(e) : 4;
+    return (b == 5 || b == 6) ? b : 4;
   }();
-  auto dfs_kernel = dfs_blocks == 6 ? cd_dfs_kernel<6> : cd_dfs_kernel<4>;
+  auto dfs_kernel = dfs_blocks == 6 ? cd_dfs_kernel<6> : (dfs_blocks == 5 ? cd_dfs_kernel<5> : cd_dfs_kernel<4>);
   int per_sm = 0;
   CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, dfs_kernel, block, 0));
   if (per_sm < 1) per_sm = 1;
