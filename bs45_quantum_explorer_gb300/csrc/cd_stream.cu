@@ -288,8 +288,13 @@ __global__ void __launch_bounds__(256, MINB) cd_dfs_kernel(CdParams P) {
         }
       }
     }
-    const unsigned gw = (__ballot_sync(FULL_MASK, written) >> (8 * g)) & 0xFFu;
-    const unsigned gunw = (__ballot_sync(FULL_MASK, emit && !written) >> (8 * g)) & 0xFFu;
+    // which of the group's leaves were written and which are still owed (no leaf in the
+    // warp: nothing to ask, the common case above the leaf level)
+    unsigned gw = 0, gunw = 0;
+    if (eb) {
+      gw = (__ballot_sync(FULL_MASK, written) >> (8 * g)) & 0xFFu;
+      gunw = (__ballot_sync(FULL_MASK, emit && !written) >> (8 * g)) & 0xFFu;
+    }
 
     // ---- move the walk (group-uniform) ----
     bool finished = false;
