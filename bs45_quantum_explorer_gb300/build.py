@@ -42,7 +42,7 @@ def _stale(target, deps):
 # host translation units linked into the library (the cell algebra behind bs_cell_list and
 # bs_ab_rows); the lane's main() is built separately as bin/bs_firsthit
 LIB_HOST = ["celllist.cpp", "cell_capi.cpp"]
-HOSTFLAGS = ["-O2", "-std=c++17", "-fPIC", f"-I{INCLUDE}"]
+HOSTFLAGS = ["-O2", "-std=c++17", "-fPIC", "-pthread", f"-I{INCLUDE}"]
 
 
 def build_library(force=False, verbose=False):
@@ -71,7 +71,7 @@ def build_library(force=False, verbose=False):
         if r.returncode != 0:
             raise RuntimeError(f"compile failed: {' '.join(cmd)}\n{r.stderr}")
     if force or jobs or _stale(LIB, objs):
-        cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart"]
+        cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart", "-lpthread"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stderr}")

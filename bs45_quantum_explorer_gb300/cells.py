@@ -20,6 +20,9 @@ def lane_defaults(n):
     return dict(m6=n >= 36, thm211b=n >= 36, thm212=n >= 36)
 
 
+LIST_GUESS = 1 << 20
+
+
 def cell_list(n, sig, m6=None, thm211b=None, thm212=None, endpos=False, orbit_canon=False,
               orbit_q=0, qprune=False, prof_order=0, nshard=1):
     """Returns (cells, kept, digest, m): cells a ctypes array of bs_cell, kept a uint8 array,
@@ -33,17 +36,23 @@ def cell_list(n, sig, m6=None, thm211b=None, thm212=None, endpos=False, orbit_ca
     a, b, c, dd = sig
     ncells = C.c_longlong(0)
     dig = C.create_string_buffer(40)
-    rc = lib().bs_cell_list(n, a, b, c, dd, C.byref(o), None, None, 0, C.byref(ncells), dig)
-    if rc == 2:
-        raise BsError(rc, "cell_list: the reference refuses this list")
-    if rc not in (BS_OK, BS_ERR_CAP):
-        check(rc, "cell_list")
-    cells = (Cell * max(1, ncells.value))()
-    kept = np.zeros(max(1, ncells.value), dtype=np.uint8)
-    rc = lib().bs_cell_list(n, a, b, c, dd, C.byref(o), cells, kept.ctypes.data, ncells.value,
-                            C.byref(ncells), dig)
+    # one build into a buffer of LIST_GUESS cells (24 MB); a longer list is built a second
+    # time into a buffer of the size the first call reported
+    cap = LIST_GUESS
+    for _ in range(2):
+        cells = (Cell * cap)()
+        kept = np.zeros(cap, dtype=np.uint8)
+        rc = lib().bs_cell_list(n, a, b, c, dd, C.byref(o), cells, kept.ctypes.data, cap,
+                                C.byref(ncells), dig)
+        if rc == 2:
+            raise BsError(rc, "cell_list: the reference refuses this list")
+        if rc != BS_ERR_CAP:
+            break
+        cap = max(1, ncells.value)
     check(rc, "cell_list")
-    return cells, kept[:ncells.value], dig.value.decode(), 6 if o.m6 else 3
+    if ncells.value < cap:
+        cells = (Cell * max(1, ncells.value)).from_buffer_copy(cells)
+    return cells, kept[:ncells.value].copy(), dig.value.decode(), 6 if o.m6 else 3
 
 
 def ab_rows(n, sig, m, cells):

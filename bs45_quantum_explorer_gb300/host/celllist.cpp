@@ -7,8 +7,32 @@
 #include <algorithm>
 #include <cstdio>
 #include <cstdlib>
+#include <thread>
 
 namespace bsfh {
+
+// Runs f(lo, hi, part) over [0, n) split into contiguous parts, one host thread each. Callers
+// keep one output per part and join them in part order, so every result is the same as the
+// serial loop's, whatever the thread count.
+template <class F>
+static int parallel_parts(size_t n, F f, size_t min_per_part = 256) {
+  unsigned hw = std::thread::hardware_concurrency();
+  size_t parts = std::max<size_t>(1, std::min<size_t>(hw ? hw : 1, 64));
+  parts = std::min(parts, std::max<size_t>(1, n / min_per_part));
+  if (parts <= 1) {
+    f((size_t)0, n, (size_t)0);
+    return 1;
+  }
+  const size_t chunk = (n + parts - 1) / parts;
+  std::vector<std::thread> th;
+  for (size_t t = 0; t < parts; t++) {
+    const size_t lo = t * chunk, hi = std::min(n, lo + chunk);
+    if (lo >= hi) break;
+    th.emplace_back(f, lo, hi, t);
+  }
+  for (auto &x : th) x.join();
+  return (int)parts;
+}
 
 int class_count(int L, int c, int m) {
   int k = 0;
@@ -105,18 +129,23 @@ void AutoSet::build(int L, int a, int b, int m, int n, bool thm212) {
   const auto K = enum_class_sums(L, a, m), R = enum_class_sums(L, b, m);
   const int tgt = 4 * n + 2, half = m / 2;
   const bool abSide = (L == n + 1);
-  Vec T(half);
-  for (const auto &kv : K) {
-    const int kn = norm_vec(kv);
-    if (kn > tgt) continue;
-    for (const auto &rv : R) {
-      const int rn = norm_vec(rv);
-      if (kn + rn > tgt) continue;
-      if (thm212 && !thm212_ok(kv, rv, m, n, abSide)) continue;
-      for (int s = 1; s <= half; s++) T[s - 1] = pair_auto(kv, rv, s);
-      keys.insert(auto_key(T, kn + rn));
+  std::vector<std::unordered_set<uint64_t>> part(64);
+  parallel_parts(K.size(), [&](size_t lo, size_t hi, size_t t) {
+    Vec T(half);
+    for (size_t i = lo; i < hi; i++) {
+      const Vec &kv = K[i];
+      const int kn = norm_vec(kv);
+      if (kn > tgt) continue;
+      for (const auto &rv : R) {
+        const int rn = norm_vec(rv);
+        if (kn + rn > tgt) continue;
+        if (thm212 && !thm212_ok(kv, rv, m, n, abSide)) continue;
+        for (int s = 1; s <= half; s++) T[s - 1] = pair_auto(kv, rv, s);
+        part[t].insert(auto_key(T, kn + rn));
+      }
     }
-  }
+  }, 16);
+  for (auto &p : part) keys.insert(p.begin(), p.end());
 }
 
 static Vec reduce63(const Vec &v6) { return Vec{v6[0] + v6[3], v6[1] + v6[4], v6[2] + v6[5]}; }
@@ -131,8 +160,11 @@ std::vector<Profile> survive_profiles3(int L, int sigX, int sigY, int n, const N
   std::vector<Vec> PX6r(PX6.size()), PY6r(PY6.size());
   for (size_t i = 0; i < PX6.size(); i++) PX6r[i] = reduce63(PX6[i]);
   for (size_t i = 0; i < PY6.size(); i++) PY6r[i] = reduce63(PY6[i]);
-  std::vector<Profile> out;
-  for (const auto &px : PX3) {
+  std::vector<std::vector<Profile>> part(64);
+  parallel_parts(PX3.size(), [&](size_t lo, size_t hi, size_t t) {
+  std::vector<Profile> &out = part[t];
+  for (size_t ix = lo; ix < hi; ix++) {
+    const Vec &px = PX3[ix];
     const int npx = norm_vec(px);
     if (npx > tgt) continue;
     for (const auto &py : PY3) {
@@ -162,6 +194,9 @@ std::vector<Profile> survive_profiles3(int L, int sigX, int sigY, int n, const N
       if (ok6) out.push_back({px, py});
     }
   }
+  }, 4);
+  std::vector<Profile> out;
+  for (auto &p : part) out.insert(out.end(), p.begin(), p.end());
   return out;
 }
 
@@ -176,26 +211,37 @@ std::vector<Profile> survive_profiles6(int L, int sigX, int sigY, int n, const N
     npy[j] = norm_vec(PY[j]);
     npy3[j] = norm_vec(reduce63(PY[j]));
   }
+  std::vector<std::vector<Profile>> part(64);
+  parallel_parts(PX.size(), [&](size_t lo, size_t hi, size_t t) {
+    std::vector<Profile> &out = part[t];
+    for (size_t ix = lo; ix < hi && out.size() < cap; ix++) {
+      const Vec &px = PX[ix];
+      const int npx = norm_vec(px);
+      if (npx > tgt) continue;
+      const int npx3 = norm_vec(reduce63(px));
+      if (npx3 > tgt) continue;
+      for (size_t j = 0; j < PY.size(); j++) {
+        const auto &py = PY[j];
+        const int need = tgt - npx - npy[j];
+        if (need < 0 || !comp6.has(need)) continue;
+        if (thm212 && !thm212_ok(px, py, 6, n, abSide)) continue;
+        const int need3 = tgt - npx3 - npy3[j];
+        if (need3 < 0 || !comp3.has(need3)) continue;
+        if (thm211b && comp6auto) {
+          Vec needT(3);
+          for (int s = 1; s <= 3; s++) needT[s - 1] = -pair_auto(px, py, s);
+          if (!comp6auto->has(needT, need)) continue;
+        }
+        out.push_back({px, py});
+      }
+    }
+  }, 64);
+  // the reference stops at the cap-th pair in its loop order: the same first `cap` pairs
   std::vector<Profile> out;
   if (capped) *capped = false;
-  for (const auto &px : PX) {
-    const int npx = norm_vec(px);
-    if (npx > tgt) continue;
-    const int npx3 = norm_vec(reduce63(px));
-    if (npx3 > tgt) continue;
-    for (size_t j = 0; j < PY.size(); j++) {
-      const auto &py = PY[j];
-      const int need = tgt - npx - npy[j];
-      if (need < 0 || !comp6.has(need)) continue;
-      if (thm212 && !thm212_ok(px, py, 6, n, abSide)) continue;
-      const int need3 = tgt - npx3 - npy3[j];
-      if (need3 < 0 || !comp3.has(need3)) continue;
-      if (thm211b && comp6auto) {
-        Vec needT(3);
-        for (int s = 1; s <= 3; s++) needT[s - 1] = -pair_auto(px, py, s);
-        if (!comp6auto->has(needT, need)) continue;
-      }
-      out.push_back({px, py});
+  for (auto &p : part) {
+    for (auto &x : p) {
+      out.push_back(std::move(x));
       if (out.size() >= cap) {
         if (log) {
           fprintf(log, "[mod6] WARNING: profile-pair space hit cap %zu — mod-6 PROFILE space itself explodes (Gate-A data)\n", cap);
@@ -400,12 +446,14 @@ int build_cell_list(int n, int SA, int SB, int SC, int SD, const ListOptions &op
   const CellKeyOrder &ko = CellKeyOrder::get();
   const size_t N = cells.size();
   std::vector<u128> own(N), oid(N);
-  for (size_t i = 0; i < N; i++) {
-    int px[8], py[8];
-    for (int c = 0; c < m; c++) { px[c] = cells[i].px[c]; py[c] = cells[i].py[c]; }
-    own[i] = ko.pack(px, py, m);
-    oid[i] = orbit_id(px, py, m, n, nvar, ko);
-  }
+  parallel_parts(N, [&](size_t lo, size_t hi, size_t) {
+    for (size_t i = lo; i < hi; i++) {
+      int px[8], py[8];
+      for (int c = 0; c < m; c++) { px[c] = cells[i].px[c]; py[c] = cells[i].py[c]; }
+      own[i] = ko.pack(px, py, m);
+      oid[i] = orbit_id(px, py, m, n, nvar, ko);
+    }
+  }, 4096);
   // group the cells by orbit; the orbit's representative is its smallest own key
   std::vector<uint32_t> by_orbit(N);
   for (size_t i = 0; i < N; i++) by_orbit[i] = (uint32_t)i;
@@ -443,24 +491,43 @@ int build_cell_list(int n, int SA, int SB, int SC, int SD, const ListOptions &op
       long long missing = 0, nonreal = 0, eq212 = 0, unknown = 0, nonint = 0;
       std::string cert;
       std::vector<std::string> certs;
+      // each cell's verdict on its Q image (0: the image is listed), in parallel; then the
+      // counts, dead orbits and certificates in cell order
+      enum { Q_LISTED, Q_NONINT, Q_NONREAL, Q_EQ212, Q_UNKNOWN };
+      std::vector<unsigned char> qv(N, Q_LISTED);
+      parallel_parts(N, [&](size_t lo, size_t hi, size_t) {
+        for (size_t i = lo; i < hi; i++) {
+          int qx[8], qy[8];
+          bool integral = true;
+          for (int c = 0; c < m; c++) {
+            qx[c] = cells[i].px[c];
+            qy[c] = cells[i].py[c];
+          }
+          for (int c = 0; c < m; c++) {
+            int r = ((n - 1 - c) % m + m) % m;
+            if ((qx[c] + qy[c] + qx[r] - qy[r]) & 1) integral = false;
+          }
+          quad_switch(qx, qy, m, n);
+          if (integral && std::binary_search(S.begin(), S.end(), ko.pack(qx, qy, m))) continue;
+          if (!integral) qv[i] = Q_NONINT;
+          else if (!realizable(qx) || !realizable(qy)) qv[i] = Q_NONREAL;
+          else if (thm212 && !thm212_ok(Vec(qx, qx + m), Vec(qy, qy + m), m, n, false)) qv[i] = Q_EQ212;
+          else qv[i] = Q_UNKNOWN;
+        }
+      }, 4096);
       for (size_t i = 0; i < N; i++) {
+        if (qv[i] == Q_LISTED) continue;
         int qx[8], qy[8];
-        bool integral = true;
         for (int c = 0; c < m; c++) {
           qx[c] = cells[i].px[c];
           qy[c] = cells[i].py[c];
         }
-        for (int c = 0; c < m; c++) {
-          int r = ((n - 1 - c) % m + m) % m;
-          if ((qx[c] + qy[c] + qx[r] - qy[r]) & 1) integral = false;
-        }
         quad_switch(qx, qy, m, n);
-        if (integral && std::binary_search(S.begin(), S.end(), ko.pack(qx, qy, m))) continue;
         missing++;
         const char *why = nullptr;
-        if (!integral) { nonint++; why = "nonintegral"; }
-        else if (!realizable(qx) || !realizable(qy)) { nonreal++; why = "not_realizable"; }
-        else if (thm212 && !thm212_ok(Vec(qx, qx + m), Vec(qy, qy + m), m, n, false)) { eq212++; why = "eq2.12"; }
+        if (qv[i] == Q_NONINT) { nonint++; why = "nonintegral"; }
+        else if (qv[i] == Q_NONREAL) { nonreal++; why = "not_realizable"; }
+        else if (qv[i] == Q_EQ212) { eq212++; why = "eq2.12"; }
         else { unknown++; continue; }
         if (!dead[gid[i]]) {
           dead[gid[i]] = 1;
