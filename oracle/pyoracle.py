@@ -115,17 +115,20 @@ def cd_stream(n, tx, ty, m=6, pinX=False, pinY=False, rev=False, endpos=False, c
     ty = np.ascontiguousarray(ty, np.int32)
     st = StreamStats()
     L = n + 1 if ab_side else n
-    dummy = np.zeros(2 * L, np.int8)
-    dp = np.zeros(1, np.uint8)
-    total = lib().or_cd_stream(n, L, m, tx, ty, int(pinX), int(pinY), int(rev), int(endpos),
-                               int(cd_prune), int(keep_all), dummy, dp, 0, C.byref(st))
-    if cap is not None:
-        total = min(total, cap)
-    out = np.zeros(max(1, total) * 2 * L, np.int8)
-    flags = np.zeros(max(1, total), np.uint8)
-    lib().or_cd_stream(n, L, m, tx, ty, int(pinX), int(pinY), int(rev), int(endpos),
-                       int(cd_prune), int(keep_all), out, flags, total, C.byref(st))
-    return (out[: total * 2 * L].reshape(total, 2, L), flags[:total],
+    # the walk writes at most `room` rows and returns the full count; a stream longer than
+    # the first buffer is walked a second time into one of its size
+    room = min(cap, 1 << 16) if cap is not None else 1 << 16
+    for _ in range(2):
+        out = np.zeros(max(1, room) * 2 * L, np.int8)
+        flags = np.zeros(max(1, room), np.uint8)
+        total = lib().or_cd_stream(n, L, m, tx, ty, int(pinX), int(pinY), int(rev), int(endpos),
+                                   int(cd_prune), int(keep_all), out, flags, room, C.byref(st))
+        want = min(total, cap) if cap is not None else total
+        if want <= room:
+            break
+        room = want
+        st = StreamStats()
+    return (out[: want * 2 * L].reshape(want, 2, L), flags[:want],
             dict(nodes=st.nodes, leaves=st.leaves, ok=st.ok))
 
 

@@ -15,6 +15,7 @@ Outputs (small, committed): known_quads.json, hall_golden.npz, streams_golden.np
 complete_golden.npz, controls_golden.json, bs7_6_all.npz.
 """
 import ctypes as C
+import functools
 import itertools
 import json
 import os
@@ -113,24 +114,39 @@ def abp_rows(n, a, b, px, py, m=6):
     need = 4 * n + 2 - norm(px) - norm(py)
     half = m // 2
     T = [-(acv(px, s) + acv(py, s) + acv(px, m - s) + acv(py, m - s)) for s in range(1, half + 1)]
-
-    def tups(sig):
-        out = []
-        for sgn in ([1, -1] if sig else [1]):
-            for v in enum_cs(n + 1, sgn * sig, m):
-                if norm(v) > 4 * n + 2:
-                    continue
-                out.append((v, norm(v), [acv(v, s) + acv(v, m - s) for s in range(1, half + 1)]))
-        return out
+    # the pairs (kv, rv) with kn + rn == need and kc + rc == T, in the reference's nested
+    # order: rv looked up by (rn, rc) among b's tuples, which keep their enumeration order
+    by_key = _tuples_by_key(n, b, m)
     rows = []
-    for kv, kn, kc in tups(a):
-        for rv, rn, rc in tups(b):
-            if kn + rn != need or [kc[s] + rc[s] for s in range(half)] != T:
-                continue
+    for kv, kn, kc in _tuples(n, a, m):
+        want = (need - kn, tuple(T[s] - kc[s] for s in range(half)))
+        for rv in by_key.get(want, ()):
             if not thm212(kv, rv, m, n, True):
                 continue
             rows.append(list(kv) + [0] * (8 - m) + list(rv) + [0] * (8 - m))
     return np.array(rows, np.int8).reshape(-1, 16)
+
+
+@functools.lru_cache(maxsize=None)
+def _tuples(n, sig, m):
+    """(v, norm, the half-period combined autocorrelations) of every class tuple of length
+    n+1 and class sum +sig or -sig, in enumeration order (wz_match.cpp:2318-2340)."""
+    half = m // 2
+    out = []
+    for sgn in ([1, -1] if sig else [1]):
+        for v in enum_cs(n + 1, sgn * sig, m):
+            if norm(v) > 4 * n + 2:
+                continue
+            out.append((tuple(v), norm(v), [acv(v, s) + acv(v, m - s) for s in range(1, half + 1)]))
+    return out
+
+
+@functools.lru_cache(maxsize=None)
+def _tuples_by_key(n, sig, m):
+    by = {}
+    for v, vn, vc in _tuples(n, sig, m):
+        by.setdefault((vn, tuple(vc)), []).append(v)
+    return by
 
 
 def pack(seqs):

@@ -6,6 +6,7 @@ charged node count and the completion A,B of every candidate; the kept order of 
 """
 import json
 import os
+from concurrent.futures import ThreadPoolExecutor
 
 import numpy as np
 import pytest
@@ -94,8 +95,11 @@ def test_completion_vs_oracle_first_hit(gpu, oracle):
         cells = [(x, y) for x in enum_cs(n, sig[2], 6) for y in enum_cs(n, sig[3], 6)]
         rng.shuffle(cells)
         cands, rows = [], []
-        for tx, ty in cells[:60]:
-            rs, _, _ = oracle.cd_stream(n, tx, ty, m=6, cap=20)
+        # the oracle walks each cell whole; the 60 walks run on all host threads
+        with ThreadPoolExecutor(os.cpu_count() or 4) as ex:
+            streams = list(ex.map(lambda c: oracle.cd_stream(n, c[0], c[1], m=6, cap=20)[0],
+                                  cells[:60]))
+        for (tx, ty), rs in zip(cells[:60], streams):
             if len(rs):
                 r = abp_rows(n, sig[0], sig[1], tx, ty)
                 for cand in rs[:8]:

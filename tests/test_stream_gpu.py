@@ -5,6 +5,7 @@ Bit-exact: the surviving (C,D) sequence in stream order, and per cell the DFS no
 the class-exact leaf count and the Hall-pass count.
 """
 import os
+from concurrent.futures import ThreadPoolExecutor
 
 import numpy as np
 import pytest
@@ -40,9 +41,13 @@ def _cells(n, total, m):
 
 def _oracle_batch(oracle, n, cells, m, pins, rev, endpos):
     rows, cidx, stats = [], [], []
-    for i, (tx, ty) in enumerate(cells):
-        r, _, st = oracle.cd_stream(n, tx, ty, m=m, pinX=pins[i][0], pinY=pins[i][1], rev=rev,
-                                    endpos=endpos)
+    # one oracle walk per cell, on all host threads, joined in cell order
+    with ThreadPoolExecutor(os.cpu_count() or 4) as ex:
+        outs = list(ex.map(lambda i: oracle.cd_stream(n, cells[i][0], cells[i][1], m=m,
+                                                      pinX=pins[i][0], pinY=pins[i][1],
+                                                      rev=rev, endpos=endpos),
+                           range(len(cells))))
+    for i, (r, _, st) in enumerate(outs):
         rows.append(r)
         cidx += [i] * len(r)
         stats.append(st)
