@@ -25,3 +25,22 @@ def test_reference_arm_prints_one_contract_line(built_lib):
     assert d["metric"].startswith("spectral-filtered C,D cands/s at n=42")
     assert d["unit"] == "pairs/s" and d["config"]["workload"] == "hall_filter_n42_2^24_pairs"
     assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["cpu_baseline"]["kind"] == "port"
+
+
+def test_reference_arm_under_torchrun_prints_on_rank0_only(built_lib):
+    """Launched like the multi-GPU bench (two ranks over 127.0.0.1): rank 0 alone does the
+    work and prints the line; the other rank exits 0 without output."""
+    import socket
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        port = s.getsockname()[1]
+    p = subprocess.run([sys.executable, "-m", "torch.distributed.run", "--nnodes=1",
+                        "--nproc-per-node", "2", "--master-addr", "127.0.0.1", "--master-port",
+                        str(port), os.path.join(ROOT, "bench.py"), "--impl", "reference",
+                        "--gpus", "2", "--steps", "3", "--warmup", "3"],
+                       capture_output=True, text=True, timeout=900, cwd=ROOT)
+    assert p.returncode == 0, p.stderr[-2000:]
+    lines = [l for l in p.stdout.splitlines() if l.startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["value"] > 0
