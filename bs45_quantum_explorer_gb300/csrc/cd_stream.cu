@@ -73,6 +73,10 @@ struct CdParams {
   int *stop_flag;         // set when the leaf buffer is full or the round's time is up
   unsigned long long round_ns;  // > 0: suspend every walk after about this long
   int *status;
+  // CD_PRUNE bit 2 (the REACH kernels only): the mirror blocks {r, s} as 4-bit class pairs
+  // per byte, and per depth the quads left in each block (one byte per block)
+  uint32_t reach_blk;
+  const uint32_t *reach_q;  // [32]
 };
 
 
@@ -105,9 +109,9 @@ struct QuadFx {  // the effect of branch kk at depth d
   uint64_t bx, by;
 };
 
-__device__ __forceinline__ int fld(uint64_t w, int c) { return (int)((w >> (8 * c)) & 255) - 64; }
+__host__ __device__ __forceinline__ int fld(uint64_t w, int c) { return (int)((w >> (8 * c)) & 255) - 64; }
 
-__device__ __forceinline__ void place(Walk &w, const QuadFx &f) {
+__host__ __device__ __forceinline__ void place(Walk &w, const QuadFx &f) {
   w.s0 += (uint64_t)f.ds[0];
   w.s1 += (uint64_t)f.ds[1];
   w.s2 += (uint64_t)f.ds[2];
@@ -124,7 +128,7 @@ __device__ __forceinline__ void unplace(Walk &w, const QuadFx &f, uint64_t posma
   w.Y &= ~posmask;
 }
 
-__device__ __forceinline__ void init_walk(Walk &w, const CellDev &cell, int L, int m) {
+__host__ __device__ __forceinline__ void init_walk(Walk &w, const CellDev &cell, int L, int m) {
   w.s0 = w.s1 = w.s2 = w.s3 = 0x4040404040404040ULL;
   for (int c = 0; c < m; c++) {
     const int cnt = (L - c + m - 1) / m;  // positions p < L with p % m == c
@@ -154,6 +158,26 @@ __device__ __forceinline__ uint64_t nibble_reverse(uint64_t x) {
   return ((uint64_t)__byte_perm(lo, 0, 0x0123) << 32) | (uint64_t)__byte_perm(hi, 0, 0x0123);
 }
 
+// CD_PRUNE bit 2 for a child whose slack words are a0..a3 (it passed the capacity test, so
+// every used byte is in [64, 86]): dx = ((rem + dx) - (rem - dx)) / 2, likewise dy; each of
+// the three mirror blocks must be reachable with the q3 quads it has left.
+__host__ __device__ __forceinline__ bool reach_ok(uint64_t a0, uint64_t a1, uint64_t a2, uint64_t a3,
+                                         uint32_t blk, uint32_t q3) {
+#pragma unroll
+  for (int b = 0; b < 3; b++) {
+    const int r = (blk >> (8 * b)) & 15, s = (blk >> (8 * b + 4)) & 15;
+    const int q = (q3 >> (8 * b)) & 255;
+    const int D0 = (fld(a1, r) - fld(a0, r)) >> 1, D1 = (fld(a3, r) - fld(a2, r)) >> 1;
+    const int D2 = (fld(a1, s) - fld(a0, s)) >> 1, D3 = (fld(a3, s) - fld(a2, s)) >> 1;
+    const int t0 = D0 + D1 + D2 + D3, t1 = D0 - D1 + D2 - D3, t2 = D0 + D1 - D2 - D3,
+              t3 = D0 - D1 - D2 + D3;
+    if ((t0 | t1 | t2 | t3) & 3) return false;
+    const int l1 = (abs(t0) + abs(t1) + abs(t2) + abs(t3)) >> 2;
+    if (l1 > q || ((q - l1) & 1)) return false;
+  }
+  return true;
+}
+
 __device__ __forceinline__ unsigned long long globaltimer() {
   unsigned long long t;
   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
@@ -170,14 +194,17 @@ __device__ __forceinline__ unsigned long long globaltimer() {
 // children before it count as nodes, as the reference counts them when it tries them), or,
 // when none is left, returns to the parent; at the leaf level all feasible children are
 // written at once. A warp holds four walks; warp-wide collectives run every step in every
-// lane, walks that have ended idle until the whole warp has.
-template <int MINB>
+// lane, walks that have ended idle until the whole warp has. REACH adds CD_PRUNE bit 2 to
+// every child's test (a child that fails it is still a node, as in the reference).
+template <int MINB, bool REACH>
 __global__ void __launch_bounds__(256, MINB) cd_dfs_kernel(CdParams P) {
   __shared__ QuadFx fx[32][16];
   __shared__ uint64_t posm[32];
+  __shared__ uint32_t rq[32];
   for (int t = threadIdx.x; t < 32 * 16; t += blockDim.x)
     fx[t >> 4][t & 15] = ((const QuadFx *)P.fx)[t];
   if (threadIdx.x < 32) posm[threadIdx.x] = P.posmask[threadIdx.x];
+  if (REACH && threadIdx.x < 32) rq[threadIdx.x] = P.reach_q[threadIdx.x];
   __syncthreads();
   const int lane = threadIdx.x & 31;
   const int j = lane & 7;               // the child this lane tests
@@ -246,6 +273,7 @@ __global__ void __launch_bounds__(256, MINB) cd_dfs_kernel(CdParams P) {
       const uint64_t a0 = w.s0 + (uint64_t)f.ds[0], a1 = w.s1 + (uint64_t)f.ds[1];
       const uint64_t a2 = w.s2 + (uint64_t)f.ds[2], a3 = w.s3 + (uint64_t)f.ds[3];
       ok = ((a0 & a1 & a2 & a3) & M) == M;
+      if (REACH && ok) ok = reach_ok(a0, a1, a2, a3, P.reach_blk, rq[d + 1]);
     }
     const unsigned gm = (__ballot_sync(FULL_MASK, ok) >> (8 * g)) & 0xFFu;
 
@@ -418,11 +446,71 @@ struct HostQuads {
   }
 };
 
+// The optional C,D prunes (WZ_FH_CD_PRUNE, wz_match.cpp:655-711, 719-731; C,D side, m = 6,
+// even L only). Both cut only subtrees without a class-exact leaf, so the stream is the same
+// and only the node count falls.
+//   bit 1: the root quad's entry sum must equal sum(tx) + sum(ty) mod 4 (every later quad is
+//          positive-product, entry sum 0 mod 4).
+//   bit 2: from depth 1, for each mirror block {r, s = (L-1-r) mod 6} with q quads left, the
+//          residual Delta = (dx_r, dy_r, dx_s, dy_s) is reachable by q positive-product quads
+//          (the +-columns of a 4x4 Hadamard H) iff t = H^T Delta / 4 is integral, |t|_1 <= q
+//          and q - |t|_1 is even.
+struct CdPrune {
+  bool root = false, reach = false;
+  int root_mod = 0;
+  int blk_r[3] = {0, 0, 0}, blk_s[3] = {0, 0, 0};
+  int qrem[33][3] = {};  // quads left per block at depths d..half-1
+
+  void setup(int mode, bool ab_side, int L, int m, const int8_t *tx, const int8_t *ty) {
+    const bool okk = !ab_side && m == 6 && L % 2 == 0;
+    root = okk && (mode & 1);
+    reach = okk && (mode & 2);
+    if (!okk || !mode) return;
+    int nb = 0, blk_of[6] = {0, 0, 0, 0, 0, 0};
+    for (int r = 0; r < 6; r++) {
+      const int s = (L - 1 - r) % 6;
+      if (r < s) { blk_r[nb] = r; blk_s[nb] = s; blk_of[r] = blk_of[s] = nb; nb++; }
+    }
+    const int half = L / 2;
+    for (int b = 0; b < 3; b++) qrem[half][b] = 0;
+    for (int d = half - 1; d >= 0; d--) {
+      for (int b = 0; b < 3; b++) qrem[d][b] = qrem[d + 1][b];
+      qrem[d][blk_of[d % 6]]++;
+    }
+    int tot = 0;
+    for (int c = 0; c < 6; c++) tot += tx[c] + ty[c];
+    root_mod = (tot % 4 + 4) % 4;
+  }
+  // bit 2's test at a node of depth d >= 1 with residuals dx[c] = tx - px, dy[c] = ty - py
+  bool reachable(int d, const int *dx, const int *dy) const {
+    for (int b = 0; b < 3; b++) {
+      const int r = blk_r[b], s = blk_s[b], q = qrem[d][b];
+      const int D0 = dx[r], D1 = dy[r], D2 = dx[s], D3 = dy[s];
+      const int t0 = D0 + D1 + D2 + D3, t1 = D0 - D1 + D2 - D3, t2 = D0 + D1 - D2 - D3,
+                t3 = D0 - D1 - D2 + D3;
+      if ((t0 | t1 | t2 | t3) & 3) return false;
+      const int l1 = (abs(t0) + abs(t1) + abs(t2) + abs(t3)) / 4;
+      if (l1 > q || ((q - l1) & 1)) return false;
+    }
+    return true;
+  }
+  // the per-launch form for the device: blocks as 4-bit class pairs, qrem as bytes
+  uint32_t blk_packed() const {
+    uint32_t v = 0;
+    for (int b = 0; b < 3; b++) v |= (uint32_t)blk_r[b] << (8 * b) | (uint32_t)blk_s[b] << (8 * b + 4);
+    return v;
+  }
+  uint32_t qrem_packed(int d) const {
+    return (uint32_t)qrem[d][0] | (uint32_t)qrem[d][1] << 8 | (uint32_t)qrem[d][2] << 16;
+  }
+};
+
 struct Frontier {
   int L, m, half, D, rev, root, pinX, pinY, ns0;
   int tot[8], px[8], py[8], placed[8];
   const int8_t *tx, *ty;
   const HostQuads *Q;
+  const CdPrune *prune;
   uint32_t cell;
   long long nodes;
   std::vector<Prefix> *out;
@@ -436,10 +524,20 @@ struct Frontier {
     }
     return true;
   }
+  // the whole test a node of depth d passes before its children are tried
+  bool node_ok(int d) const {
+    if (!check()) return false;
+    if (prune->reach && d >= 1) {
+      int dx[8], dy[8];
+      for (int c = 0; c < m; c++) { dx[c] = tx[c] - px[c]; dy[c] = ty[c] - py[c]; }
+      if (!prune->reachable(d, dx, dy)) return false;
+    }
+    return true;
+  }
 
   void rec(int d, uint64_t digits) {
     nodes++;
-    if (!check()) return;
+    if (!node_ok(d)) return;
     if (d == D) {
       out->push_back(Prefix{cell, (uint32_t)D, digits, 0});
       return;
@@ -451,6 +549,9 @@ struct Frontier {
       int k = rev ? ns - 1 - kk : kk;
       if (d == 0 && pinX && S[k][0] != 1) continue;
       if (d == 0 && pinY && S[k][1] != 1) continue;
+      if (d == 0 && prune->root &&
+          (((S[k][0] + S[k][1] + S[k][2] + S[k][3]) % 4 + 4) % 4) != prune->root_mod)
+        continue;
       px[c1] += S[k][0]; py[c1] += S[k][1]; px[c2] += S[k][2]; py[c2] += S[k][3];
       placed[c1]++; placed[c2]++;
       rec(d + 1, digits | ((uint64_t)kk << (4 * d)));
@@ -486,6 +587,7 @@ struct StreamBufs {
   int *stop = nullptr;
   QuadFx *fx = nullptr;      // [32][16] branch effects
   uint64_t *posm = nullptr;  // [32] position masks
+  uint32_t *reach_q = nullptr;  // [32] CD_PRUNE bit 2: quads left per mirror block and depth
 };
 
 static StreamBufs *bufs_of(bs_ctx *ctx) {
@@ -500,7 +602,7 @@ void bs_stream_free(bs_ctx *ctx) {
   cudaFree(b->leaf_words); cudaFree(b->leaf_keys); cudaFree(b->leaf_cell); cudaFree(b->leaf_pass);
   cudaFree(b->surv_words); cudaFree(b->surv_keys); cudaFree(b->surv_cell); cudaFree(b->counters);
   cudaFree(b->cell_stats); cudaFree(b->nsaved); cudaFree(b->stop); cudaFree(b->fx);
-  cudaFree(b->posm);
+  cudaFree(b->posm); cudaFree(b->reach_q);
   delete b;
   ctx->stream_bufs = nullptr;
 }
@@ -558,7 +660,6 @@ extern "C" int bs_cd_stream(bs_ctx *ctx, const bs_cell *cells, int ncells, const
   const int root_kind = opt->ab_side ? 2 : (opt->endpos ? 1 : 0);
   if (m != 3 && m != 6) return BS_ERR_ARG;
   if (L > 64 || L / 2 > 31) return BS_ERR_ARG;
-  if (opt->cd_prune != 0) return BS_ERR_ARG;  // optional CD_PRUNE is not built on the device
   int hall_mode = opt->hall_mode;
   if (hall_mode < BS_HALL_FP64 || hall_mode > BS_HALL_TC_BF16X2) return BS_ERR_ARG;
   CK(cudaSetDevice(ctx->device));
@@ -570,6 +671,7 @@ extern "C" int bs_cd_stream(bs_ctx *ctx, const bs_cell *cells, int ncells, const
   static const HostQuads Q;
   const int max_depth = std::min(half - 1, 16);
   std::vector<Frontier> F(ncells);
+  std::vector<CdPrune> prune(ncells);  // CD_PRUNE: the root rule depends on the cell
   std::vector<Prefix> coarse;
   std::vector<long long> host_nodes(ncells, 0);
   long long target = opt->target_prefixes > 0 ? opt->target_prefixes : 262144;
@@ -586,6 +688,8 @@ extern "C" int bs_cd_stream(bs_ctx *ctx, const bs_cell *cells, int ncells, const
       for (int p = k; p < L; p += m) f.tot[k]++;
     }
     f.tx = c.tx; f.ty = c.ty; f.Q = &Q; f.cell = (uint32_t)ci;
+    prune[ci].setup(opt->cd_prune, opt->ab_side != 0, L, m, c.tx, c.ty);
+    f.prune = &prune[ci];
     // deepen until the cell has enough prefixes or the split reaches the deepest prefix depth
     std::vector<Prefix> mine;
     int D = 1;
@@ -670,7 +774,7 @@ extern "C" int bs_cd_stream(bs_ctx *ctx, const bs_cell *cells, int ncells, const
       for (int k = first; k < 8; k++) {
         apply(f, t, k, +1);
         added++;
-        if (f.check()) {
+        if (f.node_ok(t + 1)) {
           uint64_t q0 = p0, q1 = p1;
           if (t < 16) q0 |= (uint64_t)k << (4 * t);
           else q1 |= (uint64_t)k << (4 * (t - 16));
@@ -696,7 +800,10 @@ extern "C" int bs_cd_stream(bs_ctx *ctx, const bs_cell *cells, int ncells, const
     const int b = e ? atoi(e) : 4;
     return (b == 5 || b == 6) ? b : 4;
   }();
-  auto dfs_kernel = dfs_blocks == 6 ? cd_dfs_kernel<6> : (dfs_blocks == 5 ? cd_dfs_kernel<5> : cd_dfs_kernel<4>);
+  const bool reach = prune[0].reach;  // the same for every cell of the batch
+  auto dfs_kernel = reach ? cd_dfs_kernel<4, true>
+                          : dfs_blocks == 6 ? cd_dfs_kernel<6, false>
+                                            : (dfs_blocks == 5 ? cd_dfs_kernel<5, false> : cd_dfs_kernel<4, false>);
   int per_sm = 0;
   CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, dfs_kernel, block, 0));
   if (per_sm < 1) per_sm = 1;
@@ -714,6 +821,7 @@ extern "C" int bs_cd_stream(bs_ctx *ctx, const bs_cell *cells, int ncells, const
     CK(cudaMalloc(&B->stop, sizeof(int)));
     CK(cudaMalloc(&B->fx, sizeof(QuadFx) * 32 * 16));
     CK(cudaMalloc(&B->posm, sizeof(uint64_t) * 32));
+    CK(cudaMalloc(&B->reach_q, sizeof(uint32_t) * 32));
   }
   long long surv_cap = opt->survivor_cap > 0 ? opt->survivor_cap : (1LL << 22);
   if (!rc) rc = ensure_store(&B->surv_words, &B->surv_keys, &B->surv_cell, &B->surv_cap, surv_cap);
@@ -754,6 +862,10 @@ extern "C" int bs_cd_stream(bs_ctx *ctx, const bs_cell *cells, int ncells, const
   cudaStream_t s = ctx->stream;
   CK(cudaMemcpyAsync(B->fx, fxh.data(), sizeof(QuadFx) * fxh.size(), cudaMemcpyHostToDevice, s));
   CK(cudaMemcpyAsync(B->posm, posm.data(), sizeof(uint64_t) * 32, cudaMemcpyHostToDevice, s));
+  std::vector<uint32_t> rqh(32, 0);
+  if (reach)
+    for (int dd = 1; dd <= half && dd < 32; dd++) rqh[dd] = prune[0].qrem_packed(dd);
+  CK(cudaMemcpyAsync(B->reach_q, rqh.data(), sizeof(uint32_t) * 32, cudaMemcpyHostToDevice, s));
   CK(cudaMemcpyAsync(B->cells, hc.data(), sizeof(CellDev) * ncells, cudaMemcpyHostToDevice, s));
   CK(cudaMemsetAsync(B->cell_stats, 0, sizeof(unsigned long long) * 3 * ncells, s));
   // counters: [0] next prefix of the queue, [1] leaf count of the round, [2] survivors of the wave
@@ -820,6 +932,7 @@ extern "C" int bs_cd_stream(bs_ctx *ctx, const bs_cell *cells, int ncells, const
       P.leaf_count = B->counters + 1; P.leaf_cap = (unsigned long long)leaf_cap;
       P.cell_nodes = cell_nodes; P.cell_leaves = cell_leaves;
       P.stop_flag = B->stop; P.round_ns = ROUND_NS; P.status = ctx->d_status;
+      P.reach_blk = prune[0].blk_packed(); P.reach_q = B->reach_q;
       bs_timed_begin(ctx);
       dfs_kernel<<<grid, block, 0, s>>>(P);
       bs_timed_end(ctx);

@@ -8,8 +8,9 @@
 //   0 FOUND, 3 no hit / range exhausted / interrupted, 2 refusal, 1 usage, 5 internal error.
 // Not carried over (measurement-only instruments of the reference): FH_TELEM telemetry,
 // HALLSTAT adaptive-order statistics, the A2 shadow, LOCATE / ORBIT_AUDIT / OUTER_DUMP / TARGET
-// canaries. WZ_FH_CD_PRUNE and WZ_FH_HALL_FAST change no stream and are accepted; WZ_FH_WALL_SEC
-// is accepted for the CFGSIG namespace but no cell is abandoned on time.
+// canaries. WZ_FH_CD_PRUNE prunes the device stream as the reference's DFS does (same stream,
+// CDSTAT counts the pruned walk); WZ_FH_HALL_FAST changes no stream and is accepted;
+// WZ_FH_WALL_SEC is accepted for the CFGSIG namespace but no cell is abandoned on time.
 #include <algorithm>
 #include <atomic>
 #include <chrono>
@@ -407,7 +408,7 @@ int main(int argc, char **argv) {
   so.m = fh_m;
   so.rev = stream_rev ? 1 : 0;
   so.endpos = endpos ? 1 : 0;
-  so.cd_prune = 0;
+  so.cd_prune = env_i("WZ_FH_CD_PRUNE", 0);
   so.hall_mode = hall_mode;
   // Front-only lanes use only a cell's first DRAIN_BATCHES x BUF_CAP survivors (the reference
   // stops the cell's DFS there); the device stream stops there too. Score filtering and the

@@ -26,17 +26,19 @@ def make_cells(cells, m, pins=None):
 
 def cd_stream(ctx, cells, m=6, pins=None, rev=False, endpos=False, hall_mode="tc_fp16",
               target_prefixes=0, leaf_chunk=0, survivor_cap=0, cap=None, as_words=False,
-              ab_side=False, limit=0, round_us=0):
+              ab_side=False, limit=0, round_us=0, cd_prune=0):
     """cells: list of (tx, ty). Returns (survivors, cell index per survivor, per-cell stats).
 
     survivors: int8 [k, 2, L] (or uint64 words [k, 2] with as_words) in stream order, L = n
     (C,D) or n+1 with ab_side (the reference's abSide stream of A,B pairs).
     stats: list of dicts {nodes, leaves, ok} per cell (the reference's CDSTAT dfs_nodes and
     CELLSIZE leaves / hall_ok; with limit > 0, of the part explored).
-    limit > 0 returns only the first `limit` survivors and stops the search there."""
+    limit > 0 returns only the first `limit` survivors and stops the search there.
+    cd_prune: WZ_FH_CD_PRUNE (bit 1 root quad rule, bit 2 block reachability; C,D side, m = 6,
+    even n only): the same survivors, fewer DFS nodes."""
     ncells = len(cells)
     arr = make_cells(cells, m, pins)
-    opt = StreamOpts(m=m, rev=int(rev), endpos=int(endpos), cd_prune=0,
+    opt = StreamOpts(m=m, rev=int(rev), endpos=int(endpos), cd_prune=int(cd_prune),
                      hall_mode=MODES[hall_mode], ab_side=int(ab_side),
                      target_prefixes=target_prefixes, leaf_chunk=leaf_chunk,
                      survivor_cap=survivor_cap, limit=limit, round_us=round_us)

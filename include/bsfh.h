@@ -131,7 +131,11 @@ typedef struct {
   int32_t m;                 /* class modulus of the cells: 3 or 6 */
   int32_t rev;               /* WZ_FH_STREAM_REV: reversed branch order */
   int32_t endpos;            /* WZ_FH_ENDPOS: positive-product endpoint quad */
-  int32_t cd_prune;          /* WZ_FH_CD_PRUNE: only 0 (the optional prunes are host-only) */
+  int32_t cd_prune;          /* WZ_FH_CD_PRUNE (wz_match.cpp:655-666, 719-731): bit 1 the root
+                                quad's entry sum mod 4, bit 2 exact reachability of each mirror
+                                block from depth 1; C,D side, m = 6, even L only (else no-op).
+                                The survivors are the same; the node counts are the pruned
+                                walk's, as the reference's CDSTAT prints them */
   int32_t hall_mode;         /* BS_HALL_* form of the leaf test */
   int32_t ab_side;           /* 1: stream the A,B side (length n+1, negative-product root quads) */
   long long target_prefixes; /* coarse split of the batch into subtrees (0 = 262144); the

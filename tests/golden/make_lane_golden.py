@@ -36,6 +36,9 @@ SETTINGS = [
     dict(WZ_FH_M6=1, WZ_FH_AB_BUDGET=5, WZ_FH_BUF_CAP=7, WZ_FH_DRAIN_TOP=3, WZ_FH_DRAIN_BATCHES=2),
     dict(WZ_FH_M6=1, WZ_FH_CELLSIZE=10 ** 9),
     dict(WZ_FH_M6=1, WZ_FH_CELLSIZE=10 ** 9, WZ_FH_STREAM_REV=1, WZ_FH_ENDPOS=1),
+    dict(WZ_FH_M6=1, WZ_FH_CELLSIZE=10 ** 9, WZ_FH_CD_PRUNE=3),
+    dict(WZ_FH_M6=1, WZ_FH_CELLSIZE=10 ** 9, WZ_FH_CD_PRUNE=1, WZ_FH_STREAM_REV=1),
+    dict(WZ_FH_M6=1, WZ_FH_CELLSIZE=10 ** 9, WZ_FH_CD_PRUNE=2, WZ_FH_ENDPOS=1),
     dict(WZ_FH_M6=0, WZ_FH_AB_BUDGET=0),
     dict(WZ_FH_M6=0, WZ_FH_AB_BUDGET=20, WZ_FH_OUTER_K=0, WZ_FH_EARLY_CHECK=0),
     dict(WZ_FH_M6=1, WZ_FH_AB_BUDGET=0, WZ_FH_ORBIT_CANON=1, WZ_FH_ORBIT_Q=1, WZ_FH_PROF_ORDER=3,

@@ -42,10 +42,22 @@ def _cases():
 
 
 def test_lane_matches_reference_runs(gpu):
+    cases = [c for c in _cases() if not c.get("resume") and "WZ_FH_CD_PRUNE" not in c["settings"]]
+    assert len(cases) > 200
+    _replay(cases)
+
+
+def test_lane_cd_prune_matches_reference_runs(gpu):
+    """WZ_FH_CD_PRUNE 1, 2, 3 with CELLSIZE on: the same lane output and the pruned CDSTAT
+    dfs_nodes of every cell."""
+    cases = [c for c in _cases() if not c.get("resume") and "WZ_FH_CD_PRUNE" in c["settings"]]
+    assert len(cases) >= 80
+    _replay(cases)
+
+
+def _replay(cases):
     from make_lane_golden import cellsize_lines, semantic
     exe = _bin()
-    cases = [c for c in _cases() if not c.get("resume")]
-    assert len(cases) > 200
     with tempfile.TemporaryDirectory() as tmp:
         for c in cases:
             rc, out, dh, dl = _run(exe, c["n"], c["sig"], c["settings"], tmp)

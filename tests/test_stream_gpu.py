@@ -121,6 +121,41 @@ def test_stream_larger_n(gpu, oracle, n):
         assert gst == rst, kw
 
 
+@pytest.mark.parametrize("n,sig", [(16, (3, 5, 4, 4)), (20, (1, 7, 4, 4)), (22, (1, 3, 4, 8))])
+def test_stream_cd_prune_matches_oracle(gpu, oracle, n, sig):
+    """WZ_FH_CD_PRUNE 1, 2, 3: the same survivors as without it and the pruned node counts of
+    the oracle (the reference's rec() calls), also with 1 us launches, so that suspended
+    walks are split on the host under the prune; m = 3 cells are not pruned."""
+    from bs45_quantum_explorer_gb300.hall import Context
+    from bs45_quantum_explorer_gb300.stream import cd_stream
+    ctx = Context(n, sig)
+    rng = np.random.default_rng(n + 100)
+    cells = [(x, y) for x in _cells(n, sig[2], 6) for y in _cells(n, sig[3], 6)]
+    # cells whose class sums are small have the largest streams
+    cells.sort(key=lambda c: sum(abs(v) for v in c[0]) + sum(abs(v) for v in c[1]))
+    cells = [cells[i] for i in rng.permutation(min(len(cells), 200))[:16]]
+    pins = [(0, 0)] * len(cells)
+    base, _, _ = cd_stream(ctx, cells, m=6, pins=pins)
+    for mode in (1, 2, 3):
+        for kw in (dict(), dict(round_us=1), dict(rev=True, endpos=True)):
+            okw = {k: v for k, v in kw.items() if k in ("rev", "endpos")}
+            with ThreadPoolExecutor(os.cpu_count() or 4) as ex:
+                want = list(ex.map(lambda c: oracle.cd_stream(n, c[0], c[1], m=6, cd_prune=mode,
+                                                              **okw), cells))
+            ref = np.concatenate([w[0] for w in want])
+            got, _, gst = cd_stream(ctx, cells, m=6, pins=pins, cd_prune=mode, **kw)
+            assert got.shape == ref.shape and (got == ref).all(), (mode, kw)
+            assert gst == [w[2] for w in want], (mode, kw)
+            if not okw:
+                assert got.shape == base.shape and (got == base).all(), (mode, kw)
+    # m = 3 cells are never pruned
+    c3 = [(x, y) for x in _cells(n, sig[2], 3) for y in _cells(n, sig[3], 3)][:8]
+    _, _, s0 = cd_stream(ctx, c3, m=3, pins=[(0, 0)] * len(c3))
+    _, _, s3 = cd_stream(ctx, c3, m=3, pins=[(0, 0)] * len(c3), cd_prune=3)
+    assert s0 == s3
+    ctx.close()
+
+
 def test_stream_golden_reference(gpu):
     """Survivors and counts exactly as the reference's count_pairs22 produced them."""
     from bs45_quantum_explorer_gb300.hall import Context
@@ -136,14 +171,11 @@ def test_stream_golden_reference(gpu):
         if key not in ctxs:
             ctxs[key] = Context(n, (a, b, c, d))
         got, _, st = cd_stream(ctxs[key], [(tx, ty)], m=m, pins=[(pinX, pinY)], rev=rev,
-                               endpos=endpos, as_words=True)
+                               endpos=endpos, as_words=True, cd_prune=cdp)
         assert got.shape[0] == cnt
         assert (got == words[off:off + cnt]).all()
         assert st[0]["leaves"] == leaves and st[0]["ok"] == ok
-        if cdp == 0:  # the optional CD_PRUNE only removes nodes, never leaves
-            assert st[0]["nodes"] == nodes
-        else:
-            assert st[0]["nodes"] >= nodes
+        assert st[0]["nodes"] == nodes, (n, m, cdp, tx, ty)
 
 
 def test_stream_limit_returns_the_stream_prefix(gpu, oracle):
