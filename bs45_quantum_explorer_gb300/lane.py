@@ -72,14 +72,15 @@ def run_lane(ctx, n, sig, skip=0, end=0, shard=0, nshard=1, budget=200000, buf_c
              drain_top=0, drain_batches=1, endpos=False, orbit_canon=True, orbit_q=1, qprune=True,
              prof_order=3, m6=None, thm211b=None, thm212=None, abp_cap=20000, outer_k=3,
              early=True, canon=True, rev=False, hall_mode="tc_fp16", chunk=65536,
-             max_seconds=0.0, listing=None, batch_cells=None):
+             max_seconds=0.0, listing=None, batch_cells=None, cd_prune=0):
     """Runs the lane over raw cells [skip, end) of its shard (end = 0: to the list's end).
     The list options are the lane's WZ_FH_* list settings (cells.cell_list); the cells must
     be mod-6 cells (the lane's buffered order). max_seconds > 0 stops between cells once
     exceeded (the result then says found=False and its counts cover the cells done).
     listing: a cell_list() result to reuse. batch_cells: cells streamed per device call
     (default 32 up to n = 30, where cells are small, else 1); a batch is streamed whole and
-    each cell cut to its front-only prefix on the host, which is the same prefix."""
+    each cell cut to its front-only prefix on the host, which is the same prefix.
+    cd_prune: WZ_FH_CD_PRUNE for the streams (fewer DFS nodes, the same candidates)."""
     cells, kept, _, m = listing if listing is not None else lane_list(
         n, sig, m6, thm211b, thm212, endpos, orbit_canon, orbit_q, qprune, prof_order)
     if m != 6:
@@ -105,7 +106,7 @@ def run_lane(ctx, n, sig, skip=0, end=0, shard=0, nshard=1, budget=200000, buf_c
         pins = [(cells[q].pinX, cells[q].pinY) for q in group]
         t0 = time.perf_counter()
         surv, cidx, st = cd_stream(ctx, args, m=m, pins=pins, rev=rev, endpos=endpos,
-                                   hall_mode=hall_mode, as_words=True,
+                                   hall_mode=hall_mode, as_words=True, cd_prune=cd_prune,
                                    limit=cut if len(group) == 1 else 0)
         res.stream_s += time.perf_counter() - t0
         if len(group) == 1:

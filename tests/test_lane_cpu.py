@@ -34,7 +34,7 @@ def _fakes(oracle):
         words, cidx, stats = [], [], []
         for i, (tx, ty) in enumerate(cells):
             r, _, st = oracle.cd_stream(ctx.n, tx, ty, m=m, pinX=pins[i][0], pinY=pins[i][1],
-                                        rev=rev, endpos=endpos)
+                                        rev=rev, endpos=endpos, cd_prune=kw.get("cd_prune", 0))
             words.append(pack(r) if len(r) else np.zeros((0, 2), np.uint64))
             cidx += [i] * len(r)
             stats.append(st)
@@ -85,3 +85,27 @@ def test_run_lane_control_flow_matches_reference_runs(built_lib, oracle, monkeyp
             res = lane.run_lane(_Ctx(c["n"], c["sig"]), c["n"], tuple(c["sig"]), batch_cells=batch,
                                 **lane_kwargs(c["settings"]))
             check_run_lane(res, summary_of(c["semantic"]), (c["n"], c["sig"], c["settings"], batch))
+
+
+def test_run_lane_cd_prune_changes_only_the_node_count(built_lib, oracle, monkeypatch):
+    """CD_PRUNE removes DFS nodes only: every lane summary is the one without it, and the
+    lane's DFS node count does not grow (even n, mod-6 cells)."""
+    import bs45_quantum_explorer_gb300.lane as lane
+    from test_lane_gpu import check_run_lane, lane_kwargs, summary_of
+    stream, topk, complete = _fakes(oracle)
+    monkeypatch.setattr(lane, "cd_stream", stream)
+    monkeypatch.setattr(lane, "flat_topk", topk)
+    monkeypatch.setattr(lane, "complete_ab", complete)
+    cases = [c for c in json.load(open(os.path.join(HERE, "golden", "lane_golden.json")))
+             if not c.get("resume") and c["settings"].get("WZ_FH_M6") == 1 and c["n"] in (8, 10)
+             and not any(k in c["settings"] for k in ("WZ_FH_CELLSIZE", "WZ_FH_SCORE_MAX"))]
+    assert len(cases) >= 10
+    fewer = 0
+    for c in cases:
+        kw = lane_kwargs(c["settings"])
+        r0 = lane.run_lane(_Ctx(c["n"], c["sig"]), c["n"], tuple(c["sig"]), **kw)
+        r3 = lane.run_lane(_Ctx(c["n"], c["sig"]), c["n"], tuple(c["sig"]), cd_prune=3, **kw)
+        check_run_lane(r3, summary_of(c["semantic"]), (c["n"], c["sig"], c["settings"]))
+        assert r3.dfs_nodes <= r0.dfs_nodes
+        fewer += r3.dfs_nodes < r0.dfs_nodes
+    assert fewer > 0
