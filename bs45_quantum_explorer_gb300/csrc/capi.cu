@@ -282,7 +282,9 @@ extern "C" int bs_ctx_retarget(bs_ctx *ctx, int n, int a, int b, int c, int d) {
     ctx->sig[0] = a; ctx->sig[1] = b; ctx->sig[2] = c; ctx->sig[3] = d;
     return BS_OK;
   }
-  return load_tables(ctx, n, a, b, c, d);
+  const int rc = load_tables(ctx, n, a, b, c, d);
+  if (rc != BS_OK) ctx->n = 0;  // tables half loaded: the next retarget reloads them all
+  return rc;
 }
 
 extern "C" void bs_ctx_destroy(bs_ctx *ctx) {

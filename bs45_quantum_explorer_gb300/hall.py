@@ -59,9 +59,13 @@ class Context:
         check(lib().bs_ctx_set_stream(self.h, C.c_void_p(stream_handle)), "bs_ctx_set_stream")
 
     def retarget(self, n, sig):
-        """Point the context at another (n, signature), keeping its stream and buffers."""
+        """Point the context at another (n, signature), keeping its stream and buffers. If it
+        fails, n becomes None until a retarget succeeds (the tables are half loaded)."""
         a, b, c, d = sig
-        check(lib().bs_ctx_retarget(self.h, n, a, b, c, d), "bs_ctx_retarget")
+        rc = lib().bs_ctx_retarget(self.h, n, a, b, c, d)
+        if rc != 0:
+            self.n = self.sig = None
+        check(rc, "bs_ctx_retarget")
         self.n, self.sig = n, tuple(sig)
 
     # ---- Hall filter ----

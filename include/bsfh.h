@@ -62,8 +62,9 @@ int bs_ctx_create(int n, int a, int b, int c, int d, int device, bs_ctx **out);
 void bs_ctx_destroy(bs_ctx *ctx);
 /* Point an existing context at another BS(n+1,n) and signature, keeping its stream and every
  * device buffer (a serving slot reuses one context across jobs instead of allocating, and so
- * synchronising the device, per job). Waits for the context's queued work first. No
- * counterpart in the reference (one process per lane there). */
+ * synchronising the device, per job). Waits for the context's queued work first. On failure
+ * the tables are left half loaded: only another bs_ctx_retarget (which then reloads them all)
+ * or bs_ctx_destroy may follow. No counterpart in the reference (one process per lane there). */
 int bs_ctx_retarget(bs_ctx *ctx, int n, int a, int b, int c, int d);
 /* Use a caller-owned CUDA stream (cudaStream_t) for every later call; NULL = the context's own. */
 int bs_ctx_set_stream(bs_ctx *ctx, void *cuda_stream);
