@@ -64,6 +64,29 @@ def test_cell_list_capi_matches_reference(built_lib):
         assert m == (6 if _opts(c)["m6"] else 3)
 
 
+def test_cell_list_longer_than_its_first_buffer(built_lib, monkeypatch):
+    """A list longer than the first buffer is built again at its reported size: the same
+    cells, kept flags and digest as a single build."""
+    import ctypes as C
+
+    import bs45_quantum_explorer_gb300.cells as cl
+    args = (17, _sigs(17)[0])
+    kw = dict(m6=True, orbit_canon=True, orbit_q=1, prof_order=3)
+    cells, kept, digest, m = cl.cell_list(*args, **kw)
+    assert len(kept) > 8 and digest
+    monkeypatch.setattr(cl, "LIST_GUESS", 8)
+    cells2, kept2, digest2, m2 = cl.cell_list(*args, **kw)
+    assert (digest2, m2) == (digest, m) and np.array_equal(kept2, kept)
+    assert len(cells2) == len(cells)
+    assert C.string_at(C.addressof(cells2), C.sizeof(cells2)) == \
+        C.string_at(C.addressof(cells), C.sizeof(cells))
+
+
+def _sigs(n):
+    from make_golden import classes
+    return [tuple(s) for s in classes(n)]
+
+
 def test_cell_list_without_canon_keeps_every_cell_and_sets_pins(built_lib):
     from bs45_quantum_explorer_gb300.cells import cell_list
     cells, kept, digest, m = cell_list(12, (1, 7, 0, 0), m6=True)
