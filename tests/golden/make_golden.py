@@ -9,10 +9,13 @@ and autocorr_key). Every expected value below is computed by that reference code
 BS(7,6) full set, which is a numpy brute force over all 2^26 (A,B) x ... pairs as the
 reference's own test_orbit_q_retention.py does it (join of pair autocorrelations).
 
-    python tests/golden/make_golden.py [REF]
+    python tests/golden/make_golden.py [REF]           # everything below but the two that follow
+    python tests/golden/make_golden.py REF ab          # ab_streams_golden.npz
+    python tests/golden/make_golden.py REF cdprune     # cd_prune_golden.npz
 
 Outputs (small, committed): known_quads.json, hall_golden.npz, streams_golden.npz,
-complete_golden.npz, controls_golden.json, bs7_6_all.npz.
+complete_golden.npz, controls_golden.json, bs7_6_all.npz, ab_streams_golden.npz,
+cd_prune_golden.npz.
 """
 import ctypes as C
 import functools
@@ -198,10 +201,49 @@ def ab_streams(R):
     print("A,B streams", len(cases), sum(len(s) for s in surv))
 
 
+def cd_prune_streams(R):
+    """C,D streams under WZ_FH_CD_PRUNE 1, 2 and 3 (count_pairs22 with G_CD_PRUNE set): even n,
+    m = 6 cells, where the prunes apply, and m = 3 cells, where they do not. Same row layout as
+    streams_golden.npz."""
+    rng = random.Random(0xCDB)
+    cases, surv = [], []
+    for n in (8, 10, 12, 14, 16, 18, 20):
+        cl = classes(n)
+        for sig in rng.sample(cl, min(2, len(cl))):
+            a, b, c, d = sig
+            R.refh_setup(n, a, b, c, d, 3)
+            for m in (6, 3):
+                cells = [(x, y) for x in enum_cs(n, c, m) for y in enum_cs(n, d, m)]
+                # small class sums first: the cells with the largest streams
+                cells.sort(key=lambda t: sum(map(abs, t[0])) + sum(map(abs, t[1])))
+                pick = cells[:40]
+                rng.shuffle(pick)
+                for (tx, ty) in pick[:2]:
+                    rev, endpos, pin = rng.choice([(0, 0, 0), (1, 0, 1), (0, 1, 0), (1, 1, 1)])
+                    pinX, pinY = int(pin and c == 0), int(pin and d == 0)
+                    for cdp in (1, 2, 3):
+                        cap = 1 << 20
+                        out = np.zeros(cap * 2 * n, np.int32)
+                        nd, lv, ok = C.c_longlong(), C.c_longlong(), C.c_longlong()
+                        w = R.refh_stream(n, np.array(tx, np.int32), np.array(ty, np.int32), m, pinX,
+                                          pinY, rev, endpos, cdp, 1, out, cap, C.byref(nd), C.byref(lv),
+                                          C.byref(ok))
+                        off = sum(len(t) for t in surv)
+                        cases.append([n, a, b, c, d, m, rev, endpos, pinX, pinY, cdp, nd.value, lv.value,
+                                      ok.value, off, w] + list(tx) + [0] * (6 - m) + list(ty) + [0] * (6 - m))
+                        surv.append(pack(out[:w * 2 * n].reshape(w, 2, n)).reshape(-1, 2))
+    np.savez_compressed(os.path.join(HERE, "cd_prune_golden.npz"), cases=np.array(cases, np.int64),
+                        words=np.concatenate(surv) if surv else np.zeros((0, 2), np.uint64))
+    print("CD_PRUNE streams", len(cases), sum(len(t) for t in surv))
+
+
 def main():
     R = load_ref()
     if len(sys.argv) > 2 and sys.argv[2] == "ab":
         ab_streams(R)
+        return
+    if len(sys.argv) > 2 and sys.argv[2] == "cdprune":
+        cd_prune_streams(R)
         return
     rng = random.Random(0xB545)
 

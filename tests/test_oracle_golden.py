@@ -39,10 +39,12 @@ def test_hall_decisions_match_reference(oracle):
     assert (got == g["near_decisions"]).all()
 
 
-def test_streams_match_reference(oracle):
-    g = np.load(os.path.join(G, "streams_golden.npz"))
+@pytest.mark.parametrize("fixture,least", [("streams_golden.npz", 100), ("cd_prune_golden.npz", 150)])
+def test_streams_match_reference(oracle, fixture, least):
+    """count_pairs22 survivors and counts; cd_prune_golden.npz holds WZ_FH_CD_PRUNE 1, 2, 3."""
+    g = np.load(os.path.join(G, fixture))
     cases, words = g["cases"], g["words"]
-    assert len(cases) >= 100
+    assert len(cases) >= least
     for row in cases:
         n, a, b, c, d, m, rev, endpos, pinX, pinY, cdp, nodes, leaves, ok, off, cnt = (int(x) for x in row[:16])
         tx = [int(x) for x in row[16:16 + m]]

@@ -156,11 +156,13 @@ def test_stream_cd_prune_matches_oracle(gpu, oracle, n, sig):
     ctx.close()
 
 
-def test_stream_golden_reference(gpu):
-    """Survivors and counts exactly as the reference's count_pairs22 produced them."""
+@pytest.mark.parametrize("fixture", ["streams_golden.npz", "cd_prune_golden.npz"])
+def test_stream_golden_reference(gpu, fixture):
+    """Survivors and counts exactly as the reference's count_pairs22 produced them
+    (cd_prune_golden.npz: under WZ_FH_CD_PRUNE 1, 2, 3)."""
     from bs45_quantum_explorer_gb300.hall import Context
     from bs45_quantum_explorer_gb300.stream import cd_stream
-    g = np.load(os.path.join(HERE, "golden", "streams_golden.npz"))
+    g = np.load(os.path.join(HERE, "golden", fixture))
     cases, words = g["cases"], g["words"]
     ctxs = {}
     for row in cases:
