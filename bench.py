@@ -8,9 +8,10 @@ pairs with sum C = sum D = 0) resident in HBM (268 MB of packed words, larger th
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
-Rank 0 prints one JSON line. --impl reference times the CPU restatement of the reference's
-filter (the oracle port; the reference's own sources are not on the GPU host) on all host
-threads over a bounded sample of the same workload.
+Rank 0 prints one JSON line. --impl reference times the reference's own filter on all host
+cores over the same 2^24-pair batch: its default predicate hall_ok_pair_fast from
+src/solver/wz_match.cpp compiled unmodified into oracle/_ref/libref.so (one arm per core, as
+the reference's lanes run), or, where that library was not built, the oracle restatement.
 """
 import argparse
 import json
@@ -20,6 +21,8 @@ import subprocess
 import sys
 import threading
 import time
+
+import numpy as np
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
@@ -116,71 +119,129 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_hall_rate(nthreads, target_s=10.0, seed=SEED):
-    """Times the CPU restatement of the reference's filter on all threads over a bounded
-    sample of the workload; returns (pairs/s, pairs filtered, threads, seconds, index of the
-    sample's first pair, the oracle's pass mask of the sample)."""
+def _oracle():
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pyoracle
-    from bs45_quantum_explorer_gb300.workloads import unpack_pairs
     pyoracle.build()
-    probe = 1 << 15
-    w = pyoracle.gen_hall_pairs(N, 1 << 24, seed=seed, nthreads=nthreads)  # full workload
-    X = unpack_pairs(w[:probe], N)
-    t0 = time.perf_counter()
-    pyoracle.hall_batch(N, X, nthreads=nthreads)
-    rate = probe / max(1e-9, time.perf_counter() - t0)
-    sample = int(min(1 << 24, max(probe, rate * target_s)))
-    # a contiguous slice spanning both halves of the workload (i.i.d. and mirror-quad)
-    lo = max(0, (1 << 23) - sample // 2)
-    X = unpack_pairs(w[lo:lo + sample], N)
-    # repeat the sample until about target_s of CPU work is timed (the workload holds 2^24)
-    reps, mask, t0 = 0, None, time.perf_counter()
-    while True:
+    return pyoracle
+
+
+def _ref_arms(narms, n=N, sig=SIG):
+    """The reference's own code as `narms` single-threaded arms (oracle/refarm.py), or None
+    when oracle/_ref/libref.so was not built on this machine."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import refarm
+    return refarm.Arms(narms, n, sig) if refarm.available() else None
+
+
+def cpu_hall_rate(nthreads, words, target_s=10.0):
+    """The reference's Hall filter on all host cores over the whole 2^24-pair batch, repeated
+    until about target_s of work is timed. Returns (pairs/s, pairs filtered, cores, seconds,
+    kind, sample, pass mask of one pass)."""
+    arms = _ref_arms(nthreads)
+    if arms is not None:
+        mask = np.zeros(len(words), np.uint8)
+        arms.hall_fast(words[: 1 << 16])  # the arms' angle orders adapt, as in a running lane
+        done, dt, reps = 0, 0.0, 0
+        while dt < target_s:
+            _, t = arms.hall_fast(words, out=mask if reps == 0 else None)
+            done += len(words)
+            dt += t
+            reps += 1
+        arms.close()
+        return (done / dt, done, nthreads, dt, "reference",
+                f"the whole {len(words)}-pair batch x{reps} through hall_ok_pair_fast "
+                f"(src/solver/wz_match.cpp compiled unmodified, {nthreads} single-threaded arms, "
+                f"{dt:.1f} s)", mask)
+    pyoracle = _oracle()
+    from bs45_quantum_explorer_gb300.workloads import unpack_pairs
+    X = unpack_pairs(words, N)
+    done, dt, mask = 0, 0.0, None
+    while dt < target_s:
+        t0 = time.perf_counter()
         got = pyoracle.hall_batch(N, X, nthreads=nthreads)
-        if mask is None:
-            mask = got
-        reps += 1
-        dt = time.perf_counter() - t0
-        if dt >= target_s:
-            break
-    return sample * reps / dt, sample * reps, nthreads, dt, lo, mask
+        dt += time.perf_counter() - t0
+        mask = got if mask is None else mask
+        done += len(words)
+    return (done / dt, done, nthreads, dt, "port",
+            f"the whole {len(words)}-pair batch through the oracle restatement ({dt:.1f} s, all threads)",
+            mask)
+
+
+def cpu_search_rate(ncpu, cell, seconds=10.0):
+    """The reference's C,D stream (count_pairs22 with hall_ok_pair_fast at the leaves,
+    src/solver/wz_match.cpp:678-784) on all host cores: every arm streams the same n = 42 cell
+    from its start for `seconds`, the same stretch of the DFS that the GPU search covers, so
+    the sum over arms is the reference's nodes/s on this workload."""
+    arms = _ref_arms(ncpu)
+    if arms is None:
+        return {"unavailable": "oracle/_ref/libref.so was not built on this machine"}
+    r = arms.stream_for([cell] * ncpu, seconds)
+    arms.close()
+    return {"value": r["nodes"] / r["seconds"], "unit": "DFS nodes/s", "cores": ncpu,
+            "kind": "reference", "leaves_per_s": r["leaves"] / r["seconds"],
+            "sample": f"{ncpu} single-threaded arms of count_pairs22 (src/solver/wz_match.cpp "
+                      f"compiled unmodified), each streaming the cell from its start for "
+                      f"{seconds:.0f} s ({r['nodes']} nodes, {r['leaves']} leaves, "
+                      f"{r['survivors']} survivors in all)"}
 
 
 def run_reference(args, rank, world):
     if rank != 0:
         return
-    nthreads = os.cpu_count() or 1
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import pyoracle
-    from bs45_quantum_explorer_gb300.workloads import unpack_pairs
-    pyoracle.build()
-    w = pyoracle.gen_hall_pairs(N, 1 << 24, seed=SEED, nthreads=nthreads)
-    step = 1 << 18
-    lo = (1 << 23) - step // 2
-    X = unpack_pairs(w[lo:lo + step], N)
+    import numpy as np
+    ncpu = os.cpu_count() or 1
+    pyoracle = _oracle()
+    w = pyoracle.gen_hall_pairs(N, args.pairs, seed=SEED, nthreads=ncpu)  # the same batch as ours
+    arms = _ref_arms(ncpu)
+    conj = None
+    if arms is not None:
+        kind = "reference"
+        what = (f"hall_ok_pair_fast, the reference's default predicate (src/solver/wz_match.cpp "
+                f"compiled unmodified), {ncpu} single-threaded arms, each on 1/{ncpu} of the batch")
+
+        def step():
+            arms.hall_fast(w)
+        # the WZ_FH_HALL_FAST=0 conjunction under OpenMP, once, for the record
+        nconj = min(len(w), 1 << 20)
+        _, tc = arms.hall_conj(w[:nconj], ncpu)
+        conj = {"value": nconj / tc, "unit": UNIT, "threads": ncpu,
+                "sample": f"the first {nconj} pairs of the batch",
+                "predicate": "hall_ok_single(X) && hall_ok_single(Y) && hall_ok(X,Y) (WZ_FH_HALL_FAST=0)"}
+    else:
+        kind = "port"
+        what = "the oracle restatement of the reference's FP64 test (oracle/_ref not built here), all threads"
+        from bs45_quantum_explorer_gb300.workloads import unpack_pairs
+        X = unpack_pairs(w, N)
+
+        def step():
+            pyoracle.hall_batch(N, X, nthreads=ncpu)
     for _ in range(args.warmup):
-        pyoracle.hall_batch(N, X, nthreads=nthreads)
+        step()
     times = []
     for _ in range(args.steps):
         t0 = time.perf_counter()
-        pyoracle.hall_batch(N, X, nthreads=nthreads)
+        step()
         times.append(time.perf_counter() - t0)
+    if arms is not None:
+        arms.close()
     total = sum(times)
-    value = step * args.steps / total
+    npairs = len(w)
+    value = npairs * args.steps / total
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "impl": "reference",
         "config": {"workload": "hall_filter_n42_2^24_pairs", "n": N, "sig": list(SIG),
-                   "pairs_per_step": step, "sample": "pairs [2^23-2^17, 2^23+2^17) of the 2^24-pair workload"},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port",
-                         "sample": f"{step} pairs per step"},
+                   "pairs_per_step": npairs, "sample": f"the whole {npairs}-pair batch every step"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": ncpu, "kind": kind, "sample": what},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "p50_ms": 1e3 * statistics.median(times),
         "p99_ms": 1e3 * sorted(times)[min(len(times) - 1, int(0.99 * len(times)))],
     }
+    if conj:
+        line["hall_fast_0_conjunction"] = conj
     print(json.dumps(line), flush=True)
 
 
@@ -277,9 +338,8 @@ def run_first_hit(seconds, cpu_seconds=10.0, with_cpu=True, drain_top=50000):
         out["hit"] = {"idx": res.hit_idx, "profile_rank": res.profile_rank,
                       "quad": [list(map(int, x)) for x in res.quad]}
     if with_cpu:
-        # the oracle completer on the first drained candidates of the window's first kept cell
-        sys.path.insert(0, os.path.join(ROOT, "oracle"))
-        import pyoracle
+        # the reference's completer on the first drained candidates of the window's first
+        # kept cell, on all host cores (the oracle's on one core where it was not built)
         from bs45_quantum_explorer_gb300.cells import ab_rows
         from bs45_quantum_explorer_gb300.hall import unpack
         pi = next(i for i in range(s, s + 4096) if kept[i])
@@ -289,17 +349,31 @@ def run_first_hit(seconds, cpu_seconds=10.0, with_cpu=True, drain_top=50000):
         order, _ = flat_topk(ctx, surv, len(surv), drain_top)
         cand = unpack(surv[order], FH_N)
         r = rows[off[0]:off[0] + nr[0]] if 0 < nr[0] <= 20000 else None
-        nodes, done, t1 = 0, 0, time.perf_counter()
-        while done < len(cand) and time.perf_counter() - t1 < cpu_seconds:
-            _, nd, _, _ = pyoracle.complete_ab(FH_N, FH_SIG[0], FH_SIG[1], cand[done, 0], cand[done, 1],
-                                               1 << 22, rows=r, m=m)
-            nodes += nd
-            done += 1
-        dt = time.perf_counter() - t1
-        out["cpu_baseline"] = {"value": nodes / dt, "unit": "A,B nodes/s", "cores": 1, "kind": "port",
-                               "sample": f"the oracle completer on the first {done} drained candidates "
-                                         f"of raw cell {pi} ({dt:.1f} s, budget 2^22); the reference "
-                                         "runs one lane per core"}
+        ncpu = os.cpu_count() or 1
+        arms = _ref_arms(ncpu, FH_N, FH_SIG)
+        if arms is not None:
+            rr = arms.complete_for(cand, 1 << 22, cpu_seconds, rows=r, m=m)
+            arms.close()
+            out["cpu_baseline"] = {
+                "value": rr["nodes"] / rr["seconds"], "unit": "A,B nodes/s", "cores": ncpu,
+                "kind": "reference",
+                "sample": f"fh_complete_ab (src/solver/wz_match.cpp compiled unmodified) on the "
+                          f"first {rr['done']} drained candidates of raw cell {pi}, {ncpu} "
+                          f"single-threaded arms ({rr['seconds']:.1f} s, budget 2^22, the cell's "
+                          f"allowed rows)"}
+        else:
+            pyoracle = _oracle()
+            nodes, done, t1 = 0, 0, time.perf_counter()
+            while done < len(cand) and time.perf_counter() - t1 < cpu_seconds:
+                _, nd, _, _ = pyoracle.complete_ab(FH_N, FH_SIG[0], FH_SIG[1], cand[done, 0],
+                                                   cand[done, 1], 1 << 22, rows=r, m=m)
+                nodes += nd
+                done += 1
+            dt = time.perf_counter() - t1
+            out["cpu_baseline"] = {"value": nodes / dt, "unit": "A,B nodes/s", "cores": 1,
+                                   "kind": "port",
+                                   "sample": f"the oracle completer on the first {done} drained "
+                                             f"candidates of raw cell {pi} ({dt:.1f} s, budget 2^22)"}
     ctx.close()
     return out
 
@@ -688,21 +762,27 @@ def main():
                 "tc_speedup": dt64 / dt_c,
                 "survivors_identical": bool(np.array_equal(surv64, surv_c)),
                 "same_as_50000_prefix": bool(np.array_equal(surv_c, surv[:CMP_LIMIT]))},
-            "reference_single_core": "14,736,335,258 nodes, 448,271,835 leaves, 5,613 survivors "
-                                     "in 348.9 s (42.2 M nodes/s, one Xeon core; run interrupted)"}
+        }
+        if not args.no_cpu_baseline:
+            line["search"]["cpu_baseline"] = cpu_search_rate(os.cpu_count() or 1, cell42)
         # ---- the n = 36 first-hit lane (bounded) and the serving mix ----
         line["first_hit"] = run_first_hit(args.fh_seconds, with_cpu=not args.no_cpu_baseline)
         line["serving"] = run_serving()
         if not args.no_cpu_baseline:
-            rate, samp, thr, dt, clo, cmask = cpu_hall_rate(os.cpu_count() or 1)
-            if npairs == (1 << 24):  # the oracle's sample is of the 2^24-pair workload
-                got = d_pass[clo:clo + len(cmask)].cpu().numpy()
-                line["parity_sample"].update(
-                    pairs=int(len(cmask)), false_rejects=int(((cmask == 1) & (got == 0)).sum()),
-                    false_accepts=int(((cmask == 0) & (got == 1)).sum()))
-            line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": thr, "kind": "port",
-                                    "sample": f"{samp} pairs of the same workload, the 2^24-pair batch's centre "
-                                              f"slice filtered repeatedly ({dt:.1f} s, FP64 oracle, all threads)"}
+            ncpu = os.cpu_count() or 1
+            words = d_words.cpu().numpy().view(np.uint64).reshape(-1, 2)
+            rate, samp, thr, dt, kind, what, rmask = cpu_hall_rate(ncpu, words)
+            # parity of the device mask on every pair of the batch: against the oracle (the
+            # checker) and against the reference's own decisions from the timed leg
+            from bs45_quantum_explorer_gb300.workloads import unpack_pairs
+            omask = _oracle().hall_batch(N, unpack_pairs(words, N), nthreads=ncpu)
+            got = d_pass.cpu().numpy()
+            line["parity_sample"].update(
+                pairs=int(len(omask)), false_rejects=int(((omask == 1) & (got == 0)).sum()),
+                false_accepts=int(((omask == 0) & (got == 1)).sum()),
+                differs_from_reference_arm=int((rmask != got).sum()) if kind == "reference" else None)
+            line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": thr, "kind": kind,
+                                    "sample": what}
     if rank == 0:
         print(json.dumps(line), flush=True)
     ctx.close()

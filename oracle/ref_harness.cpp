@@ -3,9 +3,12 @@
 //
 // TEST INFRASTRUCTURE ONLY. This file contains no reference code: it #includes the
 // read-only reference source at build time (path given by -DWZ_MATCH_SRC, main renamed by
-// -Dmain=ref_main) and calls its functions. Built by `make -C oracle ref` into oracle/_ref/,
-// which is never committed. The GPU host never builds it (the reference is not there).
+// -Dmain=ref_main) and calls its functions. Built by `make -C oracle ref REF=<root>` into
+// oracle/_ref/, which is never committed; bench.py's reference arm times the functions below
+// the "timed baselines" line.
 #include WZ_MATCH_SRC
+
+#include <thread>
 
 extern "C" {
 
@@ -89,6 +92,77 @@ int refh_complete(const int *C, const int *D, long long budget, int m, const sig
   }
   FH_ABP = nullptr;
   return v;
+}
+
+// ---- timed baselines (bench.py's reference arm) ----
+// Each library instance is one arm: the reference keeps its state in globals, so a caller
+// that wants several arms in one process loads several copies of this library.
+
+static void unpack_word(unsigned long long w, int L, int *out) {
+  for (int i = 0; i < L; i++) out[i] = ((w >> i) & 1ULL) ? 1 : -1;
+}
+
+// Hall decisions of the packed pairs [lo, hi) (two words per pair, bit i set <=> +1).
+// fast != 0: the reference's default predicate hall_ok_pair_fast (wz_match.cpp:143-168) on
+// this instance's adaptive angle order, single-threaded (it re-sorts a global order, so it
+// is one arm's predicate). fast == 0: the WZ_FH_HALL_FAST=0 conjunction
+// hall_ok_single(X) && hall_ok_single(Y) && hall_ok(X, Y) (wz_match.cpp:773-775) over
+// nthreads OpenMP threads. Returns the number of passing pairs; out (may be NULL) gets 0/1.
+long long refh_hall_batch(const unsigned long long *words, long long lo, long long hi, int L,
+                          int fast, int nthreads, unsigned char *out) {
+  long long passed = 0;
+  if (fast) {
+    int X[256], Y[256];
+    for (long long p = lo; p < hi; p++) {
+      unpack_word(words[2 * p], L, X);
+      unpack_word(words[2 * p + 1], L, Y);
+      const bool ok = hall_ok_pair_fast(X, L, Y, L);
+      passed += ok;
+      if (out) out[p] = ok;
+    }
+    return passed;
+  }
+#pragma omp parallel for schedule(static, 4096) num_threads(nthreads) reduction(+ : passed)
+  for (long long p = lo; p < hi; p++) {
+    int X[256], Y[256];
+    unpack_word(words[2 * p], L, X);
+    unpack_word(words[2 * p + 1], L, Y);
+    const bool ok = hall_ok_single(X, L) && hall_ok_single(Y, L) && hall_ok(X, L, Y, L);
+    passed += ok;
+    if (out) out[p] = ok;
+  }
+  return passed;
+}
+
+// count_pairs22 on one C,D cell (the arm's stream, hall_ok_pair_fast at the leaves) for at
+// most `seconds` of wall time, through the reference's own cooperative stop flag. Returns
+// the survivors; nodes/leaves/ok are the cell's counts so far.
+long long refh_stream_for(int L, const int *tx, const int *ty, int m, int pinX, int pinY,
+                          double seconds, long long *nodes, long long *leaves, long long *ok) {
+  G_STREAM_REV = false;
+  G_ENDPOS = false;
+  G_CD_PRUNE = 0;
+  G_HALL_FAST = 1;
+  vector<int> vx(tx, tx + m), vy(ty, ty + m);
+  atomic<bool> stop(false), done(false);
+  std::thread timer([&] {
+    const auto t_end = chrono::steady_clock::now() + chrono::duration<double>(seconds);
+    while (!done.load() && chrono::steady_clock::now() < t_end)
+      std::this_thread::sleep_for(chrono::milliseconds(2));
+    stop.store(true);
+  });
+  long long written = 0;
+  function<void(const vector<int> &, const vector<int> &)> sink =
+      [&](const vector<int> &, const vector<int> &) { written++; };
+  long long lv = 0, okc = 0;
+  unsigned long long n0 = G_CD_NODES;
+  count_pairs22(L, vx, vy, false, pinX != 0, pinY != 0, lv, okc, &sink, m, &stop);
+  done.store(true);
+  timer.join();
+  *nodes = (long long)(G_CD_NODES - n0);
+  *leaves = lv;
+  *ok = okc;
+  return written;
 }
 
 void refh_outer_tables(unsigned char *o2, unsigned char *o3) {

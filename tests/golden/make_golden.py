@@ -2,14 +2,14 @@
 """Generates the golden fixtures in this folder from the reference itself.
 
 Run on a machine that holds the reference sources (DanielGord0n/BS45_Quantum_Explorer at
-REF, default /root/reference) after `make -C oracle ref`, which compiles the reference's own
+REF, given on the command line) after `make -C oracle ref REF=...`, which compiles the reference's own
 src/solver/wz_match.cpp, unmodified, with its production flags into oracle/_ref/ (the binary,
 and a harness library that exposes hall_ok_pair_fast, count_pairs22, fh_complete_ab, npaf_at
 and autocorr_key). Every expected value below is computed by that reference code, except the
 BS(7,6) full set, which is a numpy brute force over all 2^26 (A,B) x ... pairs as the
 reference's own test_orbit_q_retention.py does it (join of pair autocorrelations).
 
-    python tests/golden/make_golden.py [REF]           # everything below but the two that follow
+    python tests/golden/make_golden.py REF             # everything below but the two that follow
     python tests/golden/make_golden.py REF ab          # ab_streams_golden.npz
     python tests/golden/make_golden.py REF cdprune     # cd_prune_golden.npz
 
@@ -29,7 +29,9 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+if len(sys.argv) < 2:
+    sys.exit("usage: make_golden.py REF [ab|cdprune]   (REF: root of the reference repository)")
+REF = sys.argv[1]
 sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
 

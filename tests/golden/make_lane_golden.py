@@ -67,14 +67,14 @@ def cellsize_lines(out):
     return rows
 
 
-def run(n, sig, settings, tmp, ckdir=None):
+def run(n, sig, settings, tmp, ckdir=None, timeout=600):
     env = {k: v for k, v in os.environ.items() if not k.startswith(("WZ_", "FH_"))}
     env.update({k: str(v) for k, v in {**BASE, **settings}.items()})
     dump = os.path.join(tmp, "dump.txt")
     env["WZ_FH_DUMP"] = dump
     if ckdir:
         env["WZ_FH_CKPT_DIR"] = ckdir
-    p = subprocess.run([REF_BIN, str(n), *map(str, sig)], env=env, capture_output=True, text=True, timeout=600)
+    p = subprocess.run([REF_BIN, str(n), *map(str, sig)], env=env, capture_output=True, text=True, timeout=timeout)
     data = open(dump, "rb").read() if os.path.exists(dump) else b""
     return p.returncode, p.stdout, hashlib.sha256(data).hexdigest(), len(data)
 
