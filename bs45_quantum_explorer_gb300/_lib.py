@@ -9,7 +9,9 @@ import os
 from .build import LIB
 
 BS_OK = 0
+BS_STOPPED, BS_WALLED = 1, 2  # partial results: the stop flag / the stream's wall limit
 ERRORS = {
+    1: "stopped by the context's stop flag", 2: "stream stopped by its wall limit",
     -1: "bad argument", -2: "CUDA runtime error", -3: "out of memory",
     -4: "device wait limit reached", -5: "internal consistency check failed",
     -6: "output capacity exceeded", -7: "no sm_103 CUDA device",
@@ -43,7 +45,7 @@ class StreamOpts(C.Structure):
                 ("cd_prune", C.c_int32), ("hall_mode", C.c_int32), ("ab_side", C.c_int32),
                 ("target_prefixes", C.c_longlong), ("leaf_chunk", C.c_longlong),
                 ("survivor_cap", C.c_longlong), ("limit", C.c_longlong),
-                ("round_us", C.c_longlong)]
+                ("round_us", C.c_longlong), ("wall_sec", C.c_double)]
 
 
 class CellStats(C.Structure):
@@ -63,7 +65,7 @@ class AbCand(C.Structure):
 class AbOpts(C.Structure):
     _fields_ = [("budget", C.c_longlong), ("outer_k", C.c_int32), ("early", C.c_int32),
                 ("canon", C.c_int32), ("m", C.c_int32), ("first_hit", C.c_int32),
-                ("reserved", C.c_int32), ("max_seconds", C.c_double)]
+                ("a2", C.c_int32), ("max_seconds", C.c_double)]
 
 
 _lib = None
@@ -77,6 +79,7 @@ SIGNATURES = {
     "bs_ctx_retarget": (C.c_int, [C.c_void_p] + [C.c_int] * 5),
     "bs_ctx_set_stream": (C.c_int, [C.c_void_p, C.c_void_p]),
     "bs_ctx_device_status": (C.c_int, [C.c_void_p]),
+    "bs_ctx_stop_flag": (C.POINTER(C.c_int32), [C.c_void_p]),
     "bs_hall_filter_batch": (C.c_int, [C.c_void_p, C.c_void_p, C.c_longlong, C.c_int, C.c_void_p,
                                        C.POINTER(HallStats)]),
     "bs_hall_filter_packed": (C.c_int, [C.c_void_p, C.c_void_p, C.c_longlong, C.c_int, C.c_void_p,

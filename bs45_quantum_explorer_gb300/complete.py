@@ -9,7 +9,7 @@ import ctypes as C
 
 import numpy as np
 
-from ._lib import AbCand, AbOpts, check, lib
+from ._lib import BS_STOPPED, AbCand, AbOpts, check, lib
 from .hall import pack
 
 
@@ -33,11 +33,12 @@ assert AB_CAND.itemsize == C.sizeof(AbCand)
 
 
 def complete_ab(ctx, cands, budget, rows_per_cand=None, m=6, outer_k=3, early=True, canon=True,
-                first_hit=False, max_seconds=0.0, rows=None):
+                first_hit=False, max_seconds=0.0, rows=None, a2=0):
     """cands: int8 [k, 2, n] (C, D) or uint64 words [k, 2]. Allowed A,B rows (int8 [r, 16]):
     `rows` shared by every candidate (one cell's list), or rows_per_cand, a list of arrays
-    (empty = unconstrained); neither: unconstrained.
-    Returns (verdict int32 [k], nodes int64 [k], A int8 [k, n+1], B int8 [k, n+1])."""
+    (empty = unconstrained); neither: unconstrained. a2 = 2: WZ_FH_A2=2, the A2 row prune.
+    Returns (verdict int32 [k], nodes int64 [k], A int8 [k, n+1], B int8 [k, n+1]); when the
+    context's stop flag stops the batch, the candidates it did not finish have verdict -1."""
     cands = np.asarray(cands)
     words = cands if cands.dtype == np.uint64 else pack(cands)
     words = np.ascontiguousarray(words.reshape(-1, 2), np.uint64)
@@ -60,14 +61,15 @@ def complete_ab(ctx, cands, budget, rows_per_cand=None, m=6, outer_k=3, early=Tr
         all_rows = np.concatenate(parts) if parts else np.zeros((1, 16), np.int8)
     all_rows = np.ascontiguousarray(all_rows)
     opt = AbOpts(budget=budget, outer_k=outer_k, early=int(early), canon=int(canon), m=m,
-                 first_hit=int(first_hit), reserved=0, max_seconds=max_seconds)
+                 first_hit=int(first_hit), a2=int(a2), max_seconds=max_seconds)
     n1 = ctx.n + 1
     verdict = np.zeros(max(1, k), np.int32)
     nodes = np.zeros(max(1, k), np.int64)
     A = np.zeros((max(1, k), n1), np.int8)
     B = np.zeros((max(1, k), n1), np.int8)
-    check(lib().bs_complete_ab_batch(ctx.h, C.cast(arr.ctypes.data, C.POINTER(AbCand)), k,
-                                     all_rows.ctypes.data, off, C.byref(opt), verdict.ctypes.data,
-                                     nodes.ctypes.data, A.ctypes.data, B.ctypes.data),
-          "bs_complete_ab_batch")
+    rc = lib().bs_complete_ab_batch(ctx.h, C.cast(arr.ctypes.data, C.POINTER(AbCand)), k,
+                                    all_rows.ctypes.data, off, C.byref(opt), verdict.ctypes.data,
+                                    nodes.ctypes.data, A.ctypes.data, B.ctypes.data)
+    if rc != BS_STOPPED:  # stopped by the context's stop flag: candidates not run read -1
+        check(rc, "bs_complete_ab_batch")
     return verdict[:k], nodes[:k], A[:k], B[:k]

@@ -9,12 +9,21 @@
 
 #define BS_MAXL 64          // longest sequence held in one packed word
 #define BS_TC_COLS 208      // tensor-core N: 104 Re columns + 104 Im columns
-#define BS_TC_IM0 104       // first Im column
+#define BS_TC_IM0 104       // first Im column of a dumped accumulator row
 #define BS_TC_NANG 101      // unique Hall angles (j = 1..100 and 200)
 
 // One tensor-core table image: 208 rows (columns of the DFT) x 64 halves, stored in the
-// 128-byte-swizzled K-major layout the UMMA shared-memory descriptor reads.
+// 128-byte-swizzled K-major layout the UMMA shared-memory descriptor reads. The 104 angle
+// slots (101 unique angles, 3 zero rows) form two blocks, each a contiguous run of rows
+// [cos of its angles][sin of its angles] that one MMA of N = 2 x (angles in the block) reads:
+// block 0 = angles 0..63 (rows 0..127), block 1 = angles 64..103 (rows 128..207).
 #define BS_TC_PART_BYTES (BS_TC_COLS * 128)
+#define BS_TC_BLK0 64
+#define BS_TC_BLK1 40
+static inline __host__ __device__ int bs_tc_row(int u, int sin_part) {
+  return u < BS_TC_BLK0 ? (sin_part ? BS_TC_BLK0 + u : u)
+                        : 2 * BS_TC_BLK0 + (sin_part ? BS_TC_BLK1 : 0) + (u - BS_TC_BLK0);
+}
 
 struct bs_hall_tc_form {
   int nparts;            // 1 (fp16) or 2 (bf16 hi + lo)
@@ -61,6 +70,8 @@ struct bs_ctx {
   double timed_ms;          // accumulated duration of the timed kernels
   long long timed_launches; // launches of the timed kernels
   long long launches;       // every kernel this context has launched
+  volatile int32_t *h_stop;  // the stop flag (bs_ctx_stop_flag): mapped pinned host memory
+  int32_t *d_stop;           // its device address
   void *stream_bufs;        // C,D stream buffers (cd_stream.cu)
   void *ab_bufs;            // A,B completion buffers (complete.cu)
 };

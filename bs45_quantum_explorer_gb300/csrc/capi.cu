@@ -52,6 +52,8 @@ extern "C" int bs_version(void) { return 100; }
 extern "C" const char *bs_strerror(int code) {
   switch (code) {
     case BS_OK: return "ok";
+    case BS_STOPPED: return "stopped by the context's stop flag (partial result)";
+    case BS_WALLED: return "stream stopped by its wall limit (partial result)";
     case BS_ERR_ARG: return "bad argument";
     case BS_ERR_CUDA: return "CUDA runtime error";
     case BS_ERR_NOMEM: return "out of memory";
@@ -114,7 +116,7 @@ static int build_tc_form(bs_ctx *ctx, const double *ct, const double *st, int mo
     int j = angle_of(u);
     for (int part_kind = 0; part_kind < 2; part_kind++) {  // 0 = cos (Re), 1 = sin (Im)
       const double *tab = part_kind ? st : ct;
-      int col = part_kind ? BS_TC_IM0 + u : u;
+      int col = bs_tc_row(u, part_kind);
       double esum = 0.0;
       for (int i = 0; i < L; i++) {
         double t = tab[(size_t)j * (ctx->n1) + i];
@@ -265,6 +267,17 @@ extern "C" int bs_ctx_create(int n, int a, int b, int c, int d, int device, bs_c
   if (e1 == cudaSuccess) e1 = cudaMalloc(&ctx->d_status, sizeof(int));
   if (e1 == cudaSuccess) e1 = cudaMemset(ctx->d_status, 0, sizeof(int));
   if (e1 == cudaSuccess) e1 = cudaMalloc(&ctx->d_count, sizeof(unsigned long long) * 8);
+  if (e1 == cudaSuccess) {
+    void *h = nullptr;
+    e1 = cudaHostAlloc(&h, sizeof(int32_t), cudaHostAllocMapped);
+    if (e1 == cudaSuccess) {
+      ctx->h_stop = (volatile int32_t *)h;
+      *ctx->h_stop = 0;
+      void *dp = nullptr;
+      e1 = cudaHostGetDevicePointer(&dp, h, 0);
+      ctx->d_stop = (int32_t *)dp;
+    }
+  }
   if (e1 != cudaSuccess) rc = bs_cuda_fail(e1);
   if (rc == BS_OK) rc = load_tables(ctx, n, a, b, c, d);
   if (rc != BS_OK) { bs_ctx_destroy(ctx); return rc; }
@@ -303,6 +316,7 @@ extern "C" void bs_ctx_destroy(bs_ctx *ctx) {
   bs_stream_free(ctx);
   bs_ab_free(ctx);
   if (ctx->h_pinned) cudaFreeHost(ctx->h_pinned);
+  if (ctx->h_stop) cudaFreeHost((void *)ctx->h_stop);
   if (ctx->ev[0])
     for (int i = 0; i < 2 * 512; i++) cudaEventDestroy(ctx->ev[i]);
   if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
@@ -314,6 +328,8 @@ extern "C" int bs_ctx_set_stream(bs_ctx *ctx, void *s) {
   ctx->stream = s ? (cudaStream_t)s : ctx->own_stream;
   return BS_OK;
 }
+
+extern "C" volatile int32_t *bs_ctx_stop_flag(bs_ctx *ctx) { return ctx ? ctx->h_stop : nullptr; }
 
 extern "C" int bs_ctx_device_status(bs_ctx *ctx) {
   if (!ctx) return BS_ERR_ARG;

@@ -899,7 +899,11 @@ extern "C" int bs_cd_stream(bs_ctx *ctx, const bs_cell *cells, int ncells, const
   int k_refine = (half - deepest >= 6) ? 2 : 0;
   long long have = 0;
   static const bool trace = getenv("BS_STREAM_TRACE") != nullptr;  // per-wave figures on stderr
-  while (pos < ncoarse && !(limit && have >= limit)) {
+  // the stop flag and the wall limit are checked between launches (each at most ROUND_NS)
+  int stop_rc = 0;
+  auto t_last_surv = std::chrono::steady_clock::now();
+  unsigned long long wave_surv_seen = 0;
+  while (pos < ncoarse && !(limit && have >= limit) && !stop_rc) {
     const long long take = std::min<long long>(std::max<long long>(1, wave_width), ncoarse - pos);
     fine.clear();
     for (long long i = pos; i < pos + take; i++) {
@@ -915,6 +919,7 @@ extern "C" int bs_cd_stream(bs_ctx *ctx, const bs_cell *cells, int ncells, const
     CK(cudaMemsetAsync(B->counters, 0, sizeof(unsigned long long) * 8, s));
     const auto t_wave = std::chrono::steady_clock::now();
     int nsaved = 0, cur = 0, rounds = 0, splits = 0;
+    wave_surv_seen = 0;
     for (;;) {
       CK(cudaMemsetAsync(B->nsaved, 0, sizeof(unsigned), s));
       CK(cudaMemsetAsync(B->stop, 0, sizeof(int), s));
@@ -937,14 +942,32 @@ extern "C" int bs_cd_stream(bs_ctx *ctx, const bs_cell *cells, int ncells, const
       dfs_kernel<<<grid, block, 0, s>>>(P);
       bs_timed_end(ctx);
       CK(cudaGetLastError());
-      unsigned long long leaf_count = 0, nextp = 0;
+      unsigned long long leaf_count = 0, nextp = 0, wave_surv = 0;
       unsigned nsv = 0;
       CK(cudaMemcpyAsync(&leaf_count, B->counters + 1, sizeof leaf_count, cudaMemcpyDeviceToHost, s));
       CK(cudaMemcpyAsync(&nextp, B->counters, sizeof nextp, cudaMemcpyDeviceToHost, s));
+      CK(cudaMemcpyAsync(&wave_surv, B->counters + 2, sizeof wave_surv, cudaMemcpyDeviceToHost, s));
       CK(cudaMemcpyAsync(&nsv, B->nsaved, sizeof nsv, cudaMemcpyDeviceToHost, s));
       CK(cudaStreamSynchronize(s));
       rounds++;
-      if ((int)nsv > saved_cap) return BS_ERR_INTERNAL;
+      if ((long long)nsv > walkers) {
+        // A group suspends at most once per launch, so a launch saves at most `walkers` walks
+        // (saved_cap = 8 x walkers); anything more is a broken invariant, reported loudly.
+        fprintf(stderr, "[bs_cd_stream] saved-walk invariant broken: nsaved=%u walkers=%lld "
+                        "saved_cap=%d nsaved_in=%d round=%d splits=%d nprefix=%lld\n",
+                nsv, walkers, saved_cap, nsaved, rounds, splits, nprefix);
+        return BS_ERR_INTERNAL;
+      }
+      if (wave_surv > wave_surv_seen) {  // survivors found since the last look (wall clock)
+        wave_surv_seen = wave_surv;
+        t_last_surv = std::chrono::steady_clock::now();
+      }
+      if (*ctx->h_stop) stop_rc = BS_STOPPED;
+      else if (opt->wall_sec > 0 &&
+               std::chrono::duration<double>(std::chrono::steady_clock::now() - t_last_surv).count() >
+                   opt->wall_sec)
+        stop_rc = BS_WALLED;
+      if (stop_rc) break;  // this wave is abandoned: its survivors are not a prefix
       long long nleaf = (long long)std::min<unsigned long long>(leaf_count, (unsigned long long)leaf_cap);
       if (nleaf > 0) {
         int r2 = bs_hall_dev_len(ctx, B->leaf_words, nleaf, hall_mode, B->leaf_pass, L);
@@ -986,6 +1009,7 @@ extern "C" int bs_cd_stream(bs_ctx *ctx, const bs_cell *cells, int ncells, const
       }
     }
 
+    if (stop_rc) break;
     // ---- the wave's survivors, in stream order ----
     unsigned long long nsurv = 0;
     int status = 0;
@@ -1021,6 +1045,7 @@ extern "C" int bs_cd_stream(bs_ctx *ctx, const bs_cell *cells, int ncells, const
         res_cell.push_back(wcell[order[i]]);
       }
       have += keep;
+      t_last_surv = std::chrono::steady_clock::now();
     }
 
     // ---- size the next wave from what this one cost ----
@@ -1049,6 +1074,17 @@ extern "C" int bs_cd_stream(bs_ctx *ctx, const bs_cell *cells, int ncells, const
   }
 
   // ---- results ----
+  if (stop_rc) {  // the counts of the part explored, the abandoned wave included
+    int status = 0;
+    CK(cudaMemcpyAsync(cs_prev.data(), B->cell_stats, sizeof(unsigned long long) * 3 * ncells,
+                       cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(&status, ctx->d_status, sizeof status, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    if (status) {
+      cudaMemsetAsync(ctx->d_status, 0, sizeof(int), s);
+      return status;
+    }
+  }
   if (stats)
     for (int ci = 0; ci < ncells; ci++) {
       stats[ci].nodes = host_nodes[ci] + (long long)cs_prev[ci];
@@ -1061,5 +1097,5 @@ extern "C" int bs_cd_stream(bs_ctx *ctx, const bs_cell *cells, int ncells, const
     memcpy(out_words, res_words.data(), sizeof(uint64_t) * 2 * have);
     if (out_cell) memcpy(out_cell, res_cell.data(), sizeof(uint32_t) * have);
   }
-  return BS_OK;
+  return stop_rc ? stop_rc : BS_OK;
 }

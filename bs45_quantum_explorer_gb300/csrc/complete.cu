@@ -12,6 +12,8 @@
 #include <stdint.h>
 #include <string.h>
 
+#include <algorithm>
+#include <utility>
 #include <vector>
 
 #include "bsfh_internal.cuh"
@@ -24,8 +26,9 @@ constexpr int AB_MAXLV = 34; // levels 0..half (n1 <= 64)
 
 struct AbCandDev {
   uint64_t c, d;
-  long long row_off;
-  int nrows, pad;
+  long long mask_off;  // first word of the candidate's row-set masks (see AbParams::masks)
+  long long row_off;   // its first row in AbParams::rows8 (the A2 test reads the rows)
+  int nrows, W;        // allowed rows of its cell, 64-bit words per row bitset
 };
 
 struct AbParams {
@@ -35,10 +38,20 @@ struct AbParams {
   long long max_cycles;
   const AbCandDev *cands;
   long long ncand;
-  const uint64_t *roww;  // allowed rows as 4 words each (see RowBox)
-  uint64_t m7, mb;       // bit 7 / all bits of each used class byte
-  uint16_t *stacks;  // per warp slot: levels 1..half, maxrows entries each
-  int maxrows;
+  // Allowed rows as bitsets. For each row set (a cell's rows) and class c, four families of
+  // W-word row masks indexed by a value v in [-T-1, T+1] (vi = v + T + 1, V = 2T + 3 values):
+  // kind 0 rows with k_c >= v, 1 rows with k_c <= v, 2 rows with r_c >= v, 3 rows with
+  // r_c <= v, at masks[mask_off + ((c * 4 + kind) * V + vi) * W].
+  const uint64_t *masks;
+  int T, V;
+  uint64_t *bits;   // per warp slot: levels 0..half, Wcap words each (the surviving rows)
+  int Wcap;
+  // WZ_FH_A2 = 2 (wz_match.cpp:977-1047): each row that passes the box is kept only if its
+  // residuals are reachable block by block with the quads left (a2_row_ok)
+  int a2, a2_nblk;
+  const int8_t *rows8;     // the rows (k[8], r[8]) of every row set, for the A2 test
+  int8_t a2_r[8], a2_s[8], a2_mid[8];
+  uint8_t a2_cnt[AB_MAXLV + 2][8];  // quads left in block b from depth p on
   const uint8_t *outer2, *outer3;
   unsigned long long *next;
   long long *hit_min;
@@ -182,31 +195,51 @@ __device__ __forceinline__ int next_quad(const AbParams &P, int d, int k, unsign
   return 8;
 }
 
-// An allowed row (k, r) as four words of biased class bytes: k+64, 64-k, r+64, 64-r. A level's
-// box test |k_c - pa_c| <= rem_c, |r_c - pb_c| <= rem_c (wz_match.cpp:1055-1075) then reads
-// k_c - pa_c + rem_c + 128 >= 128 and pa_c - k_c + rem_c + 128 >= 128 (and the same for r) off
-// bit 7 of four byte-wise sums: every byte stays in [84, 194], so no carry crosses a class.
-struct RowBox { uint64_t k1, k2, r1, r2; };
-
-__device__ __forceinline__ RowBox row_box_of(const Uni &u, const AbParams &P) {
-  RowBox b = {0, 0, 0, 0};
-  for (int c = 0; c < 6; c++) {
-    if (c >= P.m) break;
-    const int rem = P.tic[c] - fld(u.plc, c), pa = fld(u.pa, c), pb = fld(u.pb, c);
-    b.k1 |= (uint64_t)(rem - pa + 64) << (8 * c);
-    b.k2 |= (uint64_t)(rem + pa + 64) << (8 * c);
-    b.r1 |= (uint64_t)(rem - pb + 64) << (8 * c);
-    b.r2 |= (uint64_t)(rem + pb + 64) << (8 * c);
+// The level filter of the allowed rows (fh_abp_filter, wz_match.cpp:1055-1075): a row
+// survives while |k_c - pa_c| <= rem_c and |r_c - pb_c| <= rem_c for every class c. Placing
+// the mirror positions d and L-1-d changes pa, pb and rem of their two classes only, and the
+// parent's list already meets the box of every other class, so the child's list is the
+// parent's AND the four range masks of each of the two classes.
+__device__ __forceinline__ const uint64_t *mask_of(const AbParams &P, const AbCandDev &cd, int c,
+                                                   int kind, int v) {
+  v = v < -P.T - 1 ? -P.T - 1 : (v > P.T + 1 ? P.T + 1 : v);
+  return P.masks + cd.mask_off + ((size_t)(c * 4 + kind) * P.V + (size_t)(v + P.T + 1)) * cd.W;
+}
+// a2_self_ok / a2_row_ok (wz_match.cpp:1017-1038): residuals (u, v) of a self-reflected block
+// reachable with q quads of (+-2, +-2) or (0, 0); of a block {r, s}, H (ur, vr, us, vs) / 4
+// integral with an L1 norm of the same parity as q and at most q.
+__device__ __forceinline__ bool a2_self(int u, int v, int q) {
+  if ((u | v) & 1) return false;
+  if (u > 2 * q || -u > 2 * q || v > 2 * q || -v > 2 * q) return false;
+  return ((u - v) & 3) == 0;
+}
+__device__ __forceinline__ bool a2_row(const AbParams &P, const int8_t *row, const int *pa,
+                                       const int *pb, int p) {
+  for (int b = 0; b < P.a2_nblk; b++) {
+    const int r = P.a2_r[b], s = P.a2_s[b], q = P.a2_cnt[p][b];
+    const int ur = row[r] - pa[r], vr = row[8 + r] - pb[r];
+    if (r != s) {
+      const int us = row[s] - pa[s], vs = row[8 + s] - pb[s];
+      const int t0 = ur + vr + us + vs, t1 = ur - vr + us - vs, t2 = ur + vr - us - vs,
+                t3 = ur - vr - us + vs;
+      if ((t0 | t1 | t2 | t3) & 3) return false;
+      const int l1 = (absi(t0) + absi(t1) + absi(t2) + absi(t3)) >> 2;
+      if (l1 > q || ((q - l1) & 1)) return false;
+    } else if (P.a2_mid[b]) {
+      if (!a2_self(ur - 1, vr - 1, q) && !a2_self(ur - 1, vr + 1, q) &&
+          !a2_self(ur + 1, vr - 1, q) && !a2_self(ur + 1, vr + 1, q))
+        return false;
+    } else if (!a2_self(ur, vr, q)) {
+      return false;
+    }
   }
-  return b;
+  return true;
 }
-__device__ __forceinline__ bool row_box(const uint64_t *row, const RowBox &b, const AbParams &P) {
-  const uint64_t t = (row[0] + b.k1) & (row[1] + b.k2) & (row[2] + b.r1) & (row[3] + b.r2);
-  return (t & P.m7) == P.m7;
-}
-// the leaf test of a row: its class sums equal the placed ones (pa, pb hold sum + 64)
-__device__ __forceinline__ bool row_exact(const uint64_t *row, const Uni &u, const AbParams &P) {
-  return ((row[0] ^ u.pa) & P.mb) == 0 && ((row[2] ^ u.pb) & P.mb) == 0;
+
+// all rows of the cell, as bitset word w
+__device__ __forceinline__ uint64_t all_rows(int w, int nrows) {
+  const int lo = w * 64;
+  return nrows - lo >= 64 ? ~0ULL : ((1ULL << (nrows - lo)) - 1ULL);
 }
 
 __global__ void __launch_bounds__(32 * AB_WARPS) ab_kernel(AbParams P) {
@@ -214,10 +247,11 @@ __global__ void __launch_bounds__(32 * AB_WARPS) ab_kernel(AbParams P) {
   const long long slot = (long long)blockIdx.x * AB_WARPS + wib;
   __shared__ uint32_t s_ctrl[AB_WARPS][AB_MAXLV];  // k | omask << 4 | ties << 12
   __shared__ int s_res[AB_WARPS][AB_MAXLV];        // early-check residual of the level
-  __shared__ int s_len[AB_WARPS][AB_MAXLV];        // allowed-row list length of the level
+  __shared__ int s_lo[AB_WARPS][AB_MAXLV];         // the level's row bitset: nonzero words
+  __shared__ int s_hi[AB_WARPS][AB_MAXLV];         // lie in [lo, hi)
   uint32_t *ctrl = s_ctrl[wib];
-  int *res = s_res[wib], *len = s_len[wib];
-  uint16_t *stk = P.stacks + (size_t)slot * P.half * P.maxrows;
+  int *res = s_res[wib], *wlo = s_lo[wib], *whi = s_hi[wib];
+  uint64_t *lv = P.bits + (size_t)slot * (P.half + 1) * P.Wcap;
   const int L = P.L, n = P.n, half = P.half, m = P.m;
 
   while (true) {
@@ -230,7 +264,7 @@ __global__ void __launch_bounds__(32 * AB_WARPS) ab_kernel(AbParams P) {
       continue;
     }
     const AbCandDev cd = P.cands[idx];
-    const uint64_t *rows = cd.nrows > 0 ? P.roww + 4 * (size_t)cd.row_off : nullptr;
+    const bool rows = cd.nrows > 0;
     // targets -N_CD(s) and the prefilter of wz_match.cpp:1300-1308
     Lanes v;
     v.s0 = (lane + 1 <= n) ? lane + 1 : 0;
@@ -267,7 +301,8 @@ __global__ void __launch_bounds__(32 * AB_WARPS) ab_kernel(AbParams P) {
     if (lane == 0) {
       ctrl[0] = 0u | (0xFFu << 4) | (5u << 12);  // ties: a_tied = b_tied = 1
       res[0] = 0;
-      len[0] = cd.nrows;
+      wlo[0] = 0;
+      whi[0] = cd.W;
     }
     __syncwarp();
     unsigned long long steps = 0;
@@ -284,15 +319,19 @@ __global__ void __launch_bounds__(32 * AB_WARPS) ab_kernel(AbParams P) {
           bool eq = (!v.s0 || v.D0 == v.t0) && (!v.s1 || v.D1 == v.t1);
           if (!__all_sync(FULL_MASK, eq)) return false;
           if (rows) {
-            const int cnt = len[half];
-            const uint16_t *lst = stk + (size_t)(half - 1) * P.maxrows;
+            // fh_abp_leaf_ok: a row of the last list equals the placed class sums exactly
+            const uint64_t *lst = lv + (size_t)half * P.Wcap;
             bool any = false;
-            for (int base = 0; base < cnt && !any; base += 32) {
-              int t = base + lane;
-              bool hit = t < cnt && row_exact(rows + 4 * (size_t)lst[t], u, P);
-              any = __any_sync(FULL_MASK, hit);
+            for (int w = wlo[half] + lane; w < whi[half]; w += 32) {
+              uint64_t x = lst[w];
+              for (int c = 0; c < m; c++) {
+                const int pa = fld(u.pa, c), pb = fld(u.pb, c);
+                x &= mask_of(P, cd, c, 0, pa)[w] & mask_of(P, cd, c, 1, pa)[w] &
+                     mask_of(P, cd, c, 2, pb)[w] & mask_of(P, cd, c, 3, pb)[w];
+              }
+              any |= x != 0;
             }
-            if (!any) return false;
+            if (!__any_sync(FULL_MASK, any)) return false;
           }
           return true;
         };
@@ -371,27 +410,46 @@ __global__ void __launch_bounds__(32 * AB_WARPS) ab_kernel(AbParams P) {
       }
       if (!prune && rows) {
         // fh_abp_filter(d): the level-(d+1) list from the level-d list (all rows at d = 0)
-        const int srclen = (d == 0) ? cd.nrows : len[d];
-        const uint16_t *src = stk + (size_t)(d - 1) * P.maxrows;
-        uint16_t *dst = stk + (size_t)d * P.maxrows;
-        const RowBox box = row_box_of(u, P);
-        int cnt = 0;
-        for (int base = 0; base < srclen; base += 32) {
-          int t = base + lane;
-          int ri = 0;
-          bool ok = false;
-          if (t < srclen) {
-            ri = (d == 0) ? t : src[t];
-            ok = row_box(rows + 4 * (size_t)ri, box, P);
+        const int c1 = d % m, c2 = (L - 1 - d) % m;
+        const int r1 = P.tic[c1] - fld(u.plc, c1), pa1 = fld(u.pa, c1), pb1 = fld(u.pb, c1);
+        const int r2 = P.tic[c2] - fld(u.plc, c2), pa2 = fld(u.pa, c2), pb2 = fld(u.pb, c2);
+        const uint64_t *k1a = mask_of(P, cd, c1, 0, pa1 - r1), *k1b = mask_of(P, cd, c1, 1, pa1 + r1);
+        const uint64_t *q1a = mask_of(P, cd, c1, 2, pb1 - r1), *q1b = mask_of(P, cd, c1, 3, pb1 + r1);
+        const uint64_t *k2a = mask_of(P, cd, c2, 0, pa2 - r2), *k2b = mask_of(P, cd, c2, 1, pa2 + r2);
+        const uint64_t *q2a = mask_of(P, cd, c2, 2, pb2 - r2), *q2b = mask_of(P, cd, c2, 3, pb2 + r2);
+        const uint64_t *src = lv + (size_t)d * P.Wcap;
+        uint64_t *dst = lv + (size_t)(d + 1) * P.Wcap;
+        int pa[8], pb[8];
+        if (P.a2)
+          for (int c = 0; c < 8; c++) {
+            pa[c] = c < m ? fld(u.pa, c) : 0;
+            pb[c] = c < m ? fld(u.pb, c) : 0;
           }
-          unsigned ball = __ballot_sync(FULL_MASK, ok);
-          if (ok) dst[cnt + __popc(ball & ((1u << lane) - 1u))] = (uint16_t)ri;
-          cnt += __popc(ball);
+        int mylo = 1 << 30, myhi = -1;
+        for (int w = wlo[d] + lane; w < whi[d]; w += 32) {
+          uint64_t x = d == 0 ? all_rows(w, cd.nrows) : src[w];
+          x &= k1a[w] & k1b[w] & q1a[w] & q1b[w];
+          if (c2 != c1) x &= k2a[w] & k2b[w] & q2a[w] & q2b[w];
+          if (P.a2)  // A2 on the rows that passed the box, at depth d + 1
+            for (uint64_t y = x; y; y &= y - 1) {
+              const int bit = __ffsll((long long)y) - 1;
+              if (!a2_row(P, P.rows8 + 16 * (cd.row_off + (long long)w * 64 + bit), pa, pb, d + 1))
+                x &= ~(1ULL << bit);
+            }
+          dst[w] = x;
+          if (x) {
+            mylo = min(mylo, w);
+            myhi = w;
+          }
+        }
+        const int nlo = __reduce_min_sync(FULL_MASK, mylo), nhi = __reduce_max_sync(FULL_MASK, myhi);
+        __syncwarp();
+        if (lane == 0) {
+          wlo[d + 1] = nlo;
+          whi[d + 1] = nhi + 1;
         }
         __syncwarp();
-        if (lane == 0) len[d + 1] = cnt;
-        __syncwarp();
-        prune = (cnt == 0);
+        prune = nhi < 0;
       }
       if (prune) {
         unplace(u, v, L - 1 - d, L, m);
@@ -509,14 +567,20 @@ struct OuterTables {
 struct AbBufs {
   uint8_t *outer = nullptr;  // o2 then o3
   AbCandDev *cands = nullptr; long long cand_cap = 0;
-  uint64_t *rows = nullptr; long long rows_cap = 0;  // 4 words per row
-  uint16_t *stacks = nullptr; long long stack_cap = 0;
+  uint64_t *masks = nullptr; long long masks_cap = 0;  // row-set masks (AbParams::masks)
+  uint64_t *bits = nullptr; long long bits_cap = 0;    // per-warp level bitsets
+  int8_t *rows8 = nullptr; long long rows8_cap = 0;     // the rows themselves (A2 test)
+  // the row sets whose masks are on the device: the rows they were built from, their
+  // (row_off, nrows) and mask offsets, and the modulus and length
+  std::vector<int8_t> mask_rows;
+  std::vector<std::pair<long long, int>> mask_sets;
+  std::vector<long long> mask_offs;
+  int mask_m = 0, mask_n1 = 0;
   int32_t *verdict = nullptr; long long v_cap = 0;
   long long *nodes = nullptr; long long n_cap = 0;
   uint64_t *ab = nullptr; long long ab_cap = 0;
   unsigned long long *next = nullptr;
   long long *hit_min = nullptr;
-  int *stop = nullptr;
 };
 
 static AbBufs *ab_bufs(bs_ctx *ctx) {
@@ -527,9 +591,9 @@ static AbBufs *ab_bufs(bs_ctx *ctx) {
 void bs_ab_free(bs_ctx *ctx) {
   AbBufs *b = (AbBufs *)ctx->ab_bufs;
   if (!b) return;
-  cudaFree(b->outer); cudaFree(b->cands); cudaFree(b->rows); cudaFree(b->stacks);
+  cudaFree(b->outer); cudaFree(b->cands); cudaFree(b->masks); cudaFree(b->bits); cudaFree(b->rows8);
   cudaFree(b->verdict); cudaFree(b->nodes); cudaFree(b->ab); cudaFree(b->next);
-  cudaFree(b->hit_min); cudaFree(b->stop);
+  cudaFree(b->hit_min);
   delete b;
   ctx->ab_bufs = nullptr;
 }
@@ -545,6 +609,7 @@ extern "C" int bs_complete_ab_batch(bs_ctx *ctx, const bs_ab_cand *cands, long l
   if (!ctx || ncand < 0 || !opt || (ncand && (!cands || !verdict || !nodes))) return BS_ERR_ARG;
   if (opt->m != 3 && opt->m != 6) return BS_ERR_ARG;
   if (opt->outer_k != 0 && opt->outer_k != 2 && opt->outer_k != 3) return BS_ERR_ARG;
+  if (opt->a2 != 0 && opt->a2 != 2) return BS_ERR_ARG;
   if (ncand == 0) return BS_OK;
   const int n = ctx->n, n1 = n + 1, half = n1 / 2;
   if (n1 > 64 || half + 1 > AB_MAXLV) return BS_ERR_ARG;
@@ -559,22 +624,89 @@ extern "C" int bs_complete_ab_batch(bs_ctx *ctx, const bs_ab_cand *cands, long l
     CK(cudaMemcpy(Bf->outer + sizeof T.o2, T.o3, sizeof T.o3, cudaMemcpyHostToDevice));
     CK(cudaMalloc(&Bf->next, sizeof(unsigned long long)));
     CK(cudaMalloc(&Bf->hit_min, sizeof(long long)));
-    CK(cudaMalloc(&Bf->stop, sizeof(int)));
-    CK(cudaMemset(Bf->stop, 0, sizeof(int)));
   }
-  int maxrows = 1;
   std::vector<AbCandDev> hc(ncand);
   for (long long i = 0; i < ncand; i++) {
-    hc[i].c = cands[i].c;
-    hc[i].d = cands[i].d;
-    hc[i].row_off = cands[i].row_off;
-    hc[i].nrows = cands[i].nrows;
-    hc[i].pad = 0;
     if (cands[i].nrows < 0 || cands[i].nrows > 65535) return BS_ERR_ARG;
     if (cands[i].nrows > 0 &&
         (!rows || cands[i].row_off < 0 || cands[i].row_off + cands[i].nrows > nrows_total))
       return BS_ERR_ARG;
-    if (cands[i].nrows > maxrows) maxrows = cands[i].nrows;
+  }
+  // ---- the allowed-row masks of every distinct row set (kept on the device for the next
+  // batch when it has the same rows: the lane completes one cell in several batches) ----
+  const int m = opt->m;
+  int tic[8] = {0};
+  for (int c = 0; c < m; c++)
+    for (int p = c; p < n1; p += m) tic[c]++;
+  int TV = 0;
+  for (int c = 0; c < m; c++) TV = tic[c] > TV ? tic[c] : TV;
+  const int V = 2 * TV + 3;
+  std::vector<std::pair<long long, int>> sets;
+  std::vector<int> set_of(ncand, -1);
+  for (long long i = 0; i < ncand; i++) {
+    if (cands[i].nrows == 0) continue;
+    const std::pair<long long, int> key(cands[i].row_off, cands[i].nrows);
+    int k = (int)sets.size() - 1;
+    while (k >= 0 && sets[k] != key) k--;
+    if (k < 0) {
+      sets.push_back(key);
+      k = (int)sets.size() - 1;
+    }
+    set_of[i] = k;
+  }
+  bool same = Bf->mask_m == m && Bf->mask_n1 == n1 && sets.size() <= Bf->mask_sets.size();
+  std::vector<long long> offs(sets.size(), 0);
+  for (size_t k = 0; same && k < sets.size(); k++) {
+    size_t j = 0;
+    while (j < Bf->mask_sets.size() && Bf->mask_sets[j] != sets[k]) j++;
+    if (j == Bf->mask_sets.size()) { same = false; break; }
+    const long long lo = sets[k].first * 16, len = (long long)sets[k].second * 16;
+    if ((long long)Bf->mask_rows.size() < lo + len ||
+        memcmp(Bf->mask_rows.data() + lo, rows + lo, (size_t)len) != 0) { same = false; break; }
+    offs[k] = Bf->mask_offs[j];
+  }
+  int Wcap = 1;
+  for (auto &k : sets) Wcap = std::max(Wcap, (k.second + 63) / 64);
+  if (!same && !sets.empty()) {
+    long long total = 0;
+    for (size_t k = 0; k < sets.size(); k++) {
+      offs[k] = total;
+      total += (long long)m * 4 * V * ((sets[k].second + 63) / 64);
+    }
+    std::vector<uint64_t> hm((size_t)total, 0);
+    for (size_t k = 0; k < sets.size(); k++) {
+      const int W = (sets[k].second + 63) / 64;
+      for (int r = 0; r < sets[k].second; r++) {
+        const int8_t *row = rows + 16 * (sets[k].first + r);
+        const uint64_t bit = 1ULL << (r & 63);
+        for (int c = 0; c < m; c++)
+          for (int kind = 0; kind < 4; kind++) {
+            const int x = kind < 2 ? row[c] : row[8 + c];
+            // kinds 0, 2: value >= v for v <= x; kinds 1, 3: value <= v for v >= x
+            const int lo = (kind & 1) ? x : -TV - 1, hi = (kind & 1) ? TV + 1 : x;
+            uint64_t *base = hm.data() + offs[k] + (size_t)(c * 4 + kind) * V * W + (r >> 6);
+            for (int v = std::max(lo, -TV - 1); v <= std::min(hi, TV + 1); v++)
+              base[(size_t)(v + TV + 1) * W] |= bit;
+          }
+      }
+    }
+    rc = bs_ensure_dev((void **)&Bf->masks, &Bf->masks_cap, total, sizeof(uint64_t));
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(Bf->masks, hm.data(), sizeof(uint64_t) * total, cudaMemcpyHostToDevice, s));
+    CK(cudaStreamSynchronize(s));  // hm is freed on return
+    Bf->mask_rows.assign(rows, rows + 16 * nrows_total);
+    Bf->mask_sets = sets;
+    Bf->mask_offs = offs;
+    Bf->mask_m = m;
+    Bf->mask_n1 = n1;
+  }
+  for (long long i = 0; i < ncand; i++) {
+    hc[i].c = cands[i].c;
+    hc[i].d = cands[i].d;
+    hc[i].nrows = cands[i].nrows;
+    hc[i].W = cands[i].nrows > 0 ? (cands[i].nrows + 63) / 64 : 0;
+    hc[i].mask_off = set_of[i] >= 0 ? offs[set_of[i]] : 0;
+    hc[i].row_off = cands[i].nrows > 0 ? cands[i].row_off : 0;
   }
   const int grid = ctx->num_sms * 2;
   const long long slots = (long long)grid * AB_WARPS;
@@ -582,26 +714,14 @@ extern "C" int bs_complete_ab_batch(bs_ctx *ctx, const bs_ab_cand *cands, long l
   if (!rc) rc = bs_ensure_dev((void **)&Bf->verdict, &Bf->v_cap, ncand, sizeof(int32_t));
   if (!rc) rc = bs_ensure_dev((void **)&Bf->nodes, &Bf->n_cap, ncand, sizeof(long long));
   if (!rc) rc = bs_ensure_dev((void **)&Bf->ab, &Bf->ab_cap, 2 * ncand, sizeof(uint64_t));
-  if (!rc && nrows_total > 0)
-    rc = bs_ensure_dev((void **)&Bf->rows, &Bf->rows_cap, nrows_total * 4, sizeof(uint64_t));
-  if (!rc) rc = bs_ensure_dev((void **)&Bf->stacks, &Bf->stack_cap, slots * half * (long long)maxrows,
-                              sizeof(uint16_t));
+  if (!rc) rc = bs_ensure_dev((void **)&Bf->bits, &Bf->bits_cap, slots * (half + 1) * (long long)Wcap,
+                              sizeof(uint64_t));
+  if (!rc && opt->a2 && nrows_total > 0)
+    rc = bs_ensure_dev((void **)&Bf->rows8, &Bf->rows8_cap, 16 * nrows_total, 1);
   if (rc) return rc;
   CK(cudaMemcpyAsync(Bf->cands, hc.data(), sizeof(AbCandDev) * ncand, cudaMemcpyHostToDevice, s));
-  std::vector<uint64_t> roww;
-  if (nrows_total > 0) {
-    // each row (k[8], r[8], int8) as four words of biased class bytes: k+64, 64-k, r+64, 64-r
-    roww.assign(4 * (size_t)nrows_total, 0);
-    for (long long r = 0; r < nrows_total; r++)
-      for (int c = 0; c < opt->m; c++) {
-        const int k = rows[16 * r + c], q = rows[16 * r + 8 + c];
-        roww[4 * r + 0] |= (uint64_t)(k + 64) << (8 * c);
-        roww[4 * r + 1] |= (uint64_t)(64 - k) << (8 * c);
-        roww[4 * r + 2] |= (uint64_t)(q + 64) << (8 * c);
-        roww[4 * r + 3] |= (uint64_t)(64 - q) << (8 * c);
-      }
-    CK(cudaMemcpyAsync(Bf->rows, roww.data(), sizeof(uint64_t) * 4 * nrows_total, cudaMemcpyHostToDevice, s));
-  }
+  if (opt->a2 && nrows_total > 0)
+    CK(cudaMemcpyAsync(Bf->rows8, rows, (size_t)16 * nrows_total, cudaMemcpyHostToDevice, s));
   CK(cudaMemsetAsync(Bf->next, 0, sizeof(unsigned long long), s));
   const long long big = 1LL << 62;
   CK(cudaMemcpyAsync(Bf->hit_min, &big, sizeof big, cudaMemcpyHostToDevice, s));
@@ -614,13 +734,34 @@ extern "C" int bs_complete_ab_batch(bs_ctx *ctx, const bs_ab_cand *cands, long l
   P.budget = opt->budget;
   P.max_cycles = opt->max_seconds > 0 ? (long long)(opt->max_seconds * 2.0e9) : 0;
   P.cands = Bf->cands; P.ncand = ncand;
-  P.roww = Bf->rows; P.stacks = Bf->stacks; P.maxrows = maxrows;
-  P.m7 = 0; P.mb = 0;
-  for (int c = 0; c < opt->m; c++) { P.m7 |= 0x80ULL << (8 * c); P.mb |= 0xFFULL << (8 * c); }
+  P.masks = Bf->masks; P.T = TV; P.V = V;
+  P.bits = Bf->bits; P.Wcap = Wcap;
+  // A2 blocks (init_a2_tables, wz_match.cpp:1000-1016): residues paired by the reflection
+  // r -> (L-1-r) mod m, the free middle's block at odd L, and per depth p the quads left in
+  // each block (mirror positions i = p..half-1 of residue i mod m)
+  P.a2 = opt->a2;
+  P.rows8 = Bf->rows8;
+  P.a2_nblk = 0;
+  memset(P.a2_r, 0, sizeof P.a2_r); memset(P.a2_s, 0, sizeof P.a2_s);
+  memset(P.a2_mid, 0, sizeof P.a2_mid); memset(P.a2_cnt, 0, sizeof P.a2_cnt);
+  {
+    int blk_of[8];
+    for (int c = 0; c < 8; c++) blk_of[c] = -1;
+    for (int c = 0; c < m; c++) {
+      if (blk_of[c] >= 0) continue;
+      const int sref = ((n1 - 1 - c) % m + m) % m;
+      P.a2_r[P.a2_nblk] = (int8_t)c;
+      P.a2_s[P.a2_nblk] = (int8_t)sref;
+      blk_of[c] = blk_of[sref] = P.a2_nblk++;
+    }
+    if (n1 % 2 == 1) P.a2_mid[blk_of[half % m]] = 1;
+    for (int p = 0; p <= half + 1 && p < AB_MAXLV + 2; p++)
+      for (int i = p; i < half; i++) P.a2_cnt[p][blk_of[i % m]]++;
+  }
   P.outer2 = Bf->outer; P.outer3 = Bf->outer + sizeof T.o2;
   P.next = Bf->next; P.hit_min = Bf->hit_min;
   P.verdict = Bf->verdict; P.nodes_out = Bf->nodes; P.ab_out = Bf->ab;
-  P.stop_flag = Bf->stop; P.status = ctx->d_status;
+  P.stop_flag = ctx->d_stop; P.status = ctx->d_status;
   for (int c = 0; c < 8; c++) {
     P.tic[c] = 0;
     if (c < opt->m)
@@ -658,5 +799,6 @@ extern "C" int bs_complete_ab_batch(bs_ctx *ctx, const bs_ab_cand *cands, long l
     if (A) memcpy(A + i * n1, a, n1);
     if (B) memcpy(B + i * n1, b, n1);
   }
-  return BS_OK;
+  // the stop flag was raised: candidates not run are marked -1, the others are final
+  return *ctx->h_stop ? BS_STOPPED : BS_OK;
 }

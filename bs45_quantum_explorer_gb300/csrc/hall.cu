@@ -12,6 +12,7 @@
 
 #include <cmath>
 #include <cstring>
+#include <atomic>
 #include <mutex>
 
 #include "bsfh_internal.cuh"
@@ -227,21 +228,34 @@ __global__ void pack_kernel(const int8_t *__restrict__ rows, long long nrows, in
 // ------------------------------------------------------------------------------------
 // tcgen05 form
 // ------------------------------------------------------------------------------------
+// A tile is 128 pairs. Its C sequences are the rows of one [128 x K] operand and its D
+// sequences the rows of a second, so after the MMAs TMEM lane r holds the DFT of C_r in one
+// accumulator and that of D_r in another: a thread owns a whole pair and forms the pair PSD
+// without exchanging values. The 208 table columns are split into the two angle blocks of
+// bs_tc_row (N = 128 and N = 80); block b of a tile has its own accumulators (C and D), so
+// the epilogue of block 0 overlaps the MMAs of block 1 and the other way round:
+//   TMEM columns [0, 256): block 0 (C at 0, D at 128); [256, 416): block 1 (C at 256, D at 336).
 constexpr int TC_STAGES = 4;
 // warps [0, TC_PRODUCERS) producers, TC_MMA_WARP the MMA issuer (and TMEM owner), then two
-// epilogue groups of four warps
+// epilogue groups of four warps: group b reads block b of every tile
 constexpr int TC_PRODUCERS = 2;
 constexpr int TC_MMA_WARP = TC_PRODUCERS;
 constexpr int TC_THREADS = 32 * (TC_PRODUCERS + 1 + 8);
-constexpr int A_STAGE_BYTES = 128 * 128;
-constexpr uint32_t TMEM_COLS = 512;  // two accumulators of 208 columns at 0 and 256
+constexpr int TC_TILE = 128;                    // pairs per tile
+constexpr int A_SEQ_BYTES = 128 * 128;          // one operand: 128 rows x 64 halves
+constexpr int A_STAGE_BYTES = 2 * A_SEQ_BYTES;  // the C operand, then the D operand
+constexpr uint32_t TMEM_COLS = 512;
+constexpr uint32_t TM_BLK1 = 256;               // first TMEM column of block 1
+constexpr int N_BLK0 = 2 * BS_TC_BLK0, N_BLK1 = 2 * BS_TC_BLK1;
+constexpr int TC_SLOTS = 4;  // decision slots: tiles whose two blocks may be in flight at once
 
 struct TcParams {
   const uint64_t *bits;
   long long npairs, ntiles;
   const uint8_t *image;
   int nparts, ksteps;
-  uint32_t idesc;
+  uint32_t idesc[2];  // instruction descriptors of the two angle blocks (N = 128, N = 80)
+  int bits_a16;       // bits is 16-byte aligned: a pair's two words are read as one vector
   uint32_t one2;  // two packed +1.0 halves in the operand format
   float pass_below, reject_above;
   uint8_t *pass;
@@ -328,15 +342,53 @@ __device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
   return d;
 }
 
-// Two PSDs re^2 + im^2 at once with the packed f32x2 multiply and FMA: f0, f1 are exactly
-// fmaf(re0, re0, im0 * im0) and fmaf(re1, re1, im1 * im1) (round to nearest per element).
-__device__ __forceinline__ void psd2(float re0, float re1, float im0, float im1, float &f0, float &f1) {
-  uint64_t re, im, r;
-  asm("mov.b64 %0, {%1, %2};" : "=l"(re) : "f"(re0), "f"(re1));
-  asm("mov.b64 %0, {%1, %2};" : "=l"(im) : "f"(im0), "f"(im1));
-  asm("mul.rn.f32x2 %0, %1, %1;" : "=l"(r) : "l"(im));
-  asm("fma.rn.f32x2 %0, %1, %1, %0;" : "+l"(r) : "l"(re));
+// The pair PSD at two adjacent angles with the packed f32x2 multiply and FMAs:
+// f = ((imC^2 + reC^2) + imD^2) + reD^2 per element, each step rounded to nearest.
+__device__ __forceinline__ void pair_psd2(const float *rc, const float *ic, const float *rd,
+                                          const float *id, float &f0, float &f1) {
+  uint64_t a, b, c, d, r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(a) : "f"(rc[0]), "f"(rc[1]));
+  asm("mov.b64 %0, {%1, %2};" : "=l"(b) : "f"(ic[0]), "f"(ic[1]));
+  asm("mov.b64 %0, {%1, %2};" : "=l"(c) : "f"(rd[0]), "f"(rd[1]));
+  asm("mov.b64 %0, {%1, %2};" : "=l"(d) : "f"(id[0]), "f"(id[1]));
+  asm("mul.rn.f32x2 %0, %1, %1;" : "=l"(r) : "l"(b));
+  asm("fma.rn.f32x2 %0, %1, %1, %0;" : "+l"(r) : "l"(a));
+  asm("fma.rn.f32x2 %0, %1, %1, %0;" : "+l"(r) : "l"(d));
+  asm("fma.rn.f32x2 %0, %1, %1, %0;" : "+l"(r) : "l"(c));
   asm("mov.b64 {%0, %1}, %2;" : "=f"(f0), "=f"(f1) : "l"(r));
+}
+
+// Four operand halves per 32-bit word pair: the 8 bits of `byte` (bit set = +1) as 8 halves
+// +-1.0 in the operand format. neg2 holds two -1.0 halves; z = byte * 0x8001 places bit i at
+// positions i and i + 15, so a shift brings bits 2k and 2k + 1 to the sign positions 15 and 31
+// of word k, and the XOR turns the -1.0 of every set bit into +1.0.
+__device__ __forceinline__ uint4 expand_byte(uint32_t byte, uint32_t neg2) {
+  const uint32_t z = byte * 0x8001u;
+  uint4 v;
+  v.x = neg2 ^ ((z << 15) & 0x80008000u);
+  v.y = neg2 ^ ((z << 13) & 0x80008000u);
+  v.z = neg2 ^ ((z << 11) & 0x80008000u);
+  v.w = neg2 ^ ((z << 9) & 0x80008000u);
+  return v;
+}
+
+// The C and D words of one pair (one 16-byte load when the array is 16-byte aligned).
+__device__ __forceinline__ uint4 load_pair(const uint64_t *bits, long long pair, int a16) {
+  if (a16) return __ldg((const uint4 *)(bits + 2 * pair));
+  const unsigned long long c = __ldg((const unsigned long long *)(bits + 2 * pair));
+  const unsigned long long d = __ldg((const unsigned long long *)(bits + 2 * pair + 1));
+  return make_uint4((uint32_t)c, (uint32_t)(c >> 32), (uint32_t)d, (uint32_t)(d >> 32));
+}
+
+// One sequence word as one operand row (row r of a 128-row K-major operand, 128B swizzle):
+// chunk c (16 bytes, elements 8c..8c+7) goes to chunk c ^ (r & 7) of the row.
+__device__ __forceinline__ void put_row(uint8_t *A, int r, uint64_t w, int nchunks, uint32_t neg2) {
+#pragma unroll
+  for (int c = 0; c < 8; c++) {
+    if (c < nchunks)
+      *(uint4 *)(A + r * 128 + ((c ^ (r & 7)) << 4)) =
+          expand_byte((uint32_t)(w >> (8 * c)) & 0xFFu, neg2);
+  }
 }
 
 __global__ void __launch_bounds__(TC_THREADS, 1) hall_tc_kernel(TcParams P) {
@@ -344,7 +396,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1) hall_tc_kernel(TcParams P) {
   uint8_t *base = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   uint8_t *sA = base;
   uint8_t *sB = sA + TC_STAGES * A_STAGE_BYTES;
-  uint64_t *bars = (uint64_t *)(sB + P.nparts * BS_TC_PART_BYTES);
+  float *pmax = (float *)(sB + P.nparts * BS_TC_PART_BYTES);  // [TC_SLOTS][2][128]
+  int *pcnt = (int *)(pmax + TC_SLOTS * 2 * TC_TILE);         // [TC_SLOTS][4]
+  uint64_t *bars = (uint64_t *)(pcnt + TC_SLOTS * 4);
   uint32_t *tmem_slot = (uint32_t *)(bars + 2 * TC_STAGES + 4);
   volatile int *abort_flag = (volatile int *)(tmem_slot + 1);
   const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + TC_STAGES);
@@ -358,6 +412,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) hall_tc_kernel(TcParams P) {
     int nvec = P.nparts * BS_TC_PART_BYTES / 16;
     for (int i = threadIdx.x; i < nvec; i += TC_THREADS) dst[i] = src[i];
   }
+  for (int i = threadIdx.x; i < TC_SLOTS * 4; i += TC_THREADS) pcnt[i] = 0;
   if (threadIdx.x == 0) {
     for (int s = 0; s < TC_STAGES; s++) {
       mbar_init(full0 + 8 * s, 1);
@@ -378,25 +433,29 @@ __global__ void __launch_bounds__(TC_THREADS, 1) hall_tc_kernel(TcParams P) {
   const uint32_t tmem = *tmem_slot;
 
   if (warp < TC_PRODUCERS) {
-    // ---- producers: packed words -> +-1 operand rows in the swizzled layout. Producer p
-    // fills the CTA's tiles it = p, p + TC_PRODUCERS, ...; the next tile's words are loaded
-    // before the current tile is unpacked so the global-load latency overlaps the work. ----
-    const long long rows_total = 2 * P.npairs;
+    // ---- producers: packed words -> +-1 operand rows. Producer p fills the CTA's tiles
+    // it = p, p + TC_PRODUCERS, ...; lane l handles pairs l + 32 rr of the tile (one 16-byte
+    // load: the pair's C and D words), and the next tile's words are loaded before the current
+    // tile is expanded so the global-load latency overlaps the work. ----
+    const uint32_t neg2 = P.one2 | 0x80008000u;
+    const int nchunks = 2 * P.ksteps;
     int it = warp;
     long long tile = blockIdx.x + (long long)it * G;
-    uint64_t wv[4];
+    uint4 wv[4];
 #pragma unroll
     for (int rr = 0; rr < 4; rr++) {
-      long long row = tile * 128 + lane + 32 * rr;
-      wv[rr] = (tile < P.ntiles && row < rows_total) ? __ldg(P.bits + row) : 0ULL;
+      const long long pair = tile * TC_TILE + lane + 32 * rr;
+      wv[rr] = (tile < P.ntiles && pair < P.npairs) ? load_pair(P.bits, pair, P.bits_a16)
+                                                    : make_uint4(0, 0, 0, 0);
     }
     while (tile < P.ntiles) {
       const long long next = tile + TC_PRODUCERS * G;
-      uint64_t nw[4];
+      uint4 nw[4];
 #pragma unroll
       for (int rr = 0; rr < 4; rr++) {
-        long long row = next * 128 + lane + 32 * rr;
-        nw[rr] = (next < P.ntiles && row < rows_total) ? __ldg(P.bits + row) : 0ULL;
+        const long long pair = next * TC_TILE + lane + 32 * rr;
+        nw[rr] = (next < P.ntiles && pair < P.npairs) ? load_pair(P.bits, pair, P.bits_a16)
+                                                      : make_uint4(0, 0, 0, 0);
       }
       const int s = it % TC_STAGES;
       const uint32_t par = ((it / TC_STAGES) & 1) ^ 1;
@@ -404,20 +463,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1) hall_tc_kernel(TcParams P) {
         if (!*abort_flag) { set_status(P.status, BS_ERR_TIMEOUT); *abort_flag = 1; }
         break;
       }
-      uint8_t *A = sA + s * A_STAGE_BYTES;
+      uint8_t *AC = sA + s * A_STAGE_BYTES, *AD = AC + A_SEQ_BYTES;
 #pragma unroll
       for (int rr = 0; rr < 4; rr++) {
         const int r = lane + 32 * rr;
-        const uint64_t w = wv[rr];
-        for (int c = 0; c < 2 * P.ksteps; c++) {
-          uint32_t nb = ~(uint32_t)(w >> (8 * c));
-          uint4 v;
-          v.x = P.one2 | ((nb & 1u) << 15) | ((nb & 2u) << 30);
-          v.y = P.one2 | ((nb & 4u) << 13) | ((nb & 8u) << 28);
-          v.z = P.one2 | ((nb & 16u) << 11) | ((nb & 32u) << 26);
-          v.w = P.one2 | ((nb & 64u) << 9) | ((nb & 128u) << 24);
-          *(uint4 *)(A + r * 128 + ((c ^ (r & 7)) << 4)) = v;
-        }
+        put_row(AC, r, ((uint64_t)wv[rr].y << 32) | wv[rr].x, nchunks, neg2);
+        put_row(AD, r, ((uint64_t)wv[rr].w << 32) | wv[rr].z, nchunks, neg2);
       }
       fence_async_smem();
       __syncwarp();
@@ -428,116 +479,150 @@ __global__ void __launch_bounds__(TC_THREADS, 1) hall_tc_kernel(TcParams P) {
       it += TC_PRODUCERS;
     }
   } else if (warp == TC_MMA_WARP) {
-    // ---- MMA issuer (one thread) ----
+    // ---- MMA issuer (one thread): per tile, block 0 then block 1, each the C operand into
+    // the block's C accumulator and the D operand into its D accumulator ----
     if (lane == 0) {
       const uint32_t a_base = smem_u32(sA), b_base = smem_u32(sB);
       int it = 0, last = -1;
       for (long long tile = blockIdx.x; tile < P.ntiles; tile += G, it++) {
-        int s = it % TC_STAGES, b = it & 1;
-        if (!mbar_wait(tempty0 + 8 * b, ((it >> 1) & 1) ^ 1, abort_flag) ||
-            !mbar_wait(full0 + 8 * s, (it / TC_STAGES) & 1, abort_flag)) {
+        const int s = it % TC_STAGES;
+        if (!mbar_wait(full0 + 8 * s, (it / TC_STAGES) & 1, abort_flag)) {
           if (!*abort_flag) { set_status(P.status, BS_ERR_TIMEOUT); *abort_flag = 1; }
           break;
         }
-        tc_fence_after();
-        uint32_t d = tmem + (uint32_t)(b * 256);
-        uint32_t acc = 0;
-        for (int p = 0; p < P.nparts; p++)
-          for (int k = 0; k < P.ksteps; k++) {
-            uint64_t ad = sw128_desc(a_base + s * A_STAGE_BYTES + k * 32);
-            uint64_t bd = sw128_desc(b_base + p * BS_TC_PART_BYTES + k * 32);
-            tc_mma(d, ad, bd, P.idesc, acc);
-            acc = 1;
+        bool ok = true;
+        for (int blk = 0; blk < 2 && ok; blk++) {
+          if (!mbar_wait(tempty0 + 8 * blk, (it & 1) ^ 1, abort_flag)) {
+            if (!*abort_flag) { set_status(P.status, BS_ERR_TIMEOUT); *abort_flag = 1; }
+            ok = false;
+            break;
           }
+          tc_fence_after();
+          const uint32_t d0 = tmem + (blk ? TM_BLK1 : 0u);
+          const uint32_t nblk = blk ? (uint32_t)N_BLK1 : (uint32_t)N_BLK0;
+          const uint32_t b_off = blk ? (uint32_t)(N_BLK0 * 128) : 0u;
+          for (int seq = 0; seq < 2; seq++) {
+            uint32_t acc = 0;
+            for (int p = 0; p < P.nparts; p++)
+              for (int k = 0; k < P.ksteps; k++) {
+                const uint64_t ad = sw128_desc(a_base + s * A_STAGE_BYTES + seq * A_SEQ_BYTES + k * 32);
+                const uint64_t bd = sw128_desc(b_base + p * BS_TC_PART_BYTES + b_off + k * 32);
+                tc_mma(d0 + seq * nblk, ad, bd, P.idesc[blk], acc);
+                acc = 1;
+              }
+          }
+          tc_commit(tfull0 + 8 * blk);
+        }
+        if (!ok) break;
         tc_commit(empty0 + 8 * s);
-        tc_commit(tfull0 + 8 * b);
         last = it;
       }
       // Before TMEM is released, the last issued MMAs must have finished.
-      if (last >= 0) mbar_wait(tfull0 + 8 * (last & 1), (last >> 1) & 1, abort_flag, false);
+      if (last >= 0) mbar_wait(tfull0 + 8, last & 1, abort_flag, false);
     }
     __syncwarp();
   } else {
-    // ---- epilogue: TMEM -> max pair PSD -> decision. Group g owns accumulator g (the CTA's
-    // tiles it = g, g + 2, ...); its four warps cover the four 32-lane quarters. ----
-    const int eg = (warp - TC_MMA_WARP - 1) >> 2;
+    // ---- epilogue: group g reads block g of every tile; warp quarter q owns pairs
+    // 32q..32q+31 of the tile, one per lane. Each lane keeps the max pair PSD over its block's
+    // angles; of the two groups, the one that finishes a tile second takes the max of both
+    // blocks (shared memory slot, a counter per quarter) and decides the 32 pairs. ----
+    const int g = (warp - TC_MMA_WARP - 1) >> 2;
     const int q = warp & 3;
     const uint32_t lane_off = (uint32_t)(q * 32) << 16;
     const int row = q * 32 + lane;
-    const int b = eg;
-    for (int it = eg;; it += 2) {
+    const uint32_t tC = tmem + lane_off + (g ? TM_BLK1 : 0u);
+    const uint32_t tD = tC + (g ? (uint32_t)N_BLK1 : (uint32_t)N_BLK0);
+    const uint32_t nb = g ? BS_TC_BLK1 : BS_TC_BLK0;  // angles of the block; Im at column + nb
+    for (int it = 0;; it++) {
       const long long tile = blockIdx.x + (long long)it * G;
       if (tile >= P.ntiles) break;
       // warp-uniform outcome: the TMEM loads below are .sync.aligned
-      bool ready = __all_sync(FULL_MASK, mbar_wait(tfull0 + 8 * b, (it >> 1) & 1, abort_flag));
+      const bool ready = __all_sync(FULL_MASK, mbar_wait(tfull0 + 8 * g, it & 1, abort_flag));
       if (!ready) {
         if (!*abort_flag) { set_status(P.status, BS_ERR_TIMEOUT); *abort_flag = 1; }
         break;
       }
       tc_fence_after();
-      const uint32_t t0 = tmem + lane_off + (uint32_t)(b * 256);
-      float mx = 0.0f;
-      float *dump = P.dump ? P.dump + (size_t)(tile * 128 + row) * BS_TC_COLS : nullptr;
-      // A pair's rows sit in adjacent lanes (C even, D odd). Each lane forms its own row's
-      // PSD at every angle, two adjacent angles per packed f32x2 multiply and FMA; for each
-      // angle one lane adds its partner's: the even lane the even angles, the odd lane the odd
-      // ones. One shuffle then carries two angles (each lane sends the one its partner sums),
-      // and the two running maxima combine at the end. Every value is the scalar
-      // fmaf(re, re, im * im) of the same operands, and every sum fC + fD.
-      const bool odd = lane & 1;
-      float mx1 = 0.0f;
-      {  // angles 0..63: Re columns 0..63 and Im columns 104..167 in one load round
-        float v[128];
-        tmem_ld_64_64(t0, t0 + BS_TC_IM0, v);
+      const long long pair = tile * TC_TILE + row;
+      float *dump = (P.dump && pair < P.npairs) ? P.dump + (size_t)pair * 2 * BS_TC_COLS : nullptr;
+      float mx0 = 0.0f, mx1 = 0.0f;
+      // rounds of 32 angles (block 1: 32 + 8); the block's accumulators are released to the
+      // MMA issuer right after the last round's loads
+      for (uint32_t a0 = 0; a0 < nb; a0 += 32) {
+        const bool last_round = a0 + 32 >= nb;
+        if (nb - a0 >= 32) {
+          float v[128];  // Re C, Im C, Re D, Im D at angles a0..a0+31 of the block
+          tmem_ld_32x4(tC + a0, tC + nb + a0, tD + a0, tD + nb + a0, v);
+          if (last_round) {
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(tempty0 + 8 * g);
+          }
 #pragma unroll
-        for (int k = 0; k < 64; k += 2) {  // adjacent angles k, k+1 in one packed pair
-          float fa, fb;
-          psd2(v[k], v[k + 1], v[64 + k], v[65 + k], fa, fb);
-          const float got = __shfl_xor_sync(FULL_MASK, odd ? fa : fb, 1);
-          if (k & 2) mx1 = fmaxf(mx1, (odd ? fb : fa) + got);
-          else mx = fmaxf(mx, (odd ? fb : fa) + got);
-        }
-        if (dump)
-          for (int k = 0; k < 64; k++) { dump[k] = v[k]; dump[BS_TC_IM0 + k] = v[64 + k]; }
-      }
-      // A pair whose max PSD over the first 64 angles already reaches reject_above is rejected
-      // whatever the other angles hold (the max only grows). When that holds for all 16 pairs
-      // of the warp, the second round is skipped (most leaves of a stream end here).
-      const float m64 = fmaxf(fmaxf(mx, mx1), __shfl_xor_sync(FULL_MASK, fmaxf(mx, mx1), 1));
-      if (!dump && __all_sync(FULL_MASK, m64 >= P.reject_above)) {
-        mx = m64;
-        mx1 = m64;
-      } else {  // angles 64..103 (101..103 are zero padding)
-        float v[80];
-        tmem_ld_32_8_32_8(t0 + 64, t0 + 96, t0 + BS_TC_IM0 + 64, t0 + BS_TC_IM0 + 96, v);
+          for (int k = 0; k < 32; k += 2) {
+            float f0, f1;
+            pair_psd2(v + k, v + 32 + k, v + 64 + k, v + 96 + k, f0, f1);
+            mx0 = fmaxf(mx0, f0);
+            mx1 = fmaxf(mx1, f1);
+          }
+          if (dump)
+            for (int k = 0; k < 32; k++) {
+              const int u = (g ? BS_TC_BLK0 : 0) + (int)a0 + k;
+              dump[u] = v[k];
+              dump[BS_TC_IM0 + u] = v[32 + k];
+              dump[BS_TC_COLS + u] = v[64 + k];
+              dump[BS_TC_COLS + BS_TC_IM0 + u] = v[96 + k];
+            }
+        } else {  // the last 8 angles of block 1
+          float v[32];
+          tmem_ld_8x4(tC + a0, tC + nb + a0, tD + a0, tD + nb + a0, v);
+          tc_fence_before();
+          __syncwarp();
+          if (lane == 0) mbar_arrive(tempty0 + 8 * g);
 #pragma unroll
-        for (int k = 0; k < 40; k += 2) {
-          float fa, fb;
-          psd2(v[k], v[k + 1], v[40 + k], v[41 + k], fa, fb);
-          const float got = __shfl_xor_sync(FULL_MASK, odd ? fa : fb, 1);
-          if (k & 2) mx1 = fmaxf(mx1, (odd ? fb : fa) + got);
-          else mx = fmaxf(mx, (odd ? fb : fa) + got);
+          for (int k = 0; k < 8; k += 2) {
+            float f0, f1;
+            pair_psd2(v + k, v + 8 + k, v + 16 + k, v + 24 + k, f0, f1);
+            mx0 = fmaxf(mx0, f0);
+            mx1 = fmaxf(mx1, f1);
+          }
+          if (dump)
+            for (int k = 0; k < 8; k++) {
+              const int u = (g ? BS_TC_BLK0 : 0) + (int)a0 + k;
+              dump[u] = v[k];
+              dump[BS_TC_IM0 + u] = v[8 + k];
+              dump[BS_TC_COLS + u] = v[16 + k];
+              dump[BS_TC_COLS + BS_TC_IM0 + u] = v[24 + k];
+            }
         }
-        if (dump)
-          for (int k = 0; k < 40; k++) { dump[64 + k] = v[k]; dump[BS_TC_IM0 + 64 + k] = v[40 + k]; }
       }
-      mx = fmaxf(mx, mx1);
-      mx = fmaxf(mx, __shfl_xor_sync(FULL_MASK, mx, 1));
-      tc_fence_before();
+      const float mx = fmaxf(mx0, mx1);
+      // hand-over between the two groups: the second to finish this tile decides
+      const int slot = it & (TC_SLOTS - 1);
+      pmax[(slot * 2 + g) * TC_TILE + row] = mx;
+      __threadfence_block();
       __syncwarp();
-      if (lane == 0) mbar_arrive(tempty0 + 8 * b);
-      long long pair = tile * 64 + (row >> 1);
-      bool mine = !(lane & 1) && pair < P.npairs;
-      bool sure_pass = mine && mx <= P.pass_below;
-      bool unsure = mine && mx > P.pass_below && mx < P.reject_above;
-      if (mine) P.pass[pair] = sure_pass ? 1 : 0;
-      if (unsure) {
-        unsigned long long k = atomicAdd(P.count, 1ULL);
-        if (k < P.unc_cap) P.unc[k] = (unsigned)pair;
-        else atomicExch(P.count + 2, 1ULL);
+      int order = 0;
+      if (lane == 0) order = atomicAdd(&pcnt[slot * 4 + q], 1);
+      order = __shfl_sync(FULL_MASK, order, 0);
+      if (order == 1) {
+        __threadfence_block();
+        const float m = fmaxf(mx, pmax[(slot * 2 + (g ^ 1)) * TC_TILE + row]);
+        const bool mine = pair < P.npairs;
+        const bool sure_pass = mine && m <= P.pass_below;
+        const bool unsure = mine && m > P.pass_below && m < P.reject_above;
+        if (mine) P.pass[pair] = sure_pass ? 1 : 0;
+        if (unsure) {
+          unsigned long long k = atomicAdd(P.count, 1ULL);
+          if (k < P.unc_cap) P.unc[k] = (unsigned)pair;
+          else atomicExch(P.count + 2, 1ULL);
+        }
+        const unsigned np = __popc(__ballot_sync(FULL_MASK, sure_pass));
+        if (lane == 0) {
+          if (np) atomicAdd(P.count + 1, (unsigned long long)np);
+          atomicExch(&pcnt[slot * 4 + q], 0);
+        }
       }
-      unsigned np = __popc(__ballot_sync(FULL_MASK, sure_pass));
-      if (lane == 0 && np) atomicAdd(P.count + 1, (unsigned long long)np);
     }
   }
 
@@ -549,7 +634,17 @@ __global__ void __launch_bounds__(TC_THREADS, 1) hall_tc_kernel(TcParams P) {
 
 size_t tc_smem_bytes(int nparts) {
   return 1024 + (size_t)TC_STAGES * A_STAGE_BYTES + (size_t)nparts * BS_TC_PART_BYTES +
+         sizeof(float) * TC_SLOTS * 2 * TC_TILE + sizeof(int) * TC_SLOTS * 4 +
          (2 * TC_STAGES + 4) * 8 + 16;
+}
+
+// Instruction descriptors (kind::f16): D fp32, A and B of format fmt (0 f16, 1 bf16), both
+// K-major, M = 128, N = 128 for angle block 0 and N = 80 for block 1.
+void tc_idesc(int fmt, uint32_t idesc[2]) {
+  const uint32_t base = (1u << 4) | ((uint32_t)fmt << 7) | ((uint32_t)fmt << 10) |
+                        ((uint32_t)(128 >> 4) << 24);
+  idesc[0] = base | ((uint32_t)(N_BLK0 >> 3) << 17);
+  idesc[1] = base | ((uint32_t)(N_BLK1 >> 3) << 17);
 }
 
 }  // namespace
@@ -563,21 +658,34 @@ size_t tc_smem_bytes(int nparts) {
     if (e_ != cudaSuccess) return bs_cuda_fail(e_); \
   } while (0)
 
+// Shared-memory opt-ins of the Hall kernels (the tensor-core kernel takes ~100 KB, the FP64
+// kernels up to 200 KB). The attribute belongs to the device that is current when it is set,
+// so it is set once per device, with that device current; serving slots call from several
+// host threads, and one process may hold contexts on several GPUs. A failed attempt is
+// retried by the next call.
+static int hall_kernel_attrs(int dev) {
+  static std::atomic<bool> done[64];
+  static std::mutex mu;
+  if (dev < 0 || dev >= 64) return BS_ERR_ARG;
+  if (done[dev].load(std::memory_order_acquire)) return BS_OK;
+  std::lock_guard<std::mutex> lock(mu);
+  if (done[dev].load(std::memory_order_relaxed)) return BS_OK;
+  const int fp64_smem = (int)(sizeof(double) * 2 * 200 * BS_MAXL);
+  CK(cudaFuncSetAttribute(hall_fp64_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, fp64_smem));
+  CK(cudaFuncSetAttribute(hall_fp64_recheck_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                          fp64_smem));
+  CK(cudaFuncSetAttribute(hall_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                          (int)tc_smem_bytes(2)));
+  CK(cudaFuncSetAttribute(hall_fix_band_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                          (int)(sizeof(int64_t) * BS_FIX_WORDS)));
+  done[dev].store(true, std::memory_order_release);
+  return BS_OK;
+}
+
 static int launch_fp64(bs_ctx *ctx, const uint64_t *d_bits, long long npairs,
                        const unsigned *list, const unsigned long long *list_len,
                        unsigned long long list_cap, uint8_t *d_pass, int L) {
   size_t smem = sizeof(double) * 2 * 200 * L;
-  // shared-memory opt-in, once per process (a thread-safe static: serving slots call this
-  // from several host threads)
-  static const cudaError_t attr = [] {
-    cudaError_t e = cudaFuncSetAttribute(hall_fp64_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)(sizeof(double) * 2 * 200 * BS_MAXL));
-    if (e == cudaSuccess)
-      e = cudaFuncSetAttribute(hall_fp64_recheck_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               (int)(sizeof(double) * 2 * 200 * BS_MAXL));
-    return e;
-  }();
-  CK(attr);
   if (list) {  // the margin band after the tensor-core kernel: a warp per pair on every SM
     ctx->launches++;
     hall_fp64_recheck_kernel<<<ctx->num_sms, 256, smem, ctx->stream>>>(
@@ -602,13 +710,12 @@ static int launch_tc(bs_ctx *ctx, int mode, const uint64_t *d_bits, long long np
   TcParams P;
   P.bits = d_bits;
   P.npairs = npairs;
-  P.ntiles = (npairs + 63) / 64;
+  P.ntiles = (npairs + TC_TILE - 1) / TC_TILE;
+  P.bits_a16 = ((uintptr_t)d_bits & 15) == 0;
   P.image = F.d_image;
   P.nparts = F.nparts;
   P.ksteps = (L + 15) / 16;
-  // instruction descriptor: D fp32, A/B format, both K-major, N = 208, M = 128
-  P.idesc = (1u << 4) | ((uint32_t)F.fmt << 7) | ((uint32_t)F.fmt << 10) |
-            ((uint32_t)(BS_TC_COLS >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
+  tc_idesc(F.fmt, P.idesc);
   P.one2 = F.fmt ? 0x3F803F80u : 0x3C003C00u;
   P.pass_below = F.pass_below;
   P.reject_above = F.reject_above;
@@ -619,9 +726,6 @@ static int launch_tc(bs_ctx *ctx, int mode, const uint64_t *d_bits, long long np
   P.status = ctx->d_status;
   P.dump = d_dump;
   size_t smem = tc_smem_bytes(F.nparts);
-  static const cudaError_t attr = cudaFuncSetAttribute(
-      hall_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc_smem_bytes(2));
-  CK(attr);
   long long grid = P.ntiles < ctx->num_sms ? P.ntiles : ctx->num_sms;
   if (grid < 1) grid = 1;
   bs_timed_begin(ctx);
@@ -635,10 +739,6 @@ static int launch_tc(bs_ctx *ctx, int mode, const uint64_t *d_bits, long long np
 // list (d_unc2, d_count[3]).
 static int launch_fix(bs_ctx *ctx, const uint64_t *d_bits, uint8_t *d_pass, int L) {
   const bs_hall_fix_form &F = ctx->fix[L == ctx->n ? 0 : 1];
-  static const cudaError_t attr = cudaFuncSetAttribute(
-      hall_fix_band_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-      (int)(sizeof(int64_t) * BS_FIX_WORDS));
-  CK(attr);
   const size_t smem = sizeof(int64_t) * (2 * BS_TC_NANG * L + 2 * BS_TC_NANG);
   ctx->launches++;
   hall_fix_band_kernel<<<ctx->num_sms, 256, smem, ctx->stream>>>(
@@ -656,6 +756,7 @@ static int hall_dev(bs_ctx *ctx, const uint64_t *d_bits, long long npairs, int m
   if (mode < BS_HALL_FP64 || mode > BS_HALL_TC_BF16X2) return BS_ERR_ARG;
   if (npairs >= (1LL << 32)) return BS_ERR_ARG;
   CK(cudaSetDevice(ctx->device));
+  if (int rc = hall_kernel_attrs(ctx->device)) return rc;
   CK(cudaMemsetAsync(ctx->d_count, 0, sizeof(unsigned long long) * 8, ctx->stream));
   if (npairs > 0) {
     if (mode == BS_HALL_FP64) {
@@ -823,7 +924,7 @@ static void noalloc_tables(int n, NoallocDevice &S) {
     const int j = u < 100 ? u + 1 : 200;
     for (int kind = 0; kind < 2; kind++) {
       const double *tab = kind ? g_na_sin : g_na_cos;
-      const int row = kind ? BS_TC_IM0 + u : u;
+      const int row = bs_tc_row(u, kind);
       double esum = 0.0;
       for (int i = 0; i < n; i++) {
         const double t = tab[(j - 1) * BS_MAXL + i];
@@ -873,14 +974,12 @@ extern "C" int bs_hall_filter_noalloc(int n, const uint64_t *d_bits, long long n
   if (!S.scratch) {  // set-up, once per device, with that device current
     void *p = nullptr;
     CK(cudaGetSymbolAddress(&p, g_hall_noalloc_scratch));
-    S.scratch = (unsigned char *)p;
+    if (int rc = hall_kernel_attrs(dev)) return rc;
     S.n = 0;
-    CK(cudaFuncSetAttribute(hall_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                            (int)tc_smem_bytes(2)));
-    CK(cudaFuncSetAttribute(hall_fp64_recheck_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                            (int)(sizeof(double) * 2 * 200 * BS_MAXL)));
+    S.scratch = (unsigned char *)p;  // only once every set-up step has succeeded
   }
   if (S.n != n) {  // tables of another length: rebuild and upload (no device allocation)
+    S.n = 0;  // a failure below leaves no length marked as loaded: the next call rebuilds
     noalloc_tables(n, S);
     CK(cudaMemcpyAsync(S.scratch + NA_COS_OFF, g_na_cos, sizeof g_na_cos, cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(S.scratch + NA_SIN_OFF, g_na_sin, sizeof g_na_sin, cudaMemcpyHostToDevice, s));
@@ -895,11 +994,12 @@ extern "C" int bs_hall_filter_noalloc(int n, const uint64_t *d_bits, long long n
     TcParams P;
     P.bits = d_bits;
     P.npairs = npairs;
-    P.ntiles = (npairs + 63) / 64;
+    P.ntiles = (npairs + TC_TILE - 1) / TC_TILE;
+    P.bits_a16 = ((uintptr_t)d_bits & 15) == 0;
     P.image = S.scratch + NA_IMG_OFF;
     P.nparts = 1;
     P.ksteps = (n + 15) / 16;
-    P.idesc = (1u << 4) | ((uint32_t)(BS_TC_COLS >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
+    tc_idesc(0, P.idesc);
     P.one2 = 0x3C003C00u;
     P.pass_below = S.pass_below;
     P.reject_above = S.reject_above;

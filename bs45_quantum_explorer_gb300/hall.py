@@ -55,6 +55,14 @@ class Context:
         except Exception:
             pass
 
+    def request_stop(self, value=1):
+        """Raise (or, with value 0, clear) the context's stop flag: running and later stream
+        and completion calls stop within one device round and return what they completed."""
+        lib().bs_ctx_stop_flag(self.h)[0] = int(value)
+
+    def clear_stop(self):
+        self.request_stop(0)
+
     def set_stream(self, stream_handle):
         check(lib().bs_ctx_set_stream(self.h, C.c_void_p(stream_handle)), "bs_ctx_set_stream")
 

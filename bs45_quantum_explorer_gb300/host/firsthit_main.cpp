@@ -7,10 +7,12 @@
 // checkpoint file (CFGSIG line and resume fields) and the same exit codes:
 //   0 FOUND, 3 no hit / range exhausted / interrupted, 2 refusal, 1 usage, 5 internal error.
 // Not carried over (measurement-only instruments of the reference): FH_TELEM telemetry,
-// HALLSTAT adaptive-order statistics, the A2 shadow, LOCATE / ORBIT_AUDIT / OUTER_DUMP / TARGET
-// canaries. WZ_FH_CD_PRUNE prunes the device stream as the reference's DFS does (same stream,
-// CDSTAT counts the pruned walk); WZ_FH_HALL_FAST changes no stream and is accepted;
-// WZ_FH_WALL_SEC is accepted for the CFGSIG namespace but no cell is abandoned on time.
+// HALLSTAT adaptive-order statistics, the A2 shadow (WZ_FH_A2=1; the A2 prune, WZ_FH_A2=2,
+// runs on the device), LOCATE / ORBIT_AUDIT / OUTER_DUMP / TARGET canaries. WZ_FH_CD_PRUNE prunes the device stream as the reference's DFS does (same stream,
+// CDSTAT counts the pruned walk); WZ_FH_HALL_FAST changes no stream and is accepted.
+// WZ_FH_WALL_SEC abandons a cell whose stream finds no survivor for that many seconds (its
+// partial buffer is still drained, and it counts in cells_walled), and SIGTERM raises the
+// context's stop flag, which stops a running stream or completion within one device round.
 #include <algorithm>
 #include <atomic>
 #include <chrono>
@@ -35,7 +37,11 @@ using Clock = std::chrono::steady_clock;
 namespace {
 
 volatile sig_atomic_t g_sigterm = 0;
-void on_sigterm(int) { g_sigterm = 1; }
+volatile int32_t *g_stop_flag = nullptr;  // the context's mapped stop flag (bs_ctx_stop_flag)
+void on_sigterm(int) {
+  g_sigterm = 1;
+  if (g_stop_flag) *g_stop_flag = 1;  // a plain store to pinned host memory: signal-safe
+}
 
 const char *env(const char *k) { return getenv(k); }
 long long env_ll(const char *k, long long dflt) {
@@ -122,8 +128,9 @@ int main(int argc, char **argv) {
   bool thm211b = env("WZ_THM211B") != nullptr, thm212 = env("WZ_THM212") != nullptr;
   const bool endpos = env_on("WZ_FH_ENDPOS");
   const int outer_k = env_i("WZ_FH_OUTER_K", 3);
-  if (env_i("WZ_FH_A2", 0) != 0) {
-    printf("RESULT: WZ_FH_A2 (optional A2 row prune) is not built on the GPU lane — refusing\n");
+  const int a2_mode = env_i("WZ_FH_A2", 0);
+  if (a2_mode != 0 && a2_mode != 2) {
+    printf("RESULT: WZ_FH_A2=%d (the A2 shadow instrument) is not built on the GPU lane — refusing\n", a2_mode);
     return 2;
   }
   if (outer_k != 0 && outer_k != 2 && outer_k != 3) {
@@ -337,6 +344,8 @@ int main(int argc, char **argv) {
   bs_ctx *ctx = nullptr;
   int rc = bs_ctx_create(n, SA, SB, SC, SD, env_i("BS_DEVICE", 0), &ctx);
   if (rc) return fail_gpu(rc, "bs_ctx_create");
+  g_stop_flag = bs_ctx_stop_flag(ctx);
+  if (g_sigterm) *g_stop_flag = 1;  // a SIGTERM before the context existed
   bs_ab_opts abo;
   memset(&abo, 0, sizeof abo);
   abo.budget = budget;
@@ -345,6 +354,7 @@ int main(int argc, char **argv) {
   abo.canon = canon;
   abo.m = fh_m;
   abo.first_hit = 1;
+  abo.a2 = a2_mode;
   abo.max_seconds = 0;
 
   // ---- complete-only mode (WZ_FH_COMPLETE_C/_D), wz_match.cpp:2403-2455 ----
@@ -360,8 +370,15 @@ int main(int argc, char **argv) {
     std::vector<int8_t> A8(n1), B8(n1);
     auto t0c = Clock::now();
     rc = bs_complete_ab_batch(ctx, &one, 1, nullptr, 0, &abo, &v, &nd, A8.data(), B8.data());
+    if (rc == BS_STOPPED) {
+      printf("COMPLETE_ONLY interrupted (SIGTERM)\n");
+      fflush(stdout);
+      bs_ctx_destroy(ctx);
+      return 3;
+    }
     if (rc) return fail_gpu(rc, "bs_complete_ab_batch");
-    printf("COMPLETE_ONLY r=%d nodes=%lld budget=%lld outer_k=%d a2=0 sec=%g\n", v, nd, budget, outer_k, secs_since(t0c));
+    printf("COMPLETE_ONLY r=%d nodes=%lld budget=%lld outer_k=%d a2=%d sec=%g\n", v, nd, budget, outer_k, a2_mode,
+           secs_since(t0c));
     if (v == 0) {
       std::vector<int> A(n1), B(n1);
       for (int i = 0; i < n1; i++) { A[i] = A8[i]; B[i] = B8[i]; }
@@ -410,6 +427,7 @@ int main(int argc, char **argv) {
   so.endpos = endpos ? 1 : 0;
   so.cd_prune = env_i("WZ_FH_CD_PRUNE", 0);
   so.hall_mode = hall_mode;
+  so.wall_sec = (double)wall_sec;
   // Front-only lanes use only a cell's first DRAIN_BATCHES x BUF_CAP survivors (the reference
   // stops the cell's DFS there); the device stream stops there too. Score filtering and the
   // unbuffered order see further into the stream, so they stream whole cells.
@@ -465,6 +483,11 @@ int main(int argc, char **argv) {
       so.survivor_cap = std::max(so.survivor_cap, nout);
       rc = bs_cd_stream(ctx, &cell, 1, &so, surv.data(), nullptr, (long long)surv.size() / 2, &nout, &cst);
     }
+    // stopped by SIGTERM: the loop below sees g_sigterm and takes nothing of this cell;
+    // stopped by the wall: the cell's survivors so far are processed and drained as usual
+    const bool walled = rc == BS_WALLED;
+    if (walled) cells_walled++;
+    if (rc == BS_STOPPED || rc == BS_WALLED) rc = BS_OK;
     if (rc) return fail_gpu(rc, "bs_cd_stream");
     // flat scores of every survivor (stream order), computed on the GPU
     surv_score.assign((size_t)nout, 0);
@@ -548,7 +571,7 @@ int main(int argc, char **argv) {
         int r2 = bs_complete_ab_batch(ctx, cs.data(), (long long)cs.size(), rows ? rows->data() : nullptr,
                                       rows ? (long long)(rows->size() / 16) : 0, &abo, v.data(), nd.data(),
                                       A8.data(), B8.data());
-        if (r2) exit(fail_gpu(r2, "bs_complete_ab_batch"));
+        if (r2 && r2 != BS_STOPPED) exit(fail_gpu(r2, "bs_complete_ab_batch"));
         for (size_t t = b0; t < b1; t++) {
           if (found || g_sigterm) break;
           int Ci[64], Di[64];
@@ -666,7 +689,7 @@ int main(int argc, char **argv) {
       printf("CDSTAT pi=%lld dfs_nodes=%lld cd_prune=%d hall_fast=1\n", pi, cst.nodes, env_i("WZ_FH_CD_PRUNE", 0));
       fflush(stdout);
     }
-    if (cell_order && !cellbuf.empty() && !cell_stop) drain();
+    if (cell_order && !cellbuf.empty() && (!cell_stop || walled)) drain();
     if (!fh_stop && !g_sigterm) {
       cells_done++;
       if (cand == cs_start) cells_empty++;

@@ -72,7 +72,7 @@ def run_lane(ctx, n, sig, skip=0, end=0, shard=0, nshard=1, budget=200000, buf_c
              drain_top=0, drain_batches=1, endpos=False, orbit_canon=True, orbit_q=1, qprune=True,
              prof_order=3, m6=None, thm211b=None, thm212=None, abp_cap=20000, outer_k=3,
              early=True, canon=True, rev=False, hall_mode="tc_fp16", chunk=65536,
-             max_seconds=0.0, listing=None, batch_cells=None, cd_prune=0):
+             max_seconds=0.0, listing=None, batch_cells=None, cd_prune=0, a2=0):
     """Runs the lane over raw cells [skip, end) of its shard (end = 0: to the list's end).
     The list options are the lane's WZ_FH_* list settings (cells.cell_list); the cells must
     be mod-6 cells (the lane's buffered order). max_seconds > 0 stops between cells once
@@ -154,7 +154,7 @@ def run_lane(ctx, n, sig, skip=0, end=0, shard=0, nshard=1, budget=200000, buf_c
                 ctx.timing(True)
                 v, nd, A, B = complete_ab(ctx, surv[idx], budget, rows=cell_rows, m=m,
                                           outer_k=outer_k, early=early, canon=canon,
-                                          first_hit=True)
+                                          first_hit=True, a2=a2)
                 ms, _, _ = ctx.timing_read()
                 ctx.timing(False)
                 res.complete_s += time.perf_counter() - t1

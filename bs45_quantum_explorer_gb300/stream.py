@@ -9,7 +9,7 @@ import ctypes as C
 
 import numpy as np
 
-from ._lib import BS_OK, BsError, Cell, CellStats, StreamOpts, check, lib
+from ._lib import BS_OK, BS_STOPPED, BS_WALLED, BsError, Cell, CellStats, StreamOpts, check, lib
 from .hall import MODES, unpack
 
 
@@ -26,7 +26,7 @@ def make_cells(cells, m, pins=None):
 
 def cd_stream(ctx, cells, m=6, pins=None, rev=False, endpos=False, hall_mode="tc_fp16",
               target_prefixes=0, leaf_chunk=0, survivor_cap=0, cap=None, as_words=False,
-              ab_side=False, limit=0, round_us=0, cd_prune=0):
+              ab_side=False, limit=0, round_us=0, cd_prune=0, wall_sec=0.0):
     """cells: list of (tx, ty). Returns (survivors, cell index per survivor, per-cell stats).
 
     survivors: int8 [k, 2, L] (or uint64 words [k, 2] with as_words) in stream order, L = n
@@ -35,13 +35,17 @@ def cd_stream(ctx, cells, m=6, pins=None, rev=False, endpos=False, hall_mode="tc
     CELLSIZE leaves / hall_ok; with limit > 0, of the part explored).
     limit > 0 returns only the first `limit` survivors and stops the search there.
     cd_prune: WZ_FH_CD_PRUNE (bit 1 root quad rule, bit 2 block reachability; C,D side, m = 6,
-    even n only): the same survivors, fewer DFS nodes."""
+    even n only): the same survivors, fewer DFS nodes.
+    wall_sec > 0: WZ_FH_WALL_SEC, abandon the stream after that long without a new survivor.
+    A stream stopped early (the context's stop flag, or the wall) returns the survivors of the
+    part it completed, and every stats dict carries stopped = 1 (flag) or 2 (wall), else 0."""
     ncells = len(cells)
     arr = make_cells(cells, m, pins)
     opt = StreamOpts(m=m, rev=int(rev), endpos=int(endpos), cd_prune=int(cd_prune),
                      hall_mode=MODES[hall_mode], ab_side=int(ab_side),
                      target_prefixes=target_prefixes, leaf_chunk=leaf_chunk,
-                     survivor_cap=survivor_cap, limit=limit, round_us=round_us)
+                     survivor_cap=survivor_cap, limit=limit, round_us=round_us,
+                     wall_sec=float(wall_sec))
     stats = (CellStats * ncells)()
     nout = C.c_longlong(0)
     cap = cap if cap is not None else (min(1 << 20, limit) if limit > 0 else 1 << 20)
@@ -54,10 +58,11 @@ def cd_stream(ctx, cells, m=6, pins=None, rev=False, endpos=False, hall_mode="tc
             cap = max(cap, nout.value)
             opt.survivor_cap = max(opt.survivor_cap, nout.value)
             continue
-        check(rc, "bs_cd_stream")
+        if rc not in (BS_STOPPED, BS_WALLED):
+            check(rc, "bs_cd_stream")
         break
     k = nout.value
-    st = [dict(nodes=s.nodes, leaves=s.leaves, ok=s.ok) for s in stats]
+    st = [dict(nodes=s.nodes, leaves=s.leaves, ok=s.ok, stopped=rc if rc > 0 else 0) for s in stats]
     words = words[:k]
     out = words if as_words else unpack(words, ctx.n + (1 if ab_side else 0))
     return out, cidx[:k], st

@@ -18,6 +18,10 @@ extern "C" {
 #endif
 
 enum {
+  BS_STOPPED = 1,       /* stopped early by the context's stop flag: the results cover the
+                           part completed (the reference's SIGTERM path, lower bounds) */
+  BS_WALLED = 2,        /* bs_cd_stream stopped by its wall limit (WZ_FH_WALL_SEC): the
+                           survivors cover the part streamed */
   BS_OK = 0,
   BS_ERR_ARG = -1,      /* bad argument (size, length, mode, null pointer) */
   BS_ERR_CUDA = -2,     /* a CUDA runtime call failed */
@@ -70,6 +74,15 @@ int bs_ctx_retarget(bs_ctx *ctx, int n, int a, int b, int c, int d);
 int bs_ctx_set_stream(bs_ctx *ctx, void *cuda_stream);
 /* Last error recorded by the device (timeouts), cleared on read. */
 int bs_ctx_device_status(bs_ctx *ctx);
+/* The context's stop flag: one int32 of pinned host memory mapped into the device, initially
+ * 0. Storing a nonzero value (a plain store, safe in a signal handler) makes the context's
+ * running and later bs_cd_stream and bs_complete_ab_batch calls stop within one device round
+ * (bs_cd_stream: one launch of at most round_us; bs_complete_ab_batch: the warps poll it every
+ * 1,024 search steps and before each candidate) and return BS_STOPPED with the part completed.
+ * Store 0 to clear it. Replaces the reference's g_fh_sigterm / cooperative stop
+ * (src/solver/wz_match.cpp:640-642, 712-713: a stream-walled arm that ignored SIGTERM hung
+ * its lane driver past walltime). */
+volatile int32_t *bs_ctx_stop_flag(bs_ctx *ctx);
 /* Kernel timing, for measurement: when enabled, the dominant kernel of each call (the Hall
  * kernel) is bracketed by CUDA events on the context stream. _read synchronises, returns the
  * summed duration and launch count since the last read, and the number of kernels this
@@ -99,12 +112,14 @@ int bs_hall_filter_dev(bs_ctx *ctx, const uint64_t *d_bits, long long npairs, in
  * about 4.2 MiB, which every GPU that loads the library keeps until the process exits.
  * n is the sequence length (4 <= n <= 63); d_bits holds 2 words per pair and d_pass
  * receives the decisions, both device memory owned by the caller; at most 1,048,576 pairs
- * per call (BS_ERR_CAP beyond). The work is enqueued on `stream` (a cudaStream_t; NULL is
- * the legacy default stream) and the call waits for it to return the status. The first call
- * on a device, and the first call with a new n, set the scratch up (device symbol address,
- * tables); make that first call before any stream capture. Calls share the one array and
- * keep the last call's tables: calls that overlap on the GPU (other streams, other host
- * threads) race and must be serialised by the caller. */
+ * per call (BS_ERR_CAP beyond); npairs = 0 only checks the set-up. The work is enqueued on
+ * `stream` (a cudaStream_t; NULL is the legacy default stream), and every call ends by
+ * synchronising that stream to read the status word back. The first call on a device, and
+ * the first call with a new n, set the scratch up (device symbol address, kernel attributes,
+ * tables uploaded from static host arrays); make that first call before any stream capture.
+ * Calls share the one array and keep the last call's tables and band list; the counters are
+ * cleared by every call. Calls that overlap on the GPU (other streams, other host threads)
+ * race and must be serialised by the caller. */
 int bs_hall_filter_noalloc(int n, const uint64_t *d_bits, long long npairs, uint8_t *d_pass,
                            void *stream);
 /* Diagnostics: raw tensor-core accumulators for npairs (multiple of 64, <= 65536) pairs,
@@ -151,6 +166,11 @@ typedef struct {
   long long round_us;        /* longest device launch in microseconds (0 = 25,000); walks still
                                 running then suspend, and when few remain the host splits them
                                 into their remaining subtrees (small values exercise that path) */
+  double wall_sec;           /* WZ_FH_WALL_SEC (wz_match.cpp:643-653, 715-718): > 0 abandons
+                                the stream once this many seconds pass without a new survivor
+                                (counted from the call's start, then from the last launch that
+                                found one); the call returns BS_WALLED with the survivors of the
+                                waves it completed, which the lane still drains */
 } bs_stream_opts;
 
 typedef struct { long long nodes, leaves, ok; } bs_cell_stats;
@@ -236,7 +256,9 @@ typedef struct {
   int32_t canon;        /* root + reversal canonicalisation (1 unless WZ_FH_NO_CANON) */
   int32_t m;            /* class modulus of the rows: 3 or 6 */
   int32_t first_hit;    /* 1: candidates after the lowest-index hit are not run */
-  int32_t reserved;
+  int32_t a2;           /* WZ_FH_A2: 0 off, 2 the A2 row-reachability prune (wz_match.cpp:
+                           977-1047, 1069-1072); mode 1, the reference's shadow instrument, is
+                           not built (BS_ERR_ARG) */
   double max_seconds;   /* per-candidate wall limit on the device (0 = none) */
 } bs_ab_opts;
 

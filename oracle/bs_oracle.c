@@ -398,6 +398,9 @@ typedef struct {
   int nrows;
   int *stack;  /* (half+2) lists of nrows row indices */
   int *stack_len;
+  /* WZ_FH_A2 = 2 (wz_match.cpp:977-1047): blocks of residues {r, s = (L-1-r) mod m}, the
+     free middle's block at odd L, quads left per block from depth p on */
+  int a2, a2_nblk, a2_r[8], a2_s[8], a2_mid[8], a2_cnt[40][8];
 } ab_state;
 
 /* fh_place / fh_unplace, V1 form (wz_match.cpp:1127-1161). */
@@ -447,7 +450,51 @@ static unsigned ab_outer_mask(ab_state *S, int d) {
   return OUT3[pat][R[0] / 2 + 2][R[1] / 2 + 4][R[2] / 2 + 6];
 }
 
-/* fh_abp_filter, wz_match.cpp:1055-1078 (A2 off). */
+/* a2_self_ok / a2_row_ok, wz_match.cpp:1017-1038 */
+static int a2_self_ok(int u, int v, int q) {
+  if ((u | v) & 1) return 0;
+  if (abs(u) > 2 * q || abs(v) > 2 * q) return 0;
+  return ((u - v) & 3) == 0;
+}
+static int a2_row_ok(const ab_state *S, const int8_t *row, int p) {
+  for (int b = 0; b < S->a2_nblk; b++) {
+    int r = S->a2_r[b], s = S->a2_s[b], q = S->a2_cnt[p][b];
+    int ur = row[r] - S->pa[r], vr = row[8 + r] - S->pb[r];
+    if (r != s) {
+      int us = row[s] - S->pa[s], vs = row[8 + s] - S->pb[s];
+      int t0 = ur + vr + us + vs, t1 = ur - vr + us - vs, t2 = ur + vr - us - vs, t3 = ur - vr - us + vs;
+      if ((t0 | t1 | t2 | t3) & 3) return 0;
+      int l1 = (abs(t0) + abs(t1) + abs(t2) + abs(t3)) >> 2;
+      if (l1 > q || ((q - l1) & 1)) return 0;
+    } else if (S->a2_mid[b]) {
+      if (!a2_self_ok(ur - 1, vr - 1, q) && !a2_self_ok(ur - 1, vr + 1, q) &&
+          !a2_self_ok(ur + 1, vr - 1, q) && !a2_self_ok(ur + 1, vr + 1, q)) return 0;
+    } else if (!a2_self_ok(ur, vr, q)) {
+      return 0;
+    }
+  }
+  return 1;
+}
+
+/* init_a2_tables, wz_match.cpp:1000-1016 */
+static void a2_init(ab_state *S) {
+  int L = S->L, m = S->m, half = L / 2, blk_of[8];
+  for (int c = 0; c < 8; c++) blk_of[c] = -1;
+  S->a2_nblk = 0;
+  for (int c = 0; c < m; c++) {
+    if (blk_of[c] >= 0) continue;
+    int s = ((L - 1 - c) % m + m) % m;
+    S->a2_r[S->a2_nblk] = c; S->a2_s[S->a2_nblk] = s; S->a2_mid[S->a2_nblk] = 0;
+    blk_of[c] = blk_of[s] = S->a2_nblk++;
+  }
+  if (L % 2 == 1) S->a2_mid[blk_of[half % m]] = 1;
+  for (int p = 0; p <= half + 1 && p < 40; p++) {
+    for (int b = 0; b < 8; b++) S->a2_cnt[p][b] = 0;
+    for (int i = p; i < half; i++) S->a2_cnt[p][blk_of[i % m]]++;
+  }
+}
+
+/* fh_abp_filter, wz_match.cpp:1055-1078 (the A2 prune in mode 2). */
 static int ab_row_filter(ab_state *S, int d) {
   int *src = S->stack + (size_t)d * S->nrows;
   int *dst = S->stack + (size_t)(d + 1) * S->nrows;
@@ -460,6 +507,7 @@ static int ab_row_filter(ab_state *S, int d) {
       int dk = row[c] - S->pa[c], dr = row[8 + c] - S->pb[c];
       if (dk < -rem || dk > rem || dr < -rem || dr > rem) { ok = 0; break; }
     }
+    if (ok && S->a2 == 2 && !a2_row_ok(S, row, d + 1)) ok = 0;
     if (ok) dst[nd++] = src[t];
   }
   S->stack_len[d + 1] = nd;
@@ -573,10 +621,20 @@ int or_complete_ab(int n, int sigA, int sigB, const int8_t *C, const int8_t *D,
                    long long budget, int outer_k, int early, int canon, int m,
                    const int8_t *rows, int nrows, int8_t *Aout, int8_t *Bout,
                    long long *nodes) {
+  return or_complete_ab_a2(n, sigA, sigB, C, D, budget, outer_k, early, canon, m, rows, nrows, 0,
+                           Aout, Bout, nodes);
+}
+
+int or_complete_ab_a2(int n, int sigA, int sigB, const int8_t *C, const int8_t *D,
+                      long long budget, int outer_k, int early, int canon, int m,
+                      const int8_t *rows, int nrows, int a2, int8_t *Aout, int8_t *Bout,
+                      long long *nodes) {
   tables_init();
   ab_state *S = (ab_state *)calloc(1, sizeof(ab_state));
   int n1 = n + 1;
   S->n = n; S->L = n1; S->half = n1 / 2; S->m = m;
+  S->a2 = a2;
+  if (a2) a2_init(S);
   S->budget = budget; S->outer_k = outer_k; S->early = early; S->canon = canon;
   if (nodes) *nodes = 0;
   /* target = -CD, prefilter: wz_match.cpp:1300-1308 */

@@ -67,6 +67,10 @@ long long or_cd_stream(int n, int L, int m, const int *tx, const int *ty,
 int or_complete_ab(int n, int sigA, int sigB, const int8_t *C, const int8_t *D,
                    long long budget, int outer_k, int early, int canon, int m,
                    const int8_t *rows, int nrows, int8_t *A, int8_t *B, long long *nodes);
+/* The same with WZ_FH_A2 (0 off, 2 the A2 row-reachability prune, wz_match.cpp:977-1047). */
+int or_complete_ab_a2(int n, int sigA, int sigB, const int8_t *C, const int8_t *D,
+                      long long budget, int outer_k, int early, int canon, int m,
+                      const int8_t *rows, int nrows, int a2, int8_t *A, int8_t *B, long long *nodes);
 
 /* Hall microbench input generator (per-pair deterministic; the same definition as the
  * product's device generator): words[2p], words[2p+1] = C, D of pair p. */

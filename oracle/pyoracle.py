@@ -53,6 +53,10 @@ def lib():
                                      C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_int, i8p, i8p,
                                      C.POINTER(C.c_longlong)]
         L.or_complete_ab.restype = C.c_int
+        L.or_complete_ab_a2.argtypes = [C.c_int, C.c_int, C.c_int, i8p, i8p, C.c_longlong, C.c_int,
+                                        C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_int, i8p,
+                                        i8p, C.POINTER(C.c_longlong)]
+        L.or_complete_ab_a2.restype = C.c_int
         L.or_outer_tables.argtypes = [u8p, u8p]
         L.or_gen_hall_pairs.argtypes = [C.c_int, C.c_longlong, C.c_uint64,
                                         np.ctypeslib.ndpointer(dtype=np.uint64, flags="C_CONTIGUOUS"),
@@ -132,7 +136,8 @@ def cd_stream(n, tx, ty, m=6, pinX=False, pinY=False, rev=False, endpos=False, c
             dict(nodes=st.nodes, leaves=st.leaves, ok=st.ok))
 
 
-def complete_ab(n, sigA, sigB, C_, D, budget, rows=None, m=6, outer_k=3, early=True, canon=True):
+def complete_ab(n, sigA, sigB, C_, D, budget, rows=None, m=6, outer_k=3, early=True, canon=True,
+                a2=0):
     C_, D = (np.ascontiguousarray(v, np.int8) for v in (C_, D))
     A = np.zeros(n + 1, np.int8)
     B = np.zeros(n + 1, np.int8)
@@ -142,8 +147,8 @@ def complete_ab(n, sigA, sigB, C_, D, budget, rows=None, m=6, outer_k=3, early=T
         ptr, nr = rows.ctypes.data_as(C.c_void_p), rows.shape[0]
     else:
         ptr, nr = None, 0
-    v = lib().or_complete_ab(n, sigA, sigB, C_, D, budget, outer_k, int(early), int(canon), m,
-                             ptr, nr, A, B, C.byref(nodes))
+    v = lib().or_complete_ab_a2(n, sigA, sigB, C_, D, budget, outer_k, int(early), int(canon), m,
+                                ptr, nr, int(a2), A, B, C.byref(nodes))
     return v, nodes.value, A, B
 
 

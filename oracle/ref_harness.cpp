@@ -165,6 +165,13 @@ long long refh_stream_for(int L, const int *tx, const int *ty, int m, int pinX, 
   return written;
 }
 
+// WZ_FH_A2 mode for later refh_complete calls, with the block tables of modulus m
+// (init_a2_tables, as wz_match.cpp's lane does before its first-hit loop).
+void refh_set_a2(int mode, int m) {
+  G_A2 = mode;
+  init_a2_tables(G_N1, m);
+}
+
 void refh_outer_tables(unsigned char *o2, unsigned char *o3) {
   memcpy(o2, OUTER2, sizeof OUTER2);
   memcpy(o3, OUTER3, sizeof OUTER3);

@@ -29,9 +29,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
-if len(sys.argv) < 2:
-    sys.exit("usage: make_golden.py REF [ab|cdprune]   (REF: root of the reference repository)")
-REF = sys.argv[1]
+REF = None  # the reference repository's root, from the command line (main)
 sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
 
@@ -240,6 +238,10 @@ def cd_prune_streams(R):
 
 
 def main():
+    global REF
+    if len(sys.argv) < 2:
+        sys.exit("usage: make_golden.py REF [ab|cdprune]   (REF: root of the reference repository)")
+    REF = sys.argv[1]
     R = load_ref()
     if len(sys.argv) > 2 and sys.argv[2] == "ab":
         ab_streams(R)

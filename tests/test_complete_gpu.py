@@ -45,6 +45,32 @@ def test_completions_golden(gpu):
         ctx.close()
 
 
+def test_a2_completions_golden(gpu):
+    """The A2 row prune on the device (bs_ab_opts.a2 = 2) against the reference's fh_complete_ab
+    under WZ_FH_A2=2 (tests/golden/a2_complete_golden.npz): verdicts, charged nodes and the
+    first completion."""
+    from bs45_quantum_explorer_gb300.complete import complete_ab
+    from bs45_quantum_explorer_gb300.hall import Context
+    g = np.load(os.path.join(G, "a2_complete_golden.npz"))
+    cases, cd, rows = g["cases"].astype(np.int64), g["cd"], g["rows"]
+    groups = {}
+    for i, row in enumerate(cases):
+        n, a, b, budget = (int(x) for x in row[:4])
+        groups.setdefault((n, a, b, budget), []).append(i)
+    for (n, a, b, budget), idx in groups.items():
+        ctx = Context(n, (a, b) + _cd_sig(n, a, b))
+        cands = np.stack([cd[int(cases[i, 8])] for i in idx])
+        rr = [rows[int(cases[i, 4]):int(cases[i, 4]) + int(cases[i, 5])] for i in idx]
+        for a2, vcol, ncol in ((2, 6, 7), (0, 9, 10)):
+            v, nodes, A, B = complete_ab(ctx, cands, budget, rows_per_cand=rr, a2=a2)
+            for t, i in enumerate(idx):
+                assert (v[t], nodes[t]) == (cases[i, vcol], cases[i, ncol]), (n, a, b, budget, a2, t)
+                if a2 == 2 and v[t] == 0:
+                    assert (A[t] == unpack(np.uint64(cases[i, 11]), n + 1)).all()
+                    assert (B[t] == unpack(np.uint64(cases[i, 12]), n + 1)).all()
+        ctx.close()
+
+
 def _cd_sig(n, a, b):
     """Any (c, d) completing the signature norm; the completer only reads |a|, |b|."""
     rest = 4 * n + 2 - a * a - b * b

@@ -55,6 +55,25 @@ def test_lane_cd_prune_matches_reference_runs(gpu):
     _replay(cases)
 
 
+def test_lane_a2_matches_reference_runs(gpu):
+    """WZ_FH_A2=2 (the A2 row prune) in the drop-in binary and in the library lane against
+    the reference binary's runs (tests/golden/a2_lane_golden.json)."""
+    from bs45_quantum_explorer_gb300.hall import Context
+    from bs45_quantum_explorer_gb300.lane import run_lane
+    cases = json.load(open(os.path.join(HERE, "golden", "a2_lane_golden.json")))
+    assert len(cases) >= 100
+    _replay(cases)
+    ctxs = {}
+    for c in cases:
+        key = (c["n"], tuple(c["sig"]))
+        if key not in ctxs:
+            ctxs[key] = Context(*key)
+        res = run_lane(ctxs[key], c["n"], tuple(c["sig"]), **lane_kwargs(c["settings"]))
+        check_run_lane(res, summary_of(c["semantic"]), (c["n"], c["sig"], c["settings"]))
+    for x in ctxs.values():
+        x.close()
+
+
 def _replay(cases):
     from make_lane_golden import cellsize_lines, semantic
     exe = _bin()
@@ -124,7 +143,8 @@ def lane_kwargs(st):
                 orbit_canon=bool(int(st.get("WZ_FH_ORBIT_CANON", 0))), orbit_q=int(st.get("WZ_FH_ORBIT_Q", 0)),
                 qprune=bool(int(st.get("WZ_FH_ORBIT_QPRUNE", 0))), prof_order=int(st.get("WZ_FH_PROF_ORDER", 0)),
                 outer_k=int(st.get("WZ_FH_OUTER_K", 3)), early=int(st.get("WZ_FH_EARLY_CHECK", 1)) != 0,
-                canon="WZ_FH_NO_CANON" not in st, m6=True, thm211b=True, thm212=True)
+                canon="WZ_FH_NO_CANON" not in st, m6=True, thm211b=True, thm212=True,
+                a2=int(st.get("WZ_FH_A2", 0)))
 
 
 def check_run_lane(res, want, ctx):

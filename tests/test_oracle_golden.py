@@ -91,6 +91,32 @@ def test_completions_match_reference(oracle):
             assert (A == unpack(aw, n + 1)).all() and (B == unpack(bw, n + 1)).all()
 
 
+def _a2_cases():
+    g = np.load(os.path.join(G, "a2_complete_golden.npz"))
+    return g["cases"].astype(np.int64), g["cd"], g["rows"]
+
+
+def test_a2_completions_match_reference(oracle):
+    """The A2 row prune (WZ_FH_A2=2): the reference's verdicts, charged node counts and
+    completions with the prune on; and with it off, its node counts (never fewer)."""
+    cases, cd, rows = _a2_cases()
+    assert len(cases) >= 1000
+    assert (cases[:, 7] < cases[:, 10]).sum() > 100  # the prune cuts real nodes
+    for row in cases:
+        n, a, b, budget, roff, nrows, v2, n2, ci, v0, n0 = (int(x) for x in row[:11])
+        if budget == 0 and n > 17:
+            continue  # exact completions at the larger n run in the GPU suite
+        C_, D = unpack(cd[ci], n)
+        rr = rows[roff:roff + nrows]
+        got = oracle.complete_ab(n, a, b, C_, D, budget, rows=rr, a2=2)
+        assert got[:2] == (v2, n2), (n, a, b, budget)
+        if v2 == 0:
+            assert (got[2] == unpack(np.uint64(row[11]), n + 1)).all()
+            assert (got[3] == unpack(np.uint64(row[12]), n + 1)).all()
+        assert oracle.complete_ab(n, a, b, C_, D, budget, rows=rr)[:2] == (v0, n0)
+        assert n2 <= n0 or budget > 0
+
+
 def test_controls_match_reference(oracle):
     ctl = json.load(open(os.path.join(G, "controls_golden.json")))
     quads = {q["file"]: q for q in json.load(open(os.path.join(G, "known_quads.json")))}

@@ -57,6 +57,43 @@ def test_noalloc_matches_allocating_entry_point(gpu, oracle):
         assert np.array_equal(got[:4096], ref)
 
 
+def _near_threshold(n, oracle, npairs, seed, width):
+    """Pairs whose exact max pair PSD lies within +-width of the limit 4n+2.5, so that the
+    margin band and the FP64 recheck run."""
+    from bs45_quantum_explorer_gb300.workloads import unpack_pairs
+    words = oracle.gen_hall_pairs(n, npairs, seed=seed, nthreads=8)
+    ct, st = oracle.hall_tables(n)
+    X = unpack_pairs(words, n).astype(np.float64)
+    re, im = X @ ct[1:, :n].T, X @ st[1:, :n].T
+    mx = (re * re + im * im).sum(axis=1).max(axis=1)
+    return np.ascontiguousarray(words[np.abs(mx - (4 * n + 2.5)) < width])
+
+
+def test_noalloc_on_caller_stream_longest_length_and_full_size(gpu, oracle):
+    """A caller-supplied stream, the longest accepted length (n = 63, where the FP64 recheck
+    uses the most shared memory), a call at the maximum size, and an empty call."""
+    import torch
+    s = torch.cuda.Stream()
+    cases = [(63, (12, 10, 3, 1), _near_threshold(63, oracle, 1 << 18, 0xB545D1, 16.0)),
+             (42, (7, 11, 0, 0), oracle.gen_hall_pairs(42, MAX_PAIRS, seed=0xB545D2, nthreads=8))]
+    for n, sig, words in cases:
+        npairs = len(words)
+        assert npairs > 20
+        d_words = torch.from_numpy(words.view(np.int64).reshape(-1).copy()).cuda()
+        d_pass = torch.full((npairs,), 7, dtype=torch.uint8, device="cuda")
+        torch.cuda.synchronize()
+        for _ in range(2):
+            with torch.cuda.stream(s):
+                rc = _noalloc(n, d_words, npairs, d_pass, s.cuda_stream)
+            assert rc == 0, rc
+            s.synchronize()
+            got = d_pass.cpu().numpy()
+            want = _reference_mask(n, sig, d_words, npairs)
+            assert np.array_equal(got, want), (n, npairs, int((got != want).sum()))
+    d_pass = torch.zeros(1, dtype=torch.uint8, device="cuda")
+    assert _noalloc(42, d_words, 0, d_pass, s.cuda_stream) == 0
+
+
 def test_noalloc_refuses_oversized_request(gpu):
     import torch
     d_words = torch.zeros(2, dtype=torch.int64, device="cuda")
