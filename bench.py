@@ -378,13 +378,89 @@ def run_first_hit(seconds, cpu_seconds=10.0, with_cpu=True, drain_top=50000):
     return out
 
 
-def run_c3(max_cells=0, batch=16, topk=256):
+def run_spike(budget=1 << 20, ncand=2048):
+    """The reference's own GPU completer (src/solver/gpu/fh_gpu_spike.cu, compiled unmodified
+    for sm_103a into oracle/_ref/fh_gpu_spike) beside ours on the same candidates: the first
+    `ncand` drained candidates (flattest first) of the first-hit workload's first kept cell,
+    at the same node budget. The spike has no allowed rows, no outer-lag tables and no early
+    check, so ours runs with those off here too (rows=None, outer_k=0, early=False): the two
+    searches then charge the same nodes, which the line checks (verdict histogram and total)."""
+    import re
+    import subprocess
+    import tempfile
+    import torch
+    from bs45_quantum_explorer_gb300.complete import complete_ab, flat_topk
+    from bs45_quantum_explorer_gb300.hall import Context, unpack
+    from bs45_quantum_explorer_gb300.serve import serving_list
+    from bs45_quantum_explorer_gb300.stream import cd_stream
+    exe = os.path.join(ROOT, "oracle", "_ref", "fh_gpu_spike")
+    if not os.path.exists(exe):
+        return {"unavailable": "oracle/_ref/fh_gpu_spike was not built on this machine"}
+    cells, kept, _, m = serving_list(FH_N, FH_SIG)
+    rng = np.random.default_rng(SEED)
+    s = int(rng.integers(0, len(kept) - 4096))
+    pi = next(i for i in range(s, s + 4096) if kept[i])
+    c = cells[pi]
+    ctx = Context(FH_N, FH_SIG)
+    surv, _, _ = cd_stream(ctx, [(list(c.tx[:m]), list(c.ty[:m]))], m=m, as_words=True,
+                           pins=[(c.pinX, c.pinY)], limit=500000)
+    order, _ = flat_topk(ctx, surv, len(surv), ncand)
+    cand = unpack(surv[order[:ncand]], FH_N)
+    complete_ab(ctx, cand[:64], budget, outer_k=0, early=False)  # warm-up
+    torch.cuda.synchronize()
+    ctx.timing(True)
+    t0 = time.perf_counter()
+    v, nodes, _, _ = complete_ab(ctx, cand, budget, outer_k=0, early=False)
+    api_s = time.perf_counter() - t0
+    dev_ms, _, _ = ctx.timing_read()
+    ctx.close()
+    ours_hist = [int((v == k).sum()) for k in range(4)]
+    with tempfile.TemporaryDirectory() as tmp:
+        dump = os.path.join(tmp, "cands.txt")
+        with open(dump, "w") as f:
+            for x in cand:
+                f.write(" ".join(map(str, x[0])) + " | " + " ".join(map(str, x[1])) + "\n")
+        p = subprocess.run([exe, str(FH_N), *map(str, FH_SIG), dump, str(budget), str(ncand), "4"],
+                           capture_output=True, text=True, timeout=900)
+    out = p.stdout
+    ref = {}
+    mm = re.search(r"GPU_SPIKE: cpu_cands_per_s=([\d.]+) gpu_cands_per_s=([\d.]+)", out)
+    if mm:
+        ref["cpu_1core_cands_per_s"], ref["thread_per_cand_cands_per_s"] = float(mm[1]), float(mm[2])
+    mm = re.search(r"GPU_SPIKE_V2A_SORTED: cands_per_s=([\d.]+)", out)
+    if mm:
+        ref["thread_per_cand_sorted_cands_per_s"] = float(mm[1])
+    mm = re.search(r"GPU_SPIKE_V2B_WARP: cands_per_s=([\d.]+).*hist (\d+)/(\d+)/(\d+)/(\d+) nodes=(\d+)", out)
+    if mm:
+        ref["warp_per_cand_cands_per_s"] = float(mm[1])
+        ref["hist"] = [int(mm[k]) for k in range(2, 6)]
+        ref["nodes"] = int(mm[6])
+    total = int(nodes.sum())
+    return {"workload": f"the first {ncand} drained candidates (flattest first) of raw cell {pi}, "
+                        f"n={FH_N} sig={FH_SIG}, budget {budget}; no allowed rows, no outer-lag "
+                        "tables, no early check (the spike's search)",
+            "rc": p.returncode, "reference_spike": ref,
+            "ours": {"cands_per_s_device": ncand / (dev_ms * 1e-3) if dev_ms > 0 else None,
+                     "cands_per_s_api": ncand / api_s, "nodes": total,
+                     "nodes_per_s_device": total / (dev_ms * 1e-3) if dev_ms > 0 else None,
+                     "hist": ours_hist},
+            "same_verdicts": ref.get("hist") == ours_hist,
+            "node_rule": "the same charge per placed quad; after a budget abort the reference's "
+                         "solver (and ours) charges one more node per ancestor with an eligible "
+                         "quad left, which the spike does not, so totals differ by those when "
+                         "candidates abort"}
+
+
+def run_c3(max_cells=0, batch=32, topk=256, workers=3):
     """C3: the full C,D stream at n = 30, sig (1,7,6,6): every kept cell of the ORDER=3 list
     (2.11b + 2.12, orbit canon with the quad switch: 97,141 cells, 7,987 kept) streamed whole,
-    with its flattest-256 keep. Reports DFS nodes/s and the stream's algorithmic HBM rate:
-    32 B per DFS node (a 16 B frontier record written and read once) + 16 B per leaf handed to
-    the filter + 24 B per survivor (packed C,D, DFS rank, score)."""
-    import numpy as np
+    with its flattest-256 keep. Batches of `batch` cells go to `workers` host threads, each with
+    its own context (own CUDA stream and buffers), so one batch's host work (ordering its
+    survivors, the keeps) overlaps the next batch's DFS on the device. Reports DFS nodes/s and
+    the stream's algorithmic HBM rate: 32 B per DFS node (a 16 B frontier record written and
+    read once) + 16 B per leaf handed to the filter + 24 B per survivor (packed C,D, DFS rank,
+    score)."""
+    import concurrent.futures as cf
     import torch
     from bs45_quantum_explorer_gb300.cells import cell_list
     from bs45_quantum_explorer_gb300.complete import flat_topk
@@ -396,31 +472,48 @@ def run_c3(max_cells=0, batch=16, topk=256):
     live = [i for i in range(len(kept)) if kept[i]]
     if max_cells:
         live = live[:max_cells]
-    ctx = Context(n, sig)
-    cd_stream(ctx, [(list(cells[live[0]].tx[:m]), list(cells[live[0]].ty[:m]))], m=m, as_words=True)
+    ctxs = [Context(n, sig) for _ in range(workers)]
+    for ctx in ctxs:  # warm-up: buffers of every context
+        cd_stream(ctx, [(list(cells[live[0]].tx[:m]), list(cells[live[0]].ty[:m]))], m=m, as_words=True)
     torch.cuda.synchronize()
-    nodes = leaves = surv_total = kept_total = 0
+    batches = [live[b:b + batch] for b in range(0, len(live), batch)]
+    free = list(range(workers))
+    import threading
+    lock = threading.Lock()
+
+    def one(group):
+        with lock:
+            k = free.pop()
+        ctx = ctxs[k]
+        try:
+            batch_cells = [(list(cells[i].tx[:m]), list(cells[i].ty[:m])) for i in group]
+            surv, cidx, st = cd_stream(ctx, batch_cells, m=m, as_words=True, cap=1 << 23,
+                                       survivor_cap=1 << 23)
+            kept_n = 0
+            bounds = np.searchsorted(cidx, np.arange(len(group) + 1))
+            for j in range(len(group)):  # each cell's flattest 256 (one batch: the whole cell)
+                lo, hi = int(bounds[j]), int(bounds[j + 1])
+                if hi > lo:
+                    order, _ = flat_topk(ctx, surv[lo:hi], hi - lo, topk)
+                    kept_n += len(order)
+            return (sum(x["nodes"] for x in st), sum(x["leaves"] for x in st), len(surv), kept_n)
+        finally:
+            with lock:
+                free.append(k)
     t0 = time.perf_counter()
-    for b in range(0, len(live), batch):
-        group = live[b:b + batch]
-        batch_cells = [(list(cells[i].tx[:m]), list(cells[i].ty[:m])) for i in group]
-        surv, cidx, st = cd_stream(ctx, batch_cells, m=m, as_words=True, cap=1 << 23,
-                                   survivor_cap=1 << 23)
-        nodes += sum(x["nodes"] for x in st)
-        leaves += sum(x["leaves"] for x in st)
-        surv_total += len(surv)
-        # each cell's flattest 256 (one batch covering the whole cell)
-        bounds = np.searchsorted(cidx, np.arange(len(group) + 1))
-        for j in range(len(group)):
-            lo, hi = int(bounds[j]), int(bounds[j + 1])
-            if hi > lo:
-                order, _ = flat_topk(ctx, surv[lo:hi], hi - lo, topk)
-                kept_total += len(order)
+    with cf.ThreadPoolExecutor(max_workers=workers) as ex:
+        parts = list(ex.map(one, batches))
     dt = time.perf_counter() - t0
-    ctx.close()
+    for ctx in ctxs:
+        ctx.close()
+    nodes = sum(p[0] for p in parts)
+    leaves = sum(p[1] for p in parts)
+    surv_total = sum(p[2] for p in parts)
+    kept_total = sum(p[3] for p in parts)
     alg = 32 * nodes + 16 * leaves + 24 * surv_total
     return {"workload": f"C,D stream n={n} sig={sig}: {len(live)} kept cells of the ORDER=3 list "
-                        f"({len(kept)} cells, digest {digest}) streamed whole, flattest-{topk} per cell",
+                        f"({len(kept)} cells, digest {digest}) streamed whole, flattest-{topk} per cell; "
+                        f"batches of {batch} cells on {workers} host threads with their own contexts",
             "cells": len(live), "dfs_nodes": nodes, "leaves": leaves, "survivors": surv_total,
             "kept_topk": kept_total, "seconds": dt, "dfs_nodes_per_s": nodes / dt,
             "filtered_cands_per_s": leaves / dt, "cells_per_s": len(live) / dt,
@@ -476,12 +569,13 @@ def run_join(n=24):
             "probe_algorithmic_gb_per_s": alg / (probe_ms * 1e-3) / 1e9 if probe_ms > 0 else None}
 
 
-def run_serving(n_jobs=12, tail=2, rate=2.0, slots=4, max_cells=64):
+def run_serving(n_jobs=12, tail=2, rate=2.0, slots=4, max_cells=4096):
     """C5: a seeded Poisson stream of first-hit jobs, n uniform in 20..42 with a signature from
-    classes(n) and a contiguous ORDER=3 range of 1..max_cells raw cells, plus `tail` n = 42
-    ranges; per-job budget 2^16, BUF_CAP 2000, DRAIN_TOP 64 (reduced from the production lane
-    so the mix finishes in about a minute). Lists are built before the clock starts, in
-    parallel (a service keeps them). Reports cells/s, nodes/s and p50/p99 job latency."""
+    classes(n) and a contiguous ORDER=3 range of 1..max_cells raw cells (4,096: the workload's
+    stated range), plus `tail` n = 42 ranges; per-job budget 2^16, BUF_CAP 2000, DRAIN_TOP 64
+    (the per-cell work reduced from the production lane so that the mix ends in about a
+    minute). Lists are built before the clock starts, in parallel (a service keeps them).
+    Reports cells/s, nodes/s and p50/p99 job latency."""
     import concurrent.futures as cf
     from bs45_quantum_explorer_gb300.serve import Server, poisson_trace, serving_list
     plan = poisson_trace(nj=n_jobs, rate=rate, seed=SEED, n_range=(20, 42), max_cells=max_cells,
@@ -526,6 +620,8 @@ def main():
                     help="run only the full-space join for BS(N+1, N), one signature")
     ap.add_argument("--c3", type=int, default=None, metavar="CELLS",
                     help="run only the n=30 full stream over the first CELLS kept cells (0: all)")
+    ap.add_argument("--spike", action="store_true",
+                    help="run only the reference's GPU completer spike beside ours and print its line")
     ap.add_argument("--fh-drain", type=int, default=50000,
                     help="DRAIN_TOP of the first-hit lane (a smaller value makes a small profiling case)")
     ap.add_argument("--fh-seconds", type=float, default=30.0,
@@ -542,7 +638,8 @@ def main():
     if args.stream_only:
         run_stream_only(args)
         return
-    if args.first_hit is not None or args.serve or args.c3 is not None or args.join is not None:
+    if args.first_hit is not None or args.serve or args.c3 is not None or args.join is not None \
+            or args.spike:
         from bs45_quantum_explorer_gb300 import build_library
         build_library()
         if args.first_hit is not None:
@@ -554,6 +651,8 @@ def main():
             print(json.dumps(run_c3(args.c3)), flush=True)
         if args.join is not None:
             print(json.dumps(run_join(args.join)), flush=True)
+        if args.spike:
+            print(json.dumps(run_spike()), flush=True)
         return
 
     import numpy as np

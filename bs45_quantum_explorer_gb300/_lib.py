@@ -45,7 +45,9 @@ class StreamOpts(C.Structure):
                 ("cd_prune", C.c_int32), ("hall_mode", C.c_int32), ("ab_side", C.c_int32),
                 ("target_prefixes", C.c_longlong), ("leaf_chunk", C.c_longlong),
                 ("survivor_cap", C.c_longlong), ("limit", C.c_longlong),
-                ("round_us", C.c_longlong), ("wall_sec", C.c_double)]
+                ("round_us", C.c_longlong), ("wall_sec", C.c_double),
+                ("fine_nodes", C.c_double), ("wave_nodes", C.c_double),
+                ("dfs_blocks", C.c_int32), ("reserved", C.c_int32)]
 
 
 class CellStats(C.Structure):
@@ -65,7 +67,8 @@ class AbCand(C.Structure):
 class AbOpts(C.Structure):
     _fields_ = [("budget", C.c_longlong), ("outer_k", C.c_int32), ("early", C.c_int32),
                 ("canon", C.c_int32), ("m", C.c_int32), ("first_hit", C.c_int32),
-                ("a2", C.c_int32), ("max_seconds", C.c_double)]
+                ("a2", C.c_int32), ("max_seconds", C.c_double),
+                ("blocks_per_sm", C.c_int32), ("reserved", C.c_int32)]
 
 
 _lib = None

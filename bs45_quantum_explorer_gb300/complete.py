@@ -33,7 +33,7 @@ assert AB_CAND.itemsize == C.sizeof(AbCand)
 
 
 def complete_ab(ctx, cands, budget, rows_per_cand=None, m=6, outer_k=3, early=True, canon=True,
-                first_hit=False, max_seconds=0.0, rows=None, a2=0):
+                first_hit=False, max_seconds=0.0, rows=None, a2=0, blocks_per_sm=0):
     """cands: int8 [k, 2, n] (C, D) or uint64 words [k, 2]. Allowed A,B rows (int8 [r, 16]):
     `rows` shared by every candidate (one cell's list), or rows_per_cand, a list of arrays
     (empty = unconstrained); neither: unconstrained. a2 = 2: WZ_FH_A2=2, the A2 row prune.
@@ -61,7 +61,8 @@ def complete_ab(ctx, cands, budget, rows_per_cand=None, m=6, outer_k=3, early=Tr
         all_rows = np.concatenate(parts) if parts else np.zeros((1, 16), np.int8)
     all_rows = np.ascontiguousarray(all_rows)
     opt = AbOpts(budget=budget, outer_k=outer_k, early=int(early), canon=int(canon), m=m,
-                 first_hit=int(first_hit), a2=int(a2), max_seconds=max_seconds)
+                 first_hit=int(first_hit), a2=int(a2), max_seconds=max_seconds,
+                 blocks_per_sm=int(blocks_per_sm), reserved=0)
     n1 = ctx.n + 1
     verdict = np.zeros(max(1, k), np.int32)
     nodes = np.zeros(max(1, k), np.int64)

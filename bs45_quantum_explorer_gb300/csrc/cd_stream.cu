@@ -795,11 +795,13 @@ extern "C" int bs_cd_stream(bs_ctx *ctx, const bs_cell *cells, int ncells, const
   const int block = 256;
   // register budget variant (BS_DFS_BLOCKS=5 or 6 select the 48- and 40-register builds) and
   // the grid of exactly the blocks that fit at once
-  static const int dfs_blocks = [] {
+  static const int env_blocks = [] {
     const char *e = getenv("BS_DFS_BLOCKS");
     const int b = e ? atoi(e) : 4;
     return (b == 5 || b == 6) ? b : 4;
   }();
+  if (opt->dfs_blocks != 0 && (opt->dfs_blocks < 4 || opt->dfs_blocks > 6)) return BS_ERR_ARG;
+  const int dfs_blocks = opt->dfs_blocks ? opt->dfs_blocks : env_blocks;
   const bool reach = prune[0].reach;  // the same for every cell of the batch
   auto dfs_kernel = reach ? cd_dfs_kernel<4, true>
                           : dfs_blocks == 6 ? cd_dfs_kernel<6, false>
@@ -882,7 +884,8 @@ extern "C" int bs_cd_stream(bs_ctx *ctx, const bs_cell *cells, int ncells, const
   // than walkers remain, the suspended walks are split into their remaining subtrees, so one
   // large subtree never holds the GPU with a few walkers.
   const long long limit = opt->limit > 0 ? opt->limit : 0;
-  const double FINE_NODES = 2e4, WAVE_NODES = 8e9, NOMINAL_RATE = 2e10;
+  const double FINE_NODES = opt->fine_nodes > 0 ? opt->fine_nodes : 2e4;
+  const double WAVE_NODES = opt->wave_nodes > 0 ? opt->wave_nodes : 8e9, NOMINAL_RATE = 2e10;
   const unsigned long long ROUND_NS = opt->round_us > 0 ? (unsigned long long)opt->round_us * 1000ULL
                                                         : 25000000ULL;
   const long long walkers = (long long)grid * block / 8;  // eight lanes walk one subtree

@@ -708,7 +708,8 @@ extern "C" int bs_complete_ab_batch(bs_ctx *ctx, const bs_ab_cand *cands, long l
     hc[i].mask_off = set_of[i] >= 0 ? offs[set_of[i]] : 0;
     hc[i].row_off = cands[i].nrows > 0 ? cands[i].row_off : 0;
   }
-  const int grid = ctx->num_sms * 2;
+  if (opt->blocks_per_sm < 0 || opt->blocks_per_sm > 2) return BS_ERR_ARG;
+  const int grid = ctx->num_sms * (opt->blocks_per_sm ? opt->blocks_per_sm : 2);
   const long long slots = (long long)grid * AB_WARPS;
   rc = bs_ensure_dev((void **)&Bf->cands, &Bf->cand_cap, ncand, sizeof(AbCandDev));
   if (!rc) rc = bs_ensure_dev((void **)&Bf->verdict, &Bf->v_cap, ncand, sizeof(int32_t));

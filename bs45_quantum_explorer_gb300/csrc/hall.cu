@@ -233,11 +233,11 @@ __global__ void pack_kernel(const int8_t *__restrict__ rows, long long nrows, in
 // accumulator and that of D_r in another: a thread owns a whole pair and forms the pair PSD
 // without exchanging values. The 208 table columns are split into the two angle blocks of
 // bs_tc_row (N = 128 and N = 80); block b of a tile has its own accumulators (C and D), so
-// the epilogue of block 0 overlaps the MMAs of block 1 and the other way round:
+// the epilogue's reads of block 0 overlap the MMAs of block 1 and the other way round:
 //   TMEM columns [0, 256): block 0 (C at 0, D at 128); [256, 416): block 1 (C at 256, D at 336).
 constexpr int TC_STAGES = 4;
 // warps [0, TC_PRODUCERS) producers, TC_MMA_WARP the MMA issuer (and TMEM owner), then two
-// epilogue groups of four warps: group b reads block b of every tile
+// epilogue groups of four warps, each reading half of the angles of both blocks
 constexpr int TC_PRODUCERS = 2;
 constexpr int TC_MMA_WARP = TC_PRODUCERS;
 constexpr int TC_THREADS = 32 * (TC_PRODUCERS + 1 + 8);
@@ -358,6 +358,12 @@ __device__ __forceinline__ void pair_psd2(const float *rc, const float *ic, cons
   asm("mov.b64 {%0, %1}, %2;" : "=f"(f0), "=f"(f1) : "l"(r));
 }
 
+__device__ __forceinline__ float fmax3(float a, float b, float c) {
+  float r;
+  asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+  return r;
+}
+
 // Four operand halves per 32-bit word pair: the 8 bits of `byte` (bit set = +1) as 8 halves
 // +-1.0 in the operand format. neg2 holds two -1.0 halves; z = byte * 0x8001 places bit i at
 // positions i and i + 15, so a shift brings bits 2k and 2k + 1 to the sign positions 15 and 31
@@ -420,7 +426,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) hall_tc_kernel(TcParams P) {
     }
     for (int b = 0; b < 2; b++) {
       mbar_init(tfull0 + 8 * b, 1);
-      mbar_init(tempty0 + 8 * b, 4);
+      mbar_init(tempty0 + 8 * b, 8);  // every epilogue warp releases every block
     }
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -522,81 +528,82 @@ __global__ void __launch_bounds__(TC_THREADS, 1) hall_tc_kernel(TcParams P) {
     }
     __syncwarp();
   } else {
-    // ---- epilogue: group g reads block g of every tile; warp quarter q owns pairs
-    // 32q..32q+31 of the tile, one per lane. Each lane keeps the max pair PSD over its block's
-    // angles; of the two groups, the one that finishes a tile second takes the max of both
-    // blocks (shared memory slot, a counter per quarter) and decides the 32 pairs. ----
+    // ---- epilogue: both groups read both blocks of every tile, group g the angles
+    // [32g, 32g + 32) of block 0 and [20g, 20g + 20) of block 1; warp quarter q owns pairs
+    // 32q..32q+31 of the tile, one per lane. A group copies its columns of a block to
+    // registers in one round of loads and releases the block at once (the MMA issuer waits
+    // for both groups), then forms the pair PSDs. Of the two groups, the one that finishes
+    // a tile second takes the max of both (shared memory slot, a counter per quarter) and
+    // decides the 32 pairs. ----
     const int g = (warp - TC_MMA_WARP - 1) >> 2;
     const int q = warp & 3;
     const uint32_t lane_off = (uint32_t)(q * 32) << 16;
     const int row = q * 32 + lane;
-    const uint32_t tC = tmem + lane_off + (g ? TM_BLK1 : 0u);
-    const uint32_t tD = tC + (g ? (uint32_t)N_BLK1 : (uint32_t)N_BLK0);
-    const uint32_t nb = g ? BS_TC_BLK1 : BS_TC_BLK0;  // angles of the block; Im at column + nb
+    const uint32_t tC0 = tmem + lane_off + 32u * g;                 // block 0, C accumulator
+    const uint32_t tC1 = tmem + lane_off + TM_BLK1 + 20u * g;       // block 1, C accumulator
+    const uint32_t nb0 = BS_TC_BLK0, nb1 = BS_TC_BLK1;             // Im at column + nb
     for (int it = 0;; it++) {
       const long long tile = blockIdx.x + (long long)it * G;
       if (tile >= P.ntiles) break;
-      // warp-uniform outcome: the TMEM loads below are .sync.aligned
-      const bool ready = __all_sync(FULL_MASK, mbar_wait(tfull0 + 8 * g, it & 1, abort_flag));
-      if (!ready) {
-        if (!*abort_flag) { set_status(P.status, BS_ERR_TIMEOUT); *abort_flag = 1; }
-        break;
-      }
-      tc_fence_after();
       const long long pair = tile * TC_TILE + row;
       float *dump = (P.dump && pair < P.npairs) ? P.dump + (size_t)pair * 2 * BS_TC_COLS : nullptr;
-      float mx0 = 0.0f, mx1 = 0.0f;
-      // rounds of 32 angles (block 1: 32 + 8); the block's accumulators are released to the
-      // MMA issuer right after the last round's loads
-      for (uint32_t a0 = 0; a0 < nb; a0 += 32) {
-        const bool last_round = a0 + 32 >= nb;
-        if (nb - a0 >= 32) {
-          float v[128];  // Re C, Im C, Re D, Im D at angles a0..a0+31 of the block
-          tmem_ld_32x4(tC + a0, tC + nb + a0, tD + a0, tD + nb + a0, v);
-          if (last_round) {
-            tc_fence_before();
-            __syncwarp();
-            if (lane == 0) mbar_arrive(tempty0 + 8 * g);
-          }
-#pragma unroll
-          for (int k = 0; k < 32; k += 2) {
-            float f0, f1;
-            pair_psd2(v + k, v + 32 + k, v + 64 + k, v + 96 + k, f0, f1);
-            mx0 = fmaxf(mx0, f0);
-            mx1 = fmaxf(mx1, f1);
-          }
-          if (dump)
-            for (int k = 0; k < 32; k++) {
-              const int u = (g ? BS_TC_BLK0 : 0) + (int)a0 + k;
-              dump[u] = v[k];
-              dump[BS_TC_IM0 + u] = v[32 + k];
-              dump[BS_TC_COLS + u] = v[64 + k];
-              dump[BS_TC_COLS + BS_TC_IM0 + u] = v[96 + k];
-            }
-        } else {  // the last 8 angles of block 1
-          float v[32];
-          tmem_ld_8x4(tC + a0, tC + nb + a0, tD + a0, tD + nb + a0, v);
-          tc_fence_before();
-          __syncwarp();
-          if (lane == 0) mbar_arrive(tempty0 + 8 * g);
-#pragma unroll
-          for (int k = 0; k < 8; k += 2) {
-            float f0, f1;
-            pair_psd2(v + k, v + 8 + k, v + 16 + k, v + 24 + k, f0, f1);
-            mx0 = fmaxf(mx0, f0);
-            mx1 = fmaxf(mx1, f1);
-          }
-          if (dump)
-            for (int k = 0; k < 8; k++) {
-              const int u = (g ? BS_TC_BLK0 : 0) + (int)a0 + k;
-              dump[u] = v[k];
-              dump[BS_TC_IM0 + u] = v[8 + k];
-              dump[BS_TC_COLS + u] = v[16 + k];
-              dump[BS_TC_COLS + BS_TC_IM0 + u] = v[24 + k];
-            }
+      float mx = 0.0f;
+      bool ok = true;
+      {  // block 0: 32 angles
+        // warp-uniform outcome: the TMEM loads below are .sync.aligned
+        ok = __all_sync(FULL_MASK, mbar_wait(tfull0, it & 1, abort_flag));
+        if (!ok) {
+          if (!*abort_flag) { set_status(P.status, BS_ERR_TIMEOUT); *abort_flag = 1; }
+          break;
         }
+        tc_fence_after();
+        float v[128];  // Re C, Im C, Re D, Im D at the group's 32 angles
+        tmem_ld_32x4(tC0, tC0 + nb0, tC0 + N_BLK0, tC0 + N_BLK0 + nb0, v);
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(tempty0);
+#pragma unroll
+        for (int k = 0; k < 32; k += 2) {
+          float f0, f1;
+          pair_psd2(v + k, v + 32 + k, v + 64 + k, v + 96 + k, f0, f1);
+          mx = fmax3(mx, f0, f1);
+        }
+        if (dump)
+          for (int k = 0; k < 32; k++) {
+            const int u = 32 * g + k;
+            dump[u] = v[k];
+            dump[BS_TC_IM0 + u] = v[32 + k];
+            dump[BS_TC_COLS + u] = v[64 + k];
+            dump[BS_TC_COLS + BS_TC_IM0 + u] = v[96 + k];
+          }
       }
-      const float mx = fmaxf(mx0, mx1);
+      {  // block 1: 20 angles
+        ok = __all_sync(FULL_MASK, mbar_wait(tfull0 + 8, it & 1, abort_flag));
+        if (!ok) {
+          if (!*abort_flag) { set_status(P.status, BS_ERR_TIMEOUT); *abort_flag = 1; }
+          break;
+        }
+        tc_fence_after();
+        float v[80];  // Re C, Im C, Re D, Im D at the group's 20 angles
+        tmem_ld_20x4(tC1, tC1 + nb1, tC1 + N_BLK1, tC1 + N_BLK1 + nb1, v);
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(tempty0 + 8);
+#pragma unroll
+        for (int k = 0; k < 20; k += 2) {
+          float f0, f1;
+          pair_psd2(v + k, v + 20 + k, v + 40 + k, v + 60 + k, f0, f1);
+          mx = fmax3(mx, f0, f1);
+        }
+        if (dump)
+          for (int k = 0; k < 20; k++) {
+            const int u = BS_TC_BLK0 + 20 * g + k;
+            dump[u] = v[k];
+            dump[BS_TC_IM0 + u] = v[20 + k];
+            dump[BS_TC_COLS + u] = v[40 + k];
+            dump[BS_TC_COLS + BS_TC_IM0 + u] = v[60 + k];
+          }
+      }
       // hand-over between the two groups: the second to finish this tile decides
       const int slot = it & (TC_SLOTS - 1);
       pmax[(slot * 2 + g) * TC_TILE + row] = mx;

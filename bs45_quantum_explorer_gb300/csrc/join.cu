@@ -40,32 +40,35 @@ __global__ void npaf_kernel(const uint64_t *__restrict__ q, long long count, int
   }
 }
 
-// 64-bit key of a vector v[1..n] (mixing the value and the shift, as a FNV-1a-style chain
-// followed by a splitmix64 finaliser to spread it over the table).
-__device__ __forceinline__ uint64_t vec_key(const int *v, int n) {
-  uint64_t h = 1469598103934665603ULL;
+// 64-bit key of an autocorrelation vector v[1..n] (|v[s]| <= 2n + 2 < 128): the values are
+// biased into bytes and packed eight to a word, and the words are folded with one
+// multiply-xorshift step each (a splitmix64-style finaliser spreads the result over the table).
+// Equal vectors give equal keys; the exact NPAF check after a key match rules collisions out.
+template <typename F>
+__device__ __forceinline__ uint64_t vec_key(F value, int n) {
+  uint64_t h = 0x9E3779B97F4A7C15ULL, w = 0;
+  int fill = 0;
   for (int s = 1; s <= n; s++) {
-    h ^= (uint64_t)(uint16_t)(int16_t)v[s];
-    h *= 1099511628211ULL;
-    h ^= (uint64_t)s;
-    h *= 1099511628211ULL;
+    w |= (uint64_t)(uint8_t)(value(s) + 128) << (8 * fill);
+    if (++fill == 8 || s == n) {
+      h = (h ^ w) * 0xBF58476D1CE4E5B9ULL;
+      h ^= h >> 31;
+      w = 0;
+      fill = 0;
+    }
   }
-  h ^= h >> 31;
-  h *= 0xBF58476D1CE4E5B9ULL;
   h ^= h >> 29;
+  h *= 0x94D049BB133111EBULL;
+  h ^= h >> 32;
   return h ? h : 1;  // 0 marks an empty slot
 }
 
 __device__ __forceinline__ uint64_t cd_key(uint64_t C, uint64_t D, int n) {
-  int v[65];
-  for (int s = 1; s <= n; s++) v[s] = -(nacf(C, n, s) + nacf(D, n, s));
-  return vec_key(v, n);
+  return vec_key([&](int s) { return -(nacf(C, n, s) + nacf(D, n, s)); }, n);
 }
 
 __device__ __forceinline__ uint64_t ab_key(uint64_t A, uint64_t B, int n) {
-  int v[65];
-  for (int s = 1; s <= n; s++) v[s] = nacf(A, n + 1, s) + nacf(B, n + 1, s);
-  return vec_key(v, n);
+  return vec_key([&](int s) { return nacf(A, n + 1, s) + nacf(B, n + 1, s); }, n);
 }
 
 // table: keys[slot] (0 = empty) and idx[slot] (the C,D entry index)

@@ -72,7 +72,7 @@ def run_lane(ctx, n, sig, skip=0, end=0, shard=0, nshard=1, budget=200000, buf_c
              drain_top=0, drain_batches=1, endpos=False, orbit_canon=True, orbit_q=1, qprune=True,
              prof_order=3, m6=None, thm211b=None, thm212=None, abp_cap=20000, outer_k=3,
              early=True, canon=True, rev=False, hall_mode="tc_fp16", chunk=65536,
-             max_seconds=0.0, listing=None, batch_cells=None, cd_prune=0, a2=0):
+             max_seconds=0.0, listing=None, batch_cells=None, cd_prune=0, a2=0, tuning=None):
     """Runs the lane over raw cells [skip, end) of its shard (end = 0: to the list's end).
     The list options are the lane's WZ_FH_* list settings (cells.cell_list); the cells must
     be mod-6 cells (the lane's buffered order). max_seconds > 0 stops between cells once
@@ -80,7 +80,14 @@ def run_lane(ctx, n, sig, skip=0, end=0, shard=0, nshard=1, budget=200000, buf_c
     listing: a cell_list() result to reuse. batch_cells: cells streamed per device call
     (default 32 up to n = 30, where cells are small, else 1); a batch is streamed whole and
     each cell cut to its front-only prefix on the host, which is the same prefix.
-    cd_prune: WZ_FH_CD_PRUNE for the streams (fewer DFS nodes, the same candidates)."""
+    cd_prune: WZ_FH_CD_PRUNE for the streams (fewer DFS nodes, the same candidates).
+    a2: WZ_FH_A2 (2 = the A2 row prune in the completer).
+    tuning: work sizes from tune.py (stream fine_nodes / wave_nodes / dfs_blocks, completer
+    blocks_per_sm and chunk); none of them changes a result."""
+    tuning = dict(tuning or {})
+    stream_kw = {k: tuning[k] for k in ("fine_nodes", "wave_nodes", "dfs_blocks") if k in tuning}
+    ab_kw = {k: tuning[k] for k in ("blocks_per_sm",) if k in tuning}
+    chunk = int(tuning.get("chunk", chunk))
     cells, kept, _, m = listing if listing is not None else lane_list(
         n, sig, m6, thm211b, thm212, endpos, orbit_canon, orbit_q, qprune, prof_order)
     if m != 6:
@@ -107,7 +114,7 @@ def run_lane(ctx, n, sig, skip=0, end=0, shard=0, nshard=1, budget=200000, buf_c
         t0 = time.perf_counter()
         surv, cidx, st = cd_stream(ctx, args, m=m, pins=pins, rev=rev, endpos=endpos,
                                    hall_mode=hall_mode, as_words=True, cd_prune=cd_prune,
-                                   limit=cut if len(group) == 1 else 0)
+                                   limit=cut if len(group) == 1 else 0, **stream_kw)
         res.stream_s += time.perf_counter() - t0
         if len(group) == 1:
             streamed[group[0]] = (surv, st[0])
@@ -154,7 +161,7 @@ def run_lane(ctx, n, sig, skip=0, end=0, shard=0, nshard=1, budget=200000, buf_c
                 ctx.timing(True)
                 v, nd, A, B = complete_ab(ctx, surv[idx], budget, rows=cell_rows, m=m,
                                           outer_k=outer_k, early=early, canon=canon,
-                                          first_hit=True, a2=a2)
+                                          first_hit=True, a2=a2, **ab_kw)
                 ms, _, _ = ctx.timing_read()
                 ctx.timing(False)
                 res.complete_s += time.perf_counter() - t1

@@ -26,7 +26,8 @@ def make_cells(cells, m, pins=None):
 
 def cd_stream(ctx, cells, m=6, pins=None, rev=False, endpos=False, hall_mode="tc_fp16",
               target_prefixes=0, leaf_chunk=0, survivor_cap=0, cap=None, as_words=False,
-              ab_side=False, limit=0, round_us=0, cd_prune=0, wall_sec=0.0):
+              ab_side=False, limit=0, round_us=0, cd_prune=0, wall_sec=0.0, fine_nodes=0.0,
+              wave_nodes=0.0, dfs_blocks=0):
     """cells: list of (tx, ty). Returns (survivors, cell index per survivor, per-cell stats).
 
     survivors: int8 [k, 2, L] (or uint64 words [k, 2] with as_words) in stream order, L = n
@@ -37,6 +38,7 @@ def cd_stream(ctx, cells, m=6, pins=None, rev=False, endpos=False, hall_mode="tc
     cd_prune: WZ_FH_CD_PRUNE (bit 1 root quad rule, bit 2 block reachability; C,D side, m = 6,
     even n only): the same survivors, fewer DFS nodes.
     wall_sec > 0: WZ_FH_WALL_SEC, abandon the stream after that long without a new survivor.
+    fine_nodes, wave_nodes, dfs_blocks: work sizes (0 = defaults; see tune.py).
     A stream stopped early (the context's stop flag, or the wall) returns the survivors of the
     part it completed, and every stats dict carries stopped = 1 (flag) or 2 (wall), else 0."""
     ncells = len(cells)
@@ -45,7 +47,8 @@ def cd_stream(ctx, cells, m=6, pins=None, rev=False, endpos=False, hall_mode="tc
                      hall_mode=MODES[hall_mode], ab_side=int(ab_side),
                      target_prefixes=target_prefixes, leaf_chunk=leaf_chunk,
                      survivor_cap=survivor_cap, limit=limit, round_us=round_us,
-                     wall_sec=float(wall_sec))
+                     wall_sec=float(wall_sec), fine_nodes=float(fine_nodes),
+                     wave_nodes=float(wave_nodes), dfs_blocks=int(dfs_blocks))
     stats = (CellStats * ncells)()
     nout = C.c_longlong(0)
     cap = cap if cap is not None else (min(1 << 20, limit) if limit > 0 else 1 << 20)

@@ -171,6 +171,14 @@ typedef struct {
                                 (counted from the call's start, then from the last launch that
                                 found one); the call returns BS_WALLED with the survivors of the
                                 waves it completed, which the lane still drains */
+  /* work sizes (0 = the defaults; bs45_quantum_explorer_gb300.tune picks them by measuring):
+     fine_nodes  the DFS nodes a fine subtree is refined to (default 2e4),
+     wave_nodes  the DFS nodes a wave aims at (default 8e9),
+     dfs_blocks  DFS blocks per SM: 4 (64 registers), 5 (48) or 6 (40) */
+  double fine_nodes;
+  double wave_nodes;
+  int32_t dfs_blocks;
+  int32_t reserved;
 } bs_stream_opts;
 
 typedef struct { long long nodes, leaves, ok; } bs_cell_stats;
@@ -260,6 +268,8 @@ typedef struct {
                            977-1047, 1069-1072); mode 1, the reference's shadow instrument, is
                            not built (BS_ERR_ARG) */
   double max_seconds;   /* per-candidate wall limit on the device (0 = none) */
+  int32_t blocks_per_sm; /* resident completer blocks of 8 warps per SM: 1 or 2 (0 = 2) */
+  int32_t reserved;
 } bs_ab_opts;
 
 int bs_complete_ab_batch(bs_ctx *ctx, const bs_ab_cand *cands, long long ncand,

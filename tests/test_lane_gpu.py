@@ -173,3 +173,27 @@ def test_run_lane_matches_reference_runs(gpu):
         check_run_lane(res, summary_of(c["semantic"]), (c["n"], c["sig"], c["settings"]))
     for x in ctxs.values():
         x.close()
+
+
+def test_lane_resumes_across_cpu_and_gpu_arms(gpu):
+    """An arm interrupted on CPU cores (the reference binary, oracle/_ref/wz_match) resumes on
+    the GPU from its checkpoint file, and the other way round, with the same result and the
+    same final checkpoint as the reference's own interrupted-and-resumed run."""
+    from make_lane_golden import REF_BIN, semantic
+    if not os.path.exists(REF_BIN):
+        pytest.skip("the reference binary was not built on this machine (oracle/_ref)")
+    exe = _bin()
+    cases = [c for c in _cases() if c.get("resume")]
+    assert len(cases) >= 10
+    with tempfile.TemporaryDirectory() as tmp:
+        for first, second in ((REF_BIN, exe), (exe, REF_BIN)):
+            for c in cases:
+                ck = tempfile.mkdtemp(dir=tmp)
+                rc1, out1, _, _ = _run(first, c["n"], c["sig"], c["settings"], tmp, ck)
+                st2 = {k: v for k, v in c["settings"].items() if k != "WZ_FH_TEST_STOP_AFTER"}
+                rc2, out2, dh, dl = _run(second, c["n"], c["sig"], st2, tmp, ck)
+                files = sorted(os.listdir(ck))
+                ckpt2 = open(os.path.join(ck, files[0])).read() if files else ""
+                ctx = (os.path.basename(first), c["n"], c["sig"], c["settings"])
+                assert (rc1, semantic(out1)) == (c["rc"], c["semantic"]), ctx
+                assert (rc2, semantic(out2), ckpt2) == (c["rc2"], c["semantic2"], c["ckpt2"]), ctx
