@@ -797,6 +797,22 @@ def main():
             line["fp64_gpu_form"] = {"value": fp_rate, "unit": UNIT,
                                      "tc_speedup": value / world / fp_rate,
                                      "masks_identical": bool(torch.equal(d_pass64, d_pass))}
+            # the other tensor-core form (split-BF16 hi + lo, or fp16) of the same filter
+            other = "tc_bf16x2" if args.mode == "tc_fp16" else "tc_fp16"
+            d_pass2 = torch.empty_like(d_pass)
+            ctx.hall_filter_dev(d_words.data_ptr(), npairs, d_pass2.data_ptr(), other, stats=False)
+            torch.cuda.synchronize()
+            a.record(stream)
+            for _ in range(10):
+                ctx.hall_filter_dev(d_words.data_ptr(), npairs, d_pass2.data_ptr(), other, stats=False)
+            b.record(stream)
+            torch.cuda.synchronize()
+            o_rate = npairs * 10 / (a.elapsed_time(b) * 1e-3)
+            st2 = ctx.hall_filter_dev(d_words.data_ptr(), npairs, d_pass2.data_ptr(), other, stats=True)
+            line[f"{other}_form"] = {"value": o_rate, "unit": UNIT, "speedup_vs_fp64_gpu_form": o_rate / fp_rate,
+                                     "masks_identical": bool(torch.equal(d_pass2, d_pass)),
+                                     "rechecked_pairs_per_step": st2["rechecked"],
+                                     "certified_band": [st2["pass_below"], st2["reject_above"]]}
         # ---- the tensor-core PSD error against FP64 on 4,096 pairs (tables as the reference
         # builds them: cos/sin(i * (j pi / 100))); the false-reject count against the oracle is
         # taken in the CPU-baseline leg below ----
@@ -844,6 +860,10 @@ def main():
         surv64, _, sst64 = cd_stream(ctx, [cell42], m=6, as_words=True, limit=CMP_LIMIT,
                                      hall_mode="fp64")
         dt64 = time.perf_counter() - t1
+        t1 = time.perf_counter()
+        survb, _, sstb = cd_stream(ctx, [cell42], m=6, as_words=True, limit=CMP_LIMIT,
+                                   hall_mode="tc_bf16x2")
+        dtb = time.perf_counter() - t1
         line["search"] = {
             "workload": "C,D stream of the n=42 cell px=(-1,-1,1,1,1,-1) py=(-1,-3,1,1,3,-1) "
                         "(ORDER=3 raw cell 3056 of sig (7,11,0,0)), its first 50,000 survivors "
@@ -858,8 +878,12 @@ def main():
                             "filtered_cands_per_s": sst_c[0]["leaves"] / dt_c},
                 "fp64": {"seconds": dt64, "nodes_per_s": sst64[0]["nodes"] / dt64,
                          "filtered_cands_per_s": sst64[0]["leaves"] / dt64},
+                "tc_bf16x2": {"seconds": dtb, "nodes_per_s": sstb[0]["nodes"] / dtb,
+                              "filtered_cands_per_s": sstb[0]["leaves"] / dtb,
+                              "speedup_vs_fp64": dt64 / dtb},
                 "tc_speedup": dt64 / dt_c,
-                "survivors_identical": bool(np.array_equal(surv64, surv_c)),
+                "survivors_identical": bool(np.array_equal(surv64, surv_c)) and
+                bool(np.array_equal(survb, surv_c)),
                 "same_as_50000_prefix": bool(np.array_equal(surv_c, surv[:CMP_LIMIT]))},
         }
         if not args.no_cpu_baseline:

@@ -13,16 +13,33 @@
 #define BS_TC_NANG 101      // unique Hall angles (j = 1..100 and 200)
 
 // One tensor-core table image: 208 rows (columns of the DFT) x 64 halves, stored in the
-// 128-byte-swizzled K-major layout the UMMA shared-memory descriptor reads. The 104 angle
-// slots (101 unique angles, 3 zero rows) form two blocks, each a contiguous run of rows
-// [cos of its angles][sin of its angles] that one MMA of N = 2 x (angles in the block) reads:
-// block 0 = angles 0..63 (rows 0..127), block 1 = angles 64..103 (rows 128..207).
+// 128-byte-swizzled K-major layout the UMMA shared-memory descriptor reads. The 101 unique
+// angles u sit in 104 slots (3 zero rows); slot order is any permutation, since the test takes
+// a maximum over angles. Slots 0..31 hold the screening angles (32 angles spread evenly over
+// the grid, u = round(k * 100 / 31)), so that rows [0, 64) -- their cos rows, then their sin
+// rows -- are the B operand of the screening MMA (N = 64). The full table is two blocks, each
+// a contiguous run of rows one MMA of N = 2 x (slots in the block) reads:
+//   block 0 = slots 0..63: rows [cos 0..31][sin 0..31][cos 32..63][sin 32..63] (rows 0..127)
+//   block 1 = slots 64..103: rows [cos 64..103][sin 64..103] (rows 128..207)
 #define BS_TC_PART_BYTES (BS_TC_COLS * 128)
 #define BS_TC_BLK0 64
 #define BS_TC_BLK1 40
+#define BS_TC_SCREEN 32
+static inline __host__ __device__ int bs_tc_screen_u(int k) { return (k * 100 + 15) / 31; }
+// slot of angle u: the screening angles first (in order), then the others in increasing u
+static inline __host__ __device__ int bs_tc_slot_of(int u) {
+  int k = (u * 31 + 50) / 100;  // the screening index u would have
+  if (k < BS_TC_SCREEN && bs_tc_screen_u(k) == u) return k;
+  int below = 0;  // screening angles below u
+  for (int j = 0; j < BS_TC_SCREEN; j++) below += bs_tc_screen_u(j) < u;
+  return BS_TC_SCREEN + u - below;
+}
+static inline __host__ __device__ int bs_tc_row_of_slot(int slot, int sin_part) {
+  if (slot < BS_TC_BLK0) return 64 * (slot / 32) + (sin_part ? 32 : 0) + slot % 32;
+  return 2 * BS_TC_BLK0 + (sin_part ? BS_TC_BLK1 : 0) + (slot - BS_TC_BLK0);
+}
 static inline __host__ __device__ int bs_tc_row(int u, int sin_part) {
-  return u < BS_TC_BLK0 ? (sin_part ? BS_TC_BLK0 + u : u)
-                        : 2 * BS_TC_BLK0 + (sin_part ? BS_TC_BLK1 : 0) + (u - BS_TC_BLK0);
+  return bs_tc_row_of_slot(bs_tc_slot_of(u), sin_part);
 }
 
 struct bs_hall_tc_form {
@@ -55,13 +72,14 @@ struct bs_ctx {
   bs_hall_fix_form fix[2];   // fixed-point band test, lengths n (0) and n+1 (1)
   int *d_status;             // device-side error word
   unsigned long long *d_count;  // [0] band count, [1] pass count, [2] overflow flag,
-                                // [3] pairs left for the FP64 test
+                                // [3] pairs left for the FP64 test, [4] screen survivors
   // scratch for the host-buffer entry points
   uint64_t *d_bits; long long bits_cap;   // pairs
   uint8_t *d_pass; long long pass_cap;
   int8_t *d_rows; long long rows_cap;     // int8 staging for packing
   unsigned *d_unc; long long unc_cap;     // band pair indices
   unsigned *d_unc2; long long unc2_cap;   // pairs the fixed-point test leaves undecided
+  unsigned *d_scr; long long scr_cap;     // pairs the tensor-core screen did not reject
   void *h_pinned; size_t pinned_bytes;
   // kernel timing (bs_ctx_timing): start/stop events around the timed kernel class
   int timing;

@@ -312,7 +312,7 @@ extern "C" void bs_ctx_destroy(bs_ctx *ctx) {
   cudaFree(ctx->fix[0].d_tab); cudaFree(ctx->fix[1].d_tab);
   cudaFree(ctx->d_status); cudaFree(ctx->d_count);
   cudaFree(ctx->d_bits); cudaFree(ctx->d_pass); cudaFree(ctx->d_rows); cudaFree(ctx->d_unc);
-  cudaFree(ctx->d_unc2);
+  cudaFree(ctx->d_unc2); cudaFree(ctx->d_scr);
   bs_stream_free(ctx);
   bs_ab_free(ctx);
   if (ctx->h_pinned) cudaFreeHost(ctx->h_pinned);

@@ -243,6 +243,29 @@ __device__ __forceinline__ uint64_t all_rows(int w, int nrows) {
 }
 
 __global__ void __launch_bounds__(32 * AB_WARPS) ab_kernel(AbParams P) {
+  // the quad loop's canon filter as tables (entry 16 is the root level d = 0): bit k of
+  // s_elig[t] says quad k passes canon_ok with incoming ties t, s_ntie[t][k] its outgoing ties
+  __shared__ uint8_t s_elig[17];
+  __shared__ uint8_t s_ntie[17][8];
+  if (threadIdx.x < 17) {
+    const int t = threadIdx.x, dd = t == 16 ? 0 : 1;
+    uint32_t elig = 0;
+    for (int k = 0; k < 8; k++) {
+      const uint32_t q = quad_bits(dd, k);
+      uint32_t o = 0;
+      if (canon_ok(P, dd, t == 16 ? 5u : (uint32_t)t, (q & 8) ? 1 : -1, (q & 4) ? 1 : -1,
+                   (q & 2) ? 1 : -1, (q & 1) ? 1 : -1, o))
+        elig |= 1u << k;
+      s_ntie[t][k] = (uint8_t)o;
+    }
+    s_elig[t] = (uint8_t)elig;
+  }
+  __syncthreads();
+  // first eligible quad >= k at level d (next_quad): the outer mask applies from d = 1
+  auto next_q = [&](int dd, int k, unsigned om, uint32_t ties) -> int {
+    const uint32_t e = (dd == 0 ? s_elig[16] : (s_elig[ties] & om)) & (0xFFu << k) & 0xFFu;
+    return e ? __ffs(e) - 1 : 8;
+  };
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const long long slot = (long long)blockIdx.x * AB_WARPS + wib;
   __shared__ uint32_t s_ctrl[AB_WARPS][AB_MAXLV];  // k | omask << 4 | ties << 12
@@ -355,37 +378,33 @@ __global__ void __launch_bounds__(32 * AB_WARPS) ab_kernel(AbParams P) {
           int k = c0 & 15;
           unplace(u, v, L - 1 - d, L, m);
           unplace(u, v, d, L, m);
-          __syncwarp();
-          if (lane == 0) ctrl[d] = (c0 & ~15u) | (uint32_t)(k + 1);
-          __syncwarp();
+          __syncwarp();  // every lane has read the old value; all write the same
+          ctrl[d] = (c0 & ~15u) | (uint32_t)(k + 1);
         }
         continue;
       }
       const uint32_t c0 = ctrl[d];
       const unsigned omask = (c0 >> 4) & 0xFF;
       const uint32_t ties = (c0 >> 12) & 15;
-      int k = next_quad(P, d, c0 & 15, omask, ties);
+      int k = next_q(d, c0 & 15, omask, ties);
       if (k == 8) {
         if (d == 0) break;  // clean exhaustion
         d--;
         uint32_t cp = ctrl[d];
         unplace(u, v, L - 1 - d, L, m);
         unplace(u, v, d, L, m);
-        __syncwarp();
-        if (lane == 0) ctrl[d] = (cp & ~15u) | (uint32_t)((cp & 15) + 1);
-        __syncwarp();
+        __syncwarp();  // every lane has read the old value; all write the same
+        ctrl[d] = (cp & ~15u) | (uint32_t)((cp & 15) + 1);
         continue;
       }
       const uint32_t q = quad_bits(d, k);
       const int a1 = (q & 8) ? 1 : -1, b1 = (q & 4) ? 1 : -1, a2 = (q & 2) ? 1 : -1, b2 = (q & 1) ? 1 : -1;
-      uint32_t nties;
-      canon_ok(P, d, ties, a1, b1, a2, b2, nties);
+      const uint32_t nties = s_ntie[d == 0 ? 16 : ties][k];
       // charge the node before placing (wz_match.cpp:1243-1248)
       nodes++;
       if (P.budget > 0 && ++cur > P.budget) {
-        __syncwarp();
-        if (lane == 0) ctrl[d] = (c0 & ~15u) | (uint32_t)k;
-        __syncwarp();
+        __syncwarp();  // every lane has read the old value; all write the same
+        ctrl[d] = (c0 & ~15u) | (uint32_t)k;
         aborted = true;
         break;
       }
@@ -393,9 +412,8 @@ __global__ void __launch_bounds__(32 * AB_WARPS) ab_kernel(AbParams P) {
       if (P.early && d > 0) {
         int lhs = sgnbit(u.A, 0) * a2 + sgnbit(u.B, 0) * b2 + sgnbit(u.A, L - 1) * a1 + sgnbit(u.B, L - 1) * b1;
         if (lhs != res[d]) {
-          __syncwarp();
-          if (lane == 0) ctrl[d] = (c0 & ~15u) | (uint32_t)(k + 1);
-          __syncwarp();
+          __syncwarp();  // every lane has read the old value; all write the same
+          ctrl[d] = (c0 & ~15u) | (uint32_t)(k + 1);
           continue;
         }
       }
@@ -444,25 +462,20 @@ __global__ void __launch_bounds__(32 * AB_WARPS) ab_kernel(AbParams P) {
         }
         const int nlo = __reduce_min_sync(FULL_MASK, mylo), nhi = __reduce_max_sync(FULL_MASK, myhi);
         __syncwarp();
-        if (lane == 0) {
-          wlo[d + 1] = nlo;
-          whi[d + 1] = nhi + 1;
-        }
-        __syncwarp();
+        wlo[d + 1] = nlo;  // the warp's uniform state: every lane writes the same value
+        whi[d + 1] = nhi + 1;
         prune = nhi < 0;
       }
       if (prune) {
         unplace(u, v, L - 1 - d, L, m);
         unplace(u, v, d, L, m);
-        __syncwarp();
-        if (lane == 0) ctrl[d] = (c0 & ~15u) | (uint32_t)(k + 1);
-        __syncwarp();
+        __syncwarp();  // every lane has read the old value; all write the same
+        ctrl[d] = (c0 & ~15u) | (uint32_t)(k + 1);
         continue;
       }
       // descend: the child level's entry work (its outer mask may end it immediately)
-      __syncwarp();
-      if (lane == 0) ctrl[d] = (c0 & ~15u) | (uint32_t)k;
-      __syncwarp();
+      __syncwarp();  // every lane has read the old value; all write the same
+      ctrl[d] = (c0 & ~15u) | (uint32_t)k;
       const int nd = d + 1;
       unsigned om = 0xFFu;
       int r_e = 0;
@@ -473,17 +486,13 @@ __global__ void __launch_bounds__(32 * AB_WARPS) ab_kernel(AbParams P) {
       if (om == 0u) {  // fh_ab_search(d+1) returns false at once: undo and try the next quad
         unplace(u, v, L - 1 - d, L, m);
         unplace(u, v, d, L, m);
-        __syncwarp();
-        if (lane == 0) ctrl[d] = (c0 & ~15u) | (uint32_t)(k + 1);
-        __syncwarp();
+        __syncwarp();  // every lane has read the old value; all write the same
+        ctrl[d] = (c0 & ~15u) | (uint32_t)(k + 1);
         continue;
       }
-      __syncwarp();
-      if (lane == 0) {
-        ctrl[nd] = 0u | (om << 4) | (nties << 12);
-        res[nd] = r_e;
-      }
-      __syncwarp();
+      __syncwarp();  // every lane has read the old value; all write the same
+      ctrl[nd] = 0u | (om << 4) | (nties << 12);
+      res[nd] = r_e;
       d = nd;
     }
     if (aborted) {
@@ -491,7 +500,7 @@ __global__ void __launch_bounds__(32 * AB_WARPS) ab_kernel(AbParams P) {
       // it returns (wz_match.cpp:1243-1247 reached again with fh_cur already over budget).
       for (int j = d - 1; j >= 0; j--) {
         uint32_t cj = ctrl[j];
-        if (next_quad(P, j, (cj & 15) + 1, (cj >> 4) & 0xFF, (cj >> 12) & 15) < 8) nodes++;
+        if (next_q(j, (cj & 15) + 1, (cj >> 4) & 0xFF, (cj >> 12) & 15) < 8) nodes++;
       }
     }
     if (lane == 0) {

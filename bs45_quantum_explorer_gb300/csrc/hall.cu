@@ -255,7 +255,16 @@ struct TcParams {
   const uint8_t *image;
   int nparts, ksteps;
   uint32_t idesc[2];  // instruction descriptors of the two angle blocks (N = 128, N = 80)
+  uint32_t idesc_screen;  // the screening MMA (N = 64)
   int bits_a16;       // bits is 16-byte aligned: a pair's two words are read as one vector
+  // the full test over a list of pairs (the screen's survivors): pair = list[t] for
+  // t < min(*list_len, list_cap); NULL: pairs 0..npairs-1
+  const unsigned *list;
+  const unsigned long long *list_len;
+  unsigned long long list_cap;
+  // the screen's output: pairs it could not reject, appended to scr (count in count[4])
+  unsigned *scr;
+  unsigned long long scr_cap;
   uint32_t one2;  // two packed +1.0 halves in the operand format
   float pass_below, reject_above;
   uint8_t *pass;
@@ -397,6 +406,13 @@ __device__ __forceinline__ void put_row(uint8_t *A, int r, uint64_t w, int nchun
   }
 }
 
+// the angle u of a table slot (-1: a padding slot); for the diagnostic dump only
+__device__ __forceinline__ int u_of_slot(int slot) {
+  for (int u = 0; u < BS_TC_NANG; u++)
+    if (bs_tc_slot_of(u) == slot) return u;
+  return -1;
+}
+
 __global__ void __launch_bounds__(TC_THREADS, 1) hall_tc_kernel(TcParams P) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t *base = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -437,6 +453,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1) hall_tc_kernel(TcParams P) {
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
+  // the pairs of this launch: P.npairs, or the length of the list (written by the screen)
+  long long count = P.npairs, ntiles = P.ntiles;
+  if (P.list) {
+    const unsigned long long len = *P.list_len;
+    count = (long long)(len < P.list_cap ? len : P.list_cap);
+    ntiles = (count + TC_TILE - 1) / TC_TILE;
+  }
 
   if (warp < TC_PRODUCERS) {
     // ---- producers: packed words -> +-1 operand rows. Producer p fills the CTA's tiles
@@ -445,24 +468,21 @@ __global__ void __launch_bounds__(TC_THREADS, 1) hall_tc_kernel(TcParams P) {
     // tile is expanded so the global-load latency overlaps the work. ----
     const uint32_t neg2 = P.one2 | 0x80008000u;
     const int nchunks = 2 * P.ksteps;
+    auto fetch = [&](long long t) -> uint4 {
+      if (t >= count) return make_uint4(0, 0, 0, 0);
+      const long long pair = P.list ? (long long)__ldg(P.list + t) : t;
+      return load_pair(P.bits, pair, P.bits_a16);
+    };
     int it = warp;
     long long tile = blockIdx.x + (long long)it * G;
     uint4 wv[4];
 #pragma unroll
-    for (int rr = 0; rr < 4; rr++) {
-      const long long pair = tile * TC_TILE + lane + 32 * rr;
-      wv[rr] = (tile < P.ntiles && pair < P.npairs) ? load_pair(P.bits, pair, P.bits_a16)
-                                                    : make_uint4(0, 0, 0, 0);
-    }
-    while (tile < P.ntiles) {
+    for (int rr = 0; rr < 4; rr++) wv[rr] = tile < ntiles ? fetch(tile * TC_TILE + lane + 32 * rr) : make_uint4(0, 0, 0, 0);
+    while (tile < ntiles) {
       const long long next = tile + TC_PRODUCERS * G;
       uint4 nw[4];
 #pragma unroll
-      for (int rr = 0; rr < 4; rr++) {
-        const long long pair = next * TC_TILE + lane + 32 * rr;
-        nw[rr] = (next < P.ntiles && pair < P.npairs) ? load_pair(P.bits, pair, P.bits_a16)
-                                                      : make_uint4(0, 0, 0, 0);
-      }
+      for (int rr = 0; rr < 4; rr++) nw[rr] = next < ntiles ? fetch(next * TC_TILE + lane + 32 * rr) : make_uint4(0, 0, 0, 0);
       const int s = it % TC_STAGES;
       const uint32_t par = ((it / TC_STAGES) & 1) ^ 1;
       if (!mbar_wait(empty0 + 8 * s, par, abort_flag)) {
@@ -490,7 +510,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) hall_tc_kernel(TcParams P) {
     if (lane == 0) {
       const uint32_t a_base = smem_u32(sA), b_base = smem_u32(sB);
       int it = 0, last = -1;
-      for (long long tile = blockIdx.x; tile < P.ntiles; tile += G, it++) {
+      for (long long tile = blockIdx.x; tile < ntiles; tile += G, it++) {
         const int s = it % TC_STAGES;
         if (!mbar_wait(full0 + 8 * s, (it / TC_STAGES) & 1, abort_flag)) {
           if (!*abort_flag) { set_status(P.status, BS_ERR_TIMEOUT); *abort_flag = 1; }
@@ -539,14 +559,16 @@ __global__ void __launch_bounds__(TC_THREADS, 1) hall_tc_kernel(TcParams P) {
     const int q = warp & 3;
     const uint32_t lane_off = (uint32_t)(q * 32) << 16;
     const int row = q * 32 + lane;
-    const uint32_t tC0 = tmem + lane_off + 32u * g;                 // block 0, C accumulator
+    // block 0 columns: [Re slots 0..31][Im 0..31][Re 32..63][Im 32..63]; block 1: [Re][Im]
+    const uint32_t tC0 = tmem + lane_off + 64u * g;                 // block 0, C accumulator
     const uint32_t tC1 = tmem + lane_off + TM_BLK1 + 20u * g;       // block 1, C accumulator
-    const uint32_t nb0 = BS_TC_BLK0, nb1 = BS_TC_BLK1;             // Im at column + nb
+    const uint32_t nb0 = 32, nb1 = BS_TC_BLK1;                     // Im at column + nb
     for (int it = 0;; it++) {
       const long long tile = blockIdx.x + (long long)it * G;
-      if (tile >= P.ntiles) break;
-      const long long pair = tile * TC_TILE + row;
-      float *dump = (P.dump && pair < P.npairs) ? P.dump + (size_t)pair * 2 * BS_TC_COLS : nullptr;
+      if (tile >= ntiles) break;
+      const long long t = tile * TC_TILE + row;
+      const long long pair = t < count ? (P.list ? (long long)__ldg(P.list + t) : t) : -1;
+      float *dump = (P.dump && pair >= 0) ? P.dump + (size_t)pair * 2 * BS_TC_COLS : nullptr;
       float mx = 0.0f;
       bool ok = true;
       {  // block 0: 32 angles
@@ -569,8 +591,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1) hall_tc_kernel(TcParams P) {
           mx = fmax3(mx, f0, f1);
         }
         if (dump)
+#pragma unroll
           for (int k = 0; k < 32; k++) {
-            const int u = 32 * g + k;
+            const int u = u_of_slot(32 * g + k);
             dump[u] = v[k];
             dump[BS_TC_IM0 + u] = v[32 + k];
             dump[BS_TC_COLS + u] = v[64 + k];
@@ -596,8 +619,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1) hall_tc_kernel(TcParams P) {
           mx = fmax3(mx, f0, f1);
         }
         if (dump)
+#pragma unroll
           for (int k = 0; k < 20; k++) {
-            const int u = BS_TC_BLK0 + 20 * g + k;
+            const int u = u_of_slot(BS_TC_BLK0 + 20 * g + k);
+            if (u < 0) continue;  // a padding slot
             dump[u] = v[k];
             dump[BS_TC_IM0 + u] = v[20 + k];
             dump[BS_TC_COLS + u] = v[40 + k];
@@ -615,7 +640,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) hall_tc_kernel(TcParams P) {
       if (order == 1) {
         __threadfence_block();
         const float m = fmaxf(mx, pmax[(slot * 2 + (g ^ 1)) * TC_TILE + row]);
-        const bool mine = pair < P.npairs;
+        const bool mine = pair >= 0;
         const bool sure_pass = mine && m <= P.pass_below;
         const bool unsure = mine && m > P.pass_below && m < P.reject_above;
         if (mine) P.pass[pair] = sure_pass ? 1 : 0;
@@ -639,6 +664,181 @@ __global__ void __launch_bounds__(TC_THREADS, 1) hall_tc_kernel(TcParams P) {
   if (warp == TC_MMA_WARP) tc_dealloc(tmem, TMEM_COLS);
 }
 
+// ---- the screening pass: the 32 screening angles (table slots 0..31) of every pair ----
+// The same producers and operands as the full test, but one MMA of N = 64 per sequence and
+// part, into one of four TMEM buffers of 128 columns (C: Re 0..31, Im 32..63; D: 64..127),
+// so the MMA runs up to three tiles ahead of the epilogue. A thread reads its pair's 128
+// accumulator values, releases the buffer and takes the max pair PSD over the 32 angles: at
+// or above the certified reject_above the pair is rejected for good (the max over all angles
+// can only be larger); otherwise its index goes to the survivor list, which the full test
+// then decides. The full test reads four accumulator values per angle and pair out of TMEM,
+// and that read, not the MMA, bounds it; on the microbench mix and on stream leaves about
+// 2-3 % of pairs survive the screen, so the full reads are paid for those alone.
+constexpr int SC_BUFS = 4;
+constexpr uint32_t SC_COLS = 128;  // TMEM columns per buffer (C then D, 64 each)
+
+__global__ void __launch_bounds__(TC_THREADS, 1) hall_screen_kernel(TcParams P) {
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t *base = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  uint8_t *sA = base;
+  uint8_t *sB = sA + TC_STAGES * A_STAGE_BYTES;  // rows 0..63 of each part, 8 KB per part
+  uint64_t *bars = (uint64_t *)(sB + P.nparts * 64 * 128);
+  uint32_t *tmem_slot = (uint32_t *)(bars + 2 * TC_STAGES + 2 * SC_BUFS);
+  volatile int *abort_flag = (volatile int *)(tmem_slot + 1);
+  const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + TC_STAGES);
+  const uint32_t tfull0 = smem_u32(bars + 2 * TC_STAGES), tempty0 = tfull0 + 8 * SC_BUFS;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const long long G = gridDim.x;
+
+  {  // rows 0..63 (the screening angles' cos and sin rows) of each part -> shared memory
+    for (int p = 0; p < P.nparts; p++) {
+      const uint4 *src = (const uint4 *)(P.image + (size_t)p * BS_TC_PART_BYTES);
+      uint4 *dst = (uint4 *)(sB + p * 64 * 128);
+      for (int i = threadIdx.x; i < 64 * 128 / 16; i += TC_THREADS) dst[i] = src[i];
+    }
+  }
+  if (threadIdx.x == 0) {
+    for (int st = 0; st < TC_STAGES; st++) {
+      mbar_init(full0 + 8 * st, 1);
+      mbar_init(empty0 + 8 * st, 1);
+    }
+    for (int b = 0; b < SC_BUFS; b++) {
+      mbar_init(tfull0 + 8 * b, 1);
+      mbar_init(tempty0 + 8 * b, 4);  // the four warps of the group that reads the buffer
+    }
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == TC_MMA_WARP) tc_alloc(smem_u32(tmem_slot), TMEM_COLS);
+  fence_async_smem();
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp < TC_PRODUCERS) {
+    const uint32_t neg2 = P.one2 | 0x80008000u;
+    const int nchunks = 2 * P.ksteps;
+    auto fetch = [&](long long pair) -> uint4 {
+      return pair < P.npairs ? load_pair(P.bits, pair, P.bits_a16) : make_uint4(0, 0, 0, 0);
+    };
+    int it = warp;
+    long long tile = blockIdx.x + (long long)it * G;
+    uint4 wv[4];
+#pragma unroll
+    for (int rr = 0; rr < 4; rr++) wv[rr] = tile < P.ntiles ? fetch(tile * TC_TILE + lane + 32 * rr) : make_uint4(0, 0, 0, 0);
+    while (tile < P.ntiles) {
+      const long long next = tile + TC_PRODUCERS * G;
+      uint4 nw[4];
+#pragma unroll
+      for (int rr = 0; rr < 4; rr++) nw[rr] = next < P.ntiles ? fetch(next * TC_TILE + lane + 32 * rr) : make_uint4(0, 0, 0, 0);
+      const int st = it % TC_STAGES;
+      if (!mbar_wait(empty0 + 8 * st, ((it / TC_STAGES) & 1) ^ 1, abort_flag)) {
+        if (!*abort_flag) { set_status(P.status, BS_ERR_TIMEOUT); *abort_flag = 1; }
+        break;
+      }
+      uint8_t *AC = sA + st * A_STAGE_BYTES, *AD = AC + A_SEQ_BYTES;
+#pragma unroll
+      for (int rr = 0; rr < 4; rr++) {
+        const int r = lane + 32 * rr;
+        put_row(AC, r, ((uint64_t)wv[rr].y << 32) | wv[rr].x, nchunks, neg2);
+        put_row(AD, r, ((uint64_t)wv[rr].w << 32) | wv[rr].z, nchunks, neg2);
+      }
+      fence_async_smem();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(full0 + 8 * st);
+#pragma unroll
+      for (int rr = 0; rr < 4; rr++) wv[rr] = nw[rr];
+      tile = next;
+      it += TC_PRODUCERS;
+    }
+  } else if (warp == TC_MMA_WARP) {
+    if (lane == 0) {
+      const uint32_t a_base = smem_u32(sA), b_base = smem_u32(sB);
+      int it = 0, last = -1;
+      for (long long tile = blockIdx.x; tile < P.ntiles; tile += G, it++) {
+        const int st = it % TC_STAGES, b = it % SC_BUFS;
+        if (!mbar_wait(full0 + 8 * st, (it / TC_STAGES) & 1, abort_flag) ||
+            !mbar_wait(tempty0 + 8 * b, ((it / SC_BUFS) & 1) ^ 1, abort_flag)) {
+          if (!*abort_flag) { set_status(P.status, BS_ERR_TIMEOUT); *abort_flag = 1; }
+          break;
+        }
+        tc_fence_after();
+        for (int seq = 0; seq < 2; seq++) {
+          uint32_t acc = 0;
+          for (int p = 0; p < P.nparts; p++)
+            for (int k = 0; k < P.ksteps; k++) {
+              const uint64_t ad = sw128_desc(a_base + st * A_STAGE_BYTES + seq * A_SEQ_BYTES + k * 32);
+              const uint64_t bd = sw128_desc(b_base + p * 64 * 128 + k * 32);
+              tc_mma(tmem + b * SC_COLS + seq * 64, ad, bd, P.idesc_screen, acc);
+              acc = 1;
+            }
+        }
+        tc_commit(empty0 + 8 * st);
+        tc_commit(tfull0 + 8 * b);
+        last = it;
+      }
+      if (last >= 0) mbar_wait(tfull0 + 8 * (last % SC_BUFS), (last / SC_BUFS) & 1, abort_flag, false);
+    }
+    __syncwarp();
+  } else {
+    // ---- epilogue: group g reads the tiles it = g, g + 2, ... (buffer it % 4) ----
+    const int g = (warp - TC_MMA_WARP - 1) >> 2;
+    const int q = warp & 3;
+    const uint32_t lane_off = (uint32_t)(q * 32) << 16;
+    const int row = q * 32 + lane;
+    for (int it = g;; it += 2) {
+      const long long tile = blockIdx.x + (long long)it * G;
+      if (tile >= P.ntiles) break;
+      const int b = it % SC_BUFS;
+      const bool ready = __all_sync(FULL_MASK, mbar_wait(tfull0 + 8 * b, (it / SC_BUFS) & 1, abort_flag));
+      if (!ready) {
+        if (!*abort_flag) { set_status(P.status, BS_ERR_TIMEOUT); *abort_flag = 1; }
+        break;
+      }
+      tc_fence_after();
+      const uint32_t t0 = tmem + lane_off + b * SC_COLS;
+      float v[128];  // Re C, Im C, Re D, Im D at the 32 screening angles
+      tmem_ld_32x4(t0, t0 + 32, t0 + 64, t0 + 96, v);
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(tempty0 + 8 * b);
+      float mx = 0.0f;
+#pragma unroll
+      for (int k = 0; k < 32; k += 2) {
+        float f0, f1;
+        pair_psd2(v + k, v + 32 + k, v + 64 + k, v + 96 + k, f0, f1);
+        mx = fmax3(mx, f0, f1);
+      }
+      const long long pair = tile * TC_TILE + row;
+      const bool mine = pair < P.npairs;
+      const bool keep = mine && mx < P.reject_above;
+      if (mine && !keep) P.pass[pair] = 0;
+      const unsigned ball = __ballot_sync(FULL_MASK, keep);
+      if (ball) {  // one atomic per warp for its survivors, in lane order
+        unsigned long long base = 0;
+        if (lane == 0) base = atomicAdd(P.count + 4, (unsigned long long)__popc(ball));
+        base = __shfl_sync(FULL_MASK, base, 0);
+        if (keep) {
+          const unsigned long long k = base + __popc(ball & ((1u << lane) - 1u));
+          if (k < P.scr_cap) P.scr[k] = (unsigned)pair;
+          else atomicExch(P.count + 2, 1ULL);
+        }
+      }
+    }
+  }
+
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (warp == TC_MMA_WARP) tc_dealloc(tmem, TMEM_COLS);
+}
+
+size_t screen_smem_bytes(int nparts) {
+  return 1024 + (size_t)TC_STAGES * A_STAGE_BYTES + (size_t)nparts * 64 * 128 +
+         (2 * TC_STAGES + 2 * SC_BUFS) * 8 + 16;
+}
+
 size_t tc_smem_bytes(int nparts) {
   return 1024 + (size_t)TC_STAGES * A_STAGE_BYTES + (size_t)nparts * BS_TC_PART_BYTES +
          sizeof(float) * TC_SLOTS * 2 * TC_TILE + sizeof(int) * TC_SLOTS * 4 +
@@ -652,6 +852,10 @@ void tc_idesc(int fmt, uint32_t idesc[2]) {
                         ((uint32_t)(128 >> 4) << 24);
   idesc[0] = base | ((uint32_t)(N_BLK0 >> 3) << 17);
   idesc[1] = base | ((uint32_t)(N_BLK1 >> 3) << 17);
+}
+uint32_t tc_idesc_screen(int fmt) {
+  return (1u << 4) | ((uint32_t)fmt << 7) | ((uint32_t)fmt << 10) | ((uint32_t)(128 >> 4) << 24) |
+         ((uint32_t)(64 >> 3) << 17);
 }
 
 }  // namespace
@@ -683,6 +887,8 @@ static int hall_kernel_attrs(int dev) {
                           fp64_smem));
   CK(cudaFuncSetAttribute(hall_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                           (int)tc_smem_bytes(2)));
+  CK(cudaFuncSetAttribute(hall_screen_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                          (int)screen_smem_bytes(2)));
   CK(cudaFuncSetAttribute(hall_fix_band_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                           (int)(sizeof(int64_t) * BS_FIX_WORDS)));
   done[dev].store(true, std::memory_order_release);
@@ -711,10 +917,14 @@ static int launch_fp64(bs_ctx *ctx, const uint64_t *d_bits, long long npairs,
   return BS_OK;
 }
 
+// The tensor-core test of a batch: the screen over every pair (rejects most of them and lists
+// the rest in d_scr), then the full test over that list. With a dump (diagnostics) the full
+// test runs over every pair and the screen is skipped. Both kernels are one timed section.
 static int launch_tc(bs_ctx *ctx, int mode, const uint64_t *d_bits, long long npairs,
                      uint8_t *d_pass, float *d_dump, int L) {
   const bs_hall_tc_form &F = (L == ctx->n) ? ctx->tc[mode] : ctx->tc_ab[mode];
   TcParams P;
+  memset(&P, 0, sizeof P);
   P.bits = d_bits;
   P.npairs = npairs;
   P.ntiles = (npairs + TC_TILE - 1) / TC_TILE;
@@ -723,6 +933,7 @@ static int launch_tc(bs_ctx *ctx, int mode, const uint64_t *d_bits, long long np
   P.nparts = F.nparts;
   P.ksteps = (L + 15) / 16;
   tc_idesc(F.fmt, P.idesc);
+  P.idesc_screen = tc_idesc_screen(F.fmt);
   P.one2 = F.fmt ? 0x3F803F80u : 0x3C003C00u;
   P.pass_below = F.pass_below;
   P.reject_above = F.reject_above;
@@ -732,11 +943,22 @@ static int launch_tc(bs_ctx *ctx, int mode, const uint64_t *d_bits, long long np
   P.count = ctx->d_count;
   P.status = ctx->d_status;
   P.dump = d_dump;
-  size_t smem = tc_smem_bytes(F.nparts);
-  long long grid = P.ntiles < ctx->num_sms ? P.ntiles : ctx->num_sms;
-  if (grid < 1) grid = 1;
+  const long long grid = P.ntiles < ctx->num_sms ? (P.ntiles < 1 ? 1 : P.ntiles) : ctx->num_sms;
   bs_timed_begin(ctx);
-  hall_tc_kernel<<<(int)grid, TC_THREADS, smem, ctx->stream>>>(P);
+  if (!d_dump) {
+    P.scr = ctx->d_scr;
+    P.scr_cap = (unsigned long long)ctx->scr_cap;
+    hall_screen_kernel<<<(int)grid, TC_THREADS, screen_smem_bytes(F.nparts), ctx->stream>>>(P);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) { bs_timed_end(ctx); return bs_cuda_fail(e); }
+    ctx->launches++;
+    // the full test over the survivors (their count is read on the device)
+    P.list = ctx->d_scr;
+    P.list_len = ctx->d_count + 4;
+    P.list_cap = (unsigned long long)ctx->scr_cap;
+    P.scr = nullptr;
+  }
+  hall_tc_kernel<<<(int)grid, TC_THREADS, tc_smem_bytes(F.nparts), ctx->stream>>>(P);
   bs_timed_end(ctx);
   CK(cudaGetLastError());
   return BS_OK;
@@ -772,6 +994,7 @@ static int hall_dev(bs_ctx *ctx, const uint64_t *d_bits, long long npairs, int m
     } else {
       int rc = bs_ensure_dev((void **)&ctx->d_unc, &ctx->unc_cap, npairs, sizeof(unsigned));
       if (!rc) rc = bs_ensure_dev((void **)&ctx->d_unc2, &ctx->unc2_cap, npairs, sizeof(unsigned));
+      if (!rc) rc = bs_ensure_dev((void **)&ctx->d_scr, &ctx->scr_cap, npairs, sizeof(unsigned));
       if (rc) return rc;
       rc = launch_tc(ctx, mode, d_bits, npairs, d_pass, d_dump, L);
       if (rc) return rc;
@@ -896,7 +1119,8 @@ constexpr size_t NA_COS_OFF = 256;                   // FP64 cos [200][BS_MAXL]
 constexpr size_t NA_SIN_OFF = NA_COS_OFF + sizeof(double) * 200 * BS_MAXL;
 constexpr size_t NA_IMG_OFF = NA_SIN_OFF + sizeof(double) * 200 * BS_MAXL;  // fp16 table image
 constexpr size_t NA_UNC_OFF = NA_IMG_OFF + BS_TC_PART_BYTES;                // uint32 band list
-constexpr size_t NA_BYTES = NA_UNC_OFF + sizeof(unsigned) * NOALLOC_MAX_PAIRS;
+constexpr size_t NA_SCR_OFF = NA_UNC_OFF + sizeof(unsigned) * NOALLOC_MAX_PAIRS;  // screen list
+constexpr size_t NA_BYTES = NA_SCR_OFF + sizeof(unsigned) * NOALLOC_MAX_PAIRS;
 
 struct NoallocDevice {
   unsigned char *scratch;  // device address of g_hall_noalloc_scratch on this device
@@ -999,6 +1223,7 @@ extern "C" int bs_hall_filter_noalloc(int n, const uint64_t *d_bits, long long n
   CK(cudaMemsetAsync(S.scratch, 0, 128, s));  // counters and status start at zero
   if (npairs > 0) {
     TcParams P;
+    memset(&P, 0, sizeof P);
     P.bits = d_bits;
     P.npairs = npairs;
     P.ntiles = (npairs + TC_TILE - 1) / TC_TILE;
@@ -1007,6 +1232,7 @@ extern "C" int bs_hall_filter_noalloc(int n, const uint64_t *d_bits, long long n
     P.nparts = 1;
     P.ksteps = (n + 15) / 16;
     tc_idesc(0, P.idesc);
+    P.idesc_screen = tc_idesc_screen(0);
     P.one2 = 0x3C003C00u;
     P.pass_below = S.pass_below;
     P.reject_above = S.reject_above;
@@ -1019,6 +1245,15 @@ extern "C" int bs_hall_filter_noalloc(int n, const uint64_t *d_bits, long long n
     int dev_sms = 0;
     CK(cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, dev));
     const long long grid = P.ntiles < dev_sms ? P.ntiles : dev_sms;
+    // the screen, then the full test over its survivors (as bs_hall_filter_dev does)
+    P.scr = (unsigned *)(S.scratch + NA_SCR_OFF);
+    P.scr_cap = (unsigned long long)NOALLOC_MAX_PAIRS;
+    hall_screen_kernel<<<(int)grid, TC_THREADS, screen_smem_bytes(1), s>>>(P);
+    CK(cudaGetLastError());
+    P.list = P.scr;
+    P.list_len = count + 4;
+    P.list_cap = (unsigned long long)NOALLOC_MAX_PAIRS;
+    P.scr = nullptr;
     hall_tc_kernel<<<(int)grid, TC_THREADS, tc_smem_bytes(1), s>>>(P);
     CK(cudaGetLastError());
     hall_fp64_recheck_kernel<<<dev_sms, 256, sizeof(double) * 2 * 200 * n, s>>>(
