@@ -108,8 +108,9 @@ int bs_hall_filter_dev(bs_ctx *ctx, const uint64_t *d_bits, long long npairs, in
  * device-memory budget owned by a scheduler or host framework, or latency-sensitive code in
  * the middle of overlapped multi-stream work, where cudaMalloc / cudaFree would synchronise
  * the device. No counterpart in the reference. It needs no context and allocates nothing:
- * its scratch (band list, counters, status word, tables) is one fixed static device array of
- * about 4.2 MiB, which every GPU that loads the library keeps until the process exits.
+ * its scratch (screen and band lists, counters, status word, tables) is one fixed static
+ * device array of about 8.2 MiB, which every GPU that loads the library keeps until the process
+ * exits.
  * n is the sequence length (4 <= n <= 63); d_bits holds 2 words per pair and d_pass
  * receives the decisions, both device memory owned by the caller; at most 1,048,576 pairs
  * per call (BS_ERR_CAP beyond); npairs = 0 only checks the set-up. The work is enqueued on
