@@ -268,12 +268,15 @@ __global__ void __launch_bounds__(32 * AB_WARPS) ab_kernel(AbParams P) {
   };
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const long long slot = (long long)blockIdx.x * AB_WARPS + wib;
-  __shared__ uint32_t s_ctrl[AB_WARPS][AB_MAXLV];  // k | omask << 4 | ties << 12
-  __shared__ int s_res[AB_WARPS][AB_MAXLV];        // early-check residual of the level
   __shared__ int s_lo[AB_WARPS][AB_MAXLV];         // the level's row bitset: nonzero words
   __shared__ int s_hi[AB_WARPS][AB_MAXLV];         // lie in [lo, hi)
-  uint32_t *ctrl = s_ctrl[wib];
-  int *res = s_res[wib], *wlo = s_lo[wib], *whi = s_hi[wib];
+  int *wlo = s_lo[wib], *whi = s_hi[wib];
+  // Per-level control state, one level per lane (levels 0..half-1 <= 31): lane j holds
+  // level j's k | omask << 4 | ties << 12 and its early-check residual. A level's state is
+  // read with one shuffle from its lane and written by that lane alone (the values are
+  // warp-uniform), so no shared memory or warp barrier is involved.
+  uint32_t my_ctrl = 0;
+  int my_res = 0;
   uint64_t *lv = P.bits + (size_t)slot * (P.half + 1) * P.Wcap;
   const int L = P.L, n = P.n, half = P.half, m = P.m;
 
@@ -322,8 +325,10 @@ __global__ void __launch_bounds__(32 * AB_WARPS) ab_kernel(AbParams P) {
     const long long t_start = clock64();
     int d = 0;
     if (lane == 0) {
-      ctrl[0] = 0u | (0xFFu << 4) | (5u << 12);  // ties: a_tied = b_tied = 1
-      res[0] = 0;
+      my_ctrl = 0u | (0xFFu << 4) | (5u << 12);  // ties: a_tied = b_tied = 1
+      my_res = 0;
+    }
+    if (lane == 0) {
       wlo[0] = 0;
       whi[0] = cd.W;
     }
@@ -374,27 +379,25 @@ __global__ void __launch_bounds__(32 * AB_WARPS) ab_kernel(AbParams P) {
         // back to the parent level
         d--;
         {
-          uint32_t c0 = ctrl[d];
+          uint32_t c0 = __shfl_sync(FULL_MASK, my_ctrl, d);
           int k = c0 & 15;
           unplace(u, v, L - 1 - d, L, m);
           unplace(u, v, d, L, m);
-          __syncwarp();  // every lane has read the old value; all write the same
-          ctrl[d] = (c0 & ~15u) | (uint32_t)(k + 1);
+          if (lane == d) my_ctrl = (c0 & ~15u) | (uint32_t)(k + 1);
         }
         continue;
       }
-      const uint32_t c0 = ctrl[d];
+      const uint32_t c0 = __shfl_sync(FULL_MASK, my_ctrl, d);
       const unsigned omask = (c0 >> 4) & 0xFF;
       const uint32_t ties = (c0 >> 12) & 15;
       int k = next_q(d, c0 & 15, omask, ties);
       if (k == 8) {
         if (d == 0) break;  // clean exhaustion
         d--;
-        uint32_t cp = ctrl[d];
+        uint32_t cp = __shfl_sync(FULL_MASK, my_ctrl, d);
         unplace(u, v, L - 1 - d, L, m);
         unplace(u, v, d, L, m);
-        __syncwarp();  // every lane has read the old value; all write the same
-        ctrl[d] = (cp & ~15u) | (uint32_t)((cp & 15) + 1);
+        if (lane == d) my_ctrl = (cp & ~15u) | (uint32_t)((cp & 15) + 1);
         continue;
       }
       const uint32_t q = quad_bits(d, k);
@@ -403,17 +406,15 @@ __global__ void __launch_bounds__(32 * AB_WARPS) ab_kernel(AbParams P) {
       // charge the node before placing (wz_match.cpp:1243-1248)
       nodes++;
       if (P.budget > 0 && ++cur > P.budget) {
-        __syncwarp();  // every lane has read the old value; all write the same
-        ctrl[d] = (c0 & ~15u) | (uint32_t)k;
+        if (lane == d) my_ctrl = (c0 & ~15u) | (uint32_t)k;
         aborted = true;
         break;
       }
       // early outer-correlation check (wz_match.cpp:1256-1259)
       if (P.early && d > 0) {
         int lhs = sgnbit(u.A, 0) * a2 + sgnbit(u.B, 0) * b2 + sgnbit(u.A, L - 1) * a1 + sgnbit(u.B, L - 1) * b1;
-        if (lhs != res[d]) {
-          __syncwarp();  // every lane has read the old value; all write the same
-          ctrl[d] = (c0 & ~15u) | (uint32_t)(k + 1);
+        if (lhs != __shfl_sync(FULL_MASK, my_res, d)) {
+          if (lane == d) my_ctrl = (c0 & ~15u) | (uint32_t)(k + 1);
           continue;
         }
       }
@@ -469,13 +470,11 @@ __global__ void __launch_bounds__(32 * AB_WARPS) ab_kernel(AbParams P) {
       if (prune) {
         unplace(u, v, L - 1 - d, L, m);
         unplace(u, v, d, L, m);
-        __syncwarp();  // every lane has read the old value; all write the same
-        ctrl[d] = (c0 & ~15u) | (uint32_t)(k + 1);
+        if (lane == d) my_ctrl = (c0 & ~15u) | (uint32_t)(k + 1);
         continue;
       }
       // descend: the child level's entry work (its outer mask may end it immediately)
-      __syncwarp();  // every lane has read the old value; all write the same
-      ctrl[d] = (c0 & ~15u) | (uint32_t)k;
+      if (lane == d) my_ctrl = (c0 & ~15u) | (uint32_t)k;
       const int nd = d + 1;
       unsigned om = 0xFFu;
       int r_e = 0;
@@ -486,20 +485,20 @@ __global__ void __launch_bounds__(32 * AB_WARPS) ab_kernel(AbParams P) {
       if (om == 0u) {  // fh_ab_search(d+1) returns false at once: undo and try the next quad
         unplace(u, v, L - 1 - d, L, m);
         unplace(u, v, d, L, m);
-        __syncwarp();  // every lane has read the old value; all write the same
-        ctrl[d] = (c0 & ~15u) | (uint32_t)(k + 1);
+        if (lane == d) my_ctrl = (c0 & ~15u) | (uint32_t)(k + 1);
         continue;
       }
-      __syncwarp();  // every lane has read the old value; all write the same
-      ctrl[nd] = 0u | (om << 4) | (nties << 12);
-      res[nd] = r_e;
+      if (lane == nd) {
+        my_ctrl = 0u | (om << 4) | (nties << 12);
+        my_res = r_e;
+      }
       d = nd;
     }
     if (aborted) {
       // Every ancestor level whose loop has another eligible quad charges one more node before
       // it returns (wz_match.cpp:1243-1247 reached again with fh_cur already over budget).
       for (int j = d - 1; j >= 0; j--) {
-        uint32_t cj = ctrl[j];
+        uint32_t cj = __shfl_sync(FULL_MASK, my_ctrl, j);
         if (next_q(j, (cj & 15) + 1, (cj >> 4) & 0xFF, (cj >> 12) & 15) < 8) nodes++;
       }
     }

@@ -63,11 +63,27 @@ __device__ __forceinline__ uint64_t vec_key(F value, int n) {
   return h ? h : 1;  // 0 marks an empty slot
 }
 
+// the same autocorrelation on 32-bit words, for sequences of length <= 32 (every length the
+// full-space join runs at): half the integer instructions of the 64-bit form
+__device__ __forceinline__ int nacf32(uint32_t x, int L, int s) {
+  if (s >= L) return 0;
+  const uint32_t mask = (L - s >= 32) ? ~0u : ((1u << (L - s)) - 1u);
+  return (L - s) - 2 * __popc((x ^ (x >> s)) & mask);
+}
+
 __device__ __forceinline__ uint64_t cd_key(uint64_t C, uint64_t D, int n) {
+  if (n <= 32) {
+    const uint32_t c = (uint32_t)C, d = (uint32_t)D;
+    return vec_key([&](int s) { return -(nacf32(c, n, s) + nacf32(d, n, s)); }, n);
+  }
   return vec_key([&](int s) { return -(nacf(C, n, s) + nacf(D, n, s)); }, n);
 }
 
 __device__ __forceinline__ uint64_t ab_key(uint64_t A, uint64_t B, int n) {
+  if (n + 1 <= 32) {
+    const uint32_t a = (uint32_t)A, b = (uint32_t)B;
+    return vec_key([&](int s) { return nacf32(a, n + 1, s) + nacf32(b, n + 1, s); }, n);
+  }
   return vec_key([&](int s) { return nacf(A, n + 1, s) + nacf(B, n + 1, s); }, n);
 }
 
@@ -114,8 +130,14 @@ __global__ void join_probe_kernel(const uint64_t *__restrict__ ab, long long cou
         const long long j = idx[slot];
         const uint64_t C = cd[2 * j], D = cd[2 * j + 1];
         bool ok = true;
-        for (int s = 1; s <= n && ok; s++)
-          ok = (nacf(A, n + 1, s) + nacf(B, n + 1, s) + nacf(C, n, s) + nacf(D, n, s)) == 0;
+        if (n + 1 <= 32) {
+          const uint32_t a = (uint32_t)A, b = (uint32_t)B, c = (uint32_t)C, dd = (uint32_t)D;
+          for (int s = 1; s <= n && ok; s++)
+            ok = (nacf32(a, n + 1, s) + nacf32(b, n + 1, s) + nacf32(c, n, s) + nacf32(dd, n, s)) == 0;
+        } else {
+          for (int s = 1; s <= n && ok; s++)
+            ok = (nacf(A, n + 1, s) + nacf(B, n + 1, s) + nacf(C, n, s) + nacf(D, n, s)) == 0;
+        }
         if (ok) {
           unsigned long long o = atomicAdd(nout, 1ULL);
           if (o < cap) {
