@@ -296,7 +296,7 @@ def _classes(n):
     return out
 
 
-def run_first_hit(seconds, cpu_seconds=10.0, with_cpu=True, drain_top=50000):
+def run_first_hit(seconds, cpu_seconds=10.0, with_cpu=True, drain_top=50000, tune=True):
     """One production lane (orbit canon + quad switch + Q-prune, ORDER=3; budget 2^22,
     BUF_CAP 500,000, DRAIN_TOP 50,000) over raw cells [s, s+4096) of n = 36, sig (5,11,0,0),
     s drawn from the seed; stopped between cells after `seconds`. Reports the completer's
@@ -317,6 +317,12 @@ def run_first_hit(seconds, cpu_seconds=10.0, with_cpu=True, drain_top=50000):
     s = int(rng.integers(0, len(kept) - 4096))
     ctx = Context(FH_N, FH_SIG)
     kw = dict(budget=1 << 22, buf_cap=500000, drain_top=drain_top, listing=listing)
+    tune_report = None
+    if tune:  # work sizes picked by timing probes of this window's first kept cell
+        from bs45_quantum_explorer_gb300.tune import tune_lane
+        kw["tuning"], tune_report = tune_lane(ctx, FH_N, FH_SIG, listing, s, s + 4096, 1 << 22,
+                                              buf_cap=500000, drain_top=drain_top, probe=20000,
+                                              sample=2048)
     run_lane(ctx, FH_N, FH_SIG, skip=s, end=s + 1, **kw)  # warm-up: buffers, first cell
     torch.cuda.synchronize()
     res = run_lane(ctx, FH_N, FH_SIG, skip=s, end=s + 4096, max_seconds=seconds, **kw)
@@ -334,6 +340,11 @@ def run_first_hit(seconds, cpu_seconds=10.0, with_cpu=True, drain_top=50000):
            "dfs_nodes": res.dfs_nodes, "stream_s": res.stream_s,
            "dfs_nodes_per_s": res.dfs_nodes / res.stream_s if res.stream_s > 0 else None,
            "wall_s": res.timings.get("wall_s"), "found": res.found}
+    if tune_report is not None:
+        out["autotune"] = {"choice": tune_report.get("choice"), "seconds": tune_report.get("seconds"),
+                           "probe_cell": tune_report.get("cell"),
+                           "stream_probes": tune_report.get("stream_probes"),
+                           "completer_probes": tune_report.get("completer_probes")}
     if res.found:
         out["hit"] = {"idx": res.hit_idx, "profile_rank": res.profile_rank,
                       "quad": [list(map(int, x)) for x in res.quad]}
@@ -569,7 +580,7 @@ def run_join(n=24):
             "probe_algorithmic_gb_per_s": alg / (probe_ms * 1e-3) / 1e9 if probe_ms > 0 else None}
 
 
-def run_serving(n_jobs=12, tail=2, rate=2.0, slots=4, max_cells=4096):
+def run_serving(n_jobs=12, tail=2, rate=2.0, slots=4, max_cells=4096, ref_seconds=0.0):
     """C5: a seeded Poisson stream of first-hit jobs, n uniform in 20..42 with a signature from
     classes(n) and a contiguous ORDER=3 range of 1..max_cells raw cells (4,096: the workload's
     stated range), plus `tail` n = 42 ranges; per-job budget 2^16, BUF_CAP 2000, DRAIN_TOP 64
@@ -596,7 +607,65 @@ def run_serving(n_jobs=12, tail=2, rate=2.0, slots=4, max_cells=4096):
                           "DRAIN_TOP 64", "lists_prebuilt_s": round(list_s, 2),
               "errors": sum(1 for j in out if j.error), "found": sum(1 for j in out if j.result and j.result.found),
               "peak_hbm_admitted_bytes": srv.peak_in_use})
+    if ref_seconds > 0:
+        d["cpu_baseline"] = serving_reference(jobs, ref_seconds, out)
     return d
+
+
+def serving_reference(jobs, seconds, ours):
+    """The same jobs through the reference's own lane binary (oracle/_ref/wz_match, the
+    reference's wz_match.cpp compiled unmodified), one process per job as its SLURM lanes run
+    them, all at once on the host cores, each stopped by SIGTERM after `seconds` (the
+    reference then prints its summary with lower-bound counts). Reports the jobs that
+    finished, their latency from their start, the cells done per second over the bound, and
+    for every finished job whether its summary counts equal ours."""
+    import re
+    import signal
+    import subprocess
+    exe = os.path.join(ROOT, "oracle", "_ref", "wz_match")
+    if not os.path.exists(exe):
+        return {"unavailable": "oracle/_ref/wz_match was not built on this machine"}
+    base = {k: v for k, v in os.environ.items() if not k.startswith(("WZ_", "FH_"))}
+    procs = []
+    t0 = time.perf_counter()
+    for j in jobs:
+        env = dict(base, WZ_FIRSTHIT="1", WZ_FH_M6="1", WZ_THM211B="1", WZ_THM212="1",
+                   WZ_FH_ORBIT_CANON="1", WZ_FH_ORBIT_Q="1", WZ_FH_ORBIT_QPRUNE="1",
+                   WZ_FH_PROF_ORDER="3", WZ_FH_ORD3_NODIGEST_OK="1", WZ_FH_AB_BUDGET=str(j.budget),
+                   WZ_FH_BUF_CAP=str(j.buf_cap), WZ_FH_DRAIN_TOP=str(j.drain_top),
+                   WZ_FH_PROF_SKIP=str(j.skip), WZ_FH_PROF_END=str(j.end), WZ_FH_PROG_SEC="99999")
+        procs.append(subprocess.Popen([exe, str(j.n), *map(str, j.sig)], env=env, text=True,
+                                      stdout=subprocess.PIPE, stderr=subprocess.DEVNULL))
+    finish = [None] * len(procs)
+    while time.perf_counter() - t0 < seconds and any(f is None for f in finish):
+        for i, p in enumerate(procs):
+            if finish[i] is None and p.poll() is not None:
+                finish[i] = time.perf_counter() - t0
+        time.sleep(0.05)
+    for i, p in enumerate(procs):
+        if finish[i] is None:
+            p.send_signal(signal.SIGTERM)
+    wall = time.perf_counter() - t0
+    cells, same, done = 0, 0, 0
+    for i, p in enumerate(procs):
+        out, _ = p.communicate(timeout=600)
+        m = re.search(r"cells_done=(\d+)", out)
+        cells += int(m[1]) if m else 0
+        if finish[i] is not None:
+            done += 1
+            r = ours[i].result
+            keys = dict(re.findall(r"(candidates_streamed|total_AB_nodes|cells_done|budget_aborted)=(\d+)", out))
+            if r is not None and keys and (int(keys.get("candidates_streamed", -1)) == r.candidates_streamed and
+                                           int(keys.get("total_AB_nodes", -1)) == r.total_ab_nodes and
+                                           int(keys.get("cells_done", -1)) == r.cells_done):
+                same += 1
+    lat = sorted(f for f in finish if f is not None)
+    return {"value": cells / wall, "unit": "cells/s", "cores": os.cpu_count() or 1, "kind": "reference",
+            "sample": f"the same {len(jobs)} jobs as reference lane processes (wz_match.cpp compiled "
+                      f"unmodified), all started at once, stopped after {seconds:.0f} s",
+            "jobs_finished": done, "cells_done": cells, "seconds": round(wall, 1),
+            "finished_p50_s": float(np.percentile(lat, 50)) if lat else None,
+            "finished_jobs_equal_to_ours": same}
 
 
 def main():
@@ -620,6 +689,8 @@ def main():
                     help="run only the full-space join for BS(N+1, N), one signature")
     ap.add_argument("--c3", type=int, default=None, metavar="CELLS",
                     help="run only the n=30 full stream over the first CELLS kept cells (0: all)")
+    ap.add_argument("--no-tune", action="store_true",
+                    help="first-hit lane with the default work sizes instead of the autotuner's")
     ap.add_argument("--spike", action="store_true",
                     help="run only the reference's GPU completer spike beside ours and print its line")
     ap.add_argument("--fh-drain", type=int, default=50000,
@@ -644,9 +715,9 @@ def main():
         build_library()
         if args.first_hit is not None:
             print(json.dumps(run_first_hit(args.first_hit, with_cpu=not args.no_cpu_baseline,
-                                           drain_top=args.fh_drain)), flush=True)
+                                           drain_top=args.fh_drain, tune=not args.no_tune)), flush=True)
         if args.serve:
-            print(json.dumps(run_serving()), flush=True)
+            print(json.dumps(run_serving(ref_seconds=0.0 if args.no_cpu_baseline else 60.0)), flush=True)
         if args.c3 is not None:
             print(json.dumps(run_c3(args.c3)), flush=True)
         if args.join is not None:
@@ -890,7 +961,8 @@ def main():
             line["search"]["cpu_baseline"] = cpu_search_rate(os.cpu_count() or 1, cell42)
         # ---- the n = 36 first-hit lane (bounded) and the serving mix ----
         line["first_hit"] = run_first_hit(args.fh_seconds, with_cpu=not args.no_cpu_baseline)
-        line["serving"] = run_serving()
+        line["serving"] = run_serving(ref_seconds=0.0 if args.no_cpu_baseline else 45.0)
+        line["completer_vs_reference_gpu_spike"] = run_spike()
         if not args.no_cpu_baseline:
             ncpu = os.cpu_count() or 1
             words = d_words.cpu().numpy().view(np.uint64).reshape(-1, 2)
