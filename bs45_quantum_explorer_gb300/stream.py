@@ -40,7 +40,7 @@ def cd_stream(ctx, cells, m=6, pins=None, rev=False, endpos=False, hall_mode="tc
     wall_sec > 0: WZ_FH_WALL_SEC, abandon the stream after that long without a new survivor.
     fine_nodes, wave_nodes, dfs_blocks: work sizes (0 = defaults; see tune.py).
     A stream stopped early (the context's stop flag, or the wall) returns the survivors of the
-    part it completed, and every stats dict carries stopped = 1 (flag) or 2 (wall), else 0."""
+    part it completed, and every stats dict then carries stopped = 1 (flag) or 2 (wall)."""
     ncells = len(cells)
     arr = make_cells(cells, m, pins)
     opt = StreamOpts(m=m, rev=int(rev), endpos=int(endpos), cd_prune=int(cd_prune),
@@ -65,7 +65,10 @@ def cd_stream(ctx, cells, m=6, pins=None, rev=False, endpos=False, hall_mode="tc
             check(rc, "bs_cd_stream")
         break
     k = nout.value
-    st = [dict(nodes=s.nodes, leaves=s.leaves, ok=s.ok, stopped=rc if rc > 0 else 0) for s in stats]
+    st = [dict(nodes=s.nodes, leaves=s.leaves, ok=s.ok) for s in stats]
+    if rc > 0:  # stopped early: the counts cover the part explored
+        for x in st:
+            x["stopped"] = rc
     words = words[:k]
     out = words if as_words else unpack(words, ctx.n + (1 if ab_side else 0))
     return out, cidx[:k], st

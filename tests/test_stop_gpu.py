@@ -41,12 +41,12 @@ def test_stream_stops_within_a_round(gpu):
     dt = time.perf_counter() - t0
     timer.join()
     ctx.clear_stop()
-    assert st[0]["stopped"] == 1
+    assert st[0].get("stopped", 0) == 1
     assert dt < 0.5 + 0.5, dt  # the flag is seen after the launch in flight (<= 25 ms)
     # the survivors returned are the stream's first ones, in order
     assert 0 < len(part) < 2000000
     ref, _, st2 = cd_stream(ctx, [CELL42], m=6, as_words=True, limit=len(part))
-    assert st2[0]["stopped"] == 0
+    assert st2[0].get("stopped", 0) == 0
     assert np.array_equal(part, ref)
     ctx.close()
 
@@ -57,14 +57,14 @@ def test_stream_wall_limit(gpu):
     ctx = Context(42, (7, 11, 0, 0))
     # a wall far below one launch: the stream is abandoned at its first check
     part, _, st = cd_stream(ctx, [CELL42], m=6, as_words=True, limit=200000, wall_sec=1e-4)
-    assert st[0]["stopped"] == 2
+    assert st[0].get("stopped", 0) == 2
     if len(part):
         ref, _, _ = cd_stream(ctx, [CELL42], m=6, as_words=True, limit=len(part))
         assert np.array_equal(part, ref)
     # a wall that survivors keep resetting: the stream completes as without one
     full, _, st = cd_stream(ctx, [CELL42], m=6, as_words=True, limit=20000, wall_sec=30.0)
     ref, _, _ = cd_stream(ctx, [CELL42], m=6, as_words=True, limit=20000)
-    assert st[0]["stopped"] == 0 and np.array_equal(full, ref)
+    assert st[0].get("stopped", 0) == 0 and np.array_equal(full, ref)
     ctx.close()
 
 
