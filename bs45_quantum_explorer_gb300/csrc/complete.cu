@@ -68,32 +68,49 @@ __constant__ uint8_t kQPos[8] = {0, 3, 5, 6, 9, 10, 12, 15};
 __constant__ uint8_t kQNeg[8] = {1, 2, 4, 7, 8, 11, 13, 14};
 __constant__ int8_t kPosOf[16] = {0, -1, -1, 1, -1, 2, 3, -1, -1, 4, 5, -1, 6, -1, -1, 7};
 
-__device__ __forceinline__ int sgnbit(uint64_t w, int p) { return ((w >> p) & 1ULL) ? 1 : -1; }
-__device__ __forceinline__ int fld(uint64_t w, int c) { return (int)((w >> (8 * c)) & 255) - 64; }
 __device__ __forceinline__ int absi(int x) { return x < 0 ? -x : x; }
 
 struct Lanes {
   int t0, t1;    // target at s0 = lane+1, s1 = lane+33
-  int D0, D1;    // Dab
-  int K0, K1;    // Kab
+  int D0, D1;    // Dab of the placed set, as of the last corr()
+  int K0, K1;    // Kab: twice the pairs at the shift with a position still free
   int s0, s1;    // shifts (0 when out of range)
+  int kb0, kb1;  // 2 (L - s): Kab with nothing placed
 };
 
-// Place (sign +1) or remove (sign -1) position p with values (av, bv) against the placed set
-// Pm (which excludes p); A,B hold the placed signs as bits.
-__device__ __forceinline__ void lane_update(Lanes &v, int p, int av, int bv, uint64_t A, uint64_t B,
-                                            uint64_t Pm, int L, int sign) {
-  if (v.s0) {
-    int q = p - v.s0;
-    if (q >= 0 && ((Pm >> q) & 1ULL)) { v.D0 += sign * (sgnbit(A, q) * av + sgnbit(B, q) * bv); v.K0 -= 2 * sign; }
-    q = p + v.s0;
-    if (q < L && ((Pm >> q) & 1ULL)) { v.D0 += sign * (sgnbit(A, q) * av + sgnbit(B, q) * bv); v.K0 -= 2 * sign; }
+// The placed positions as bits: bit p of Pm is set when position p is placed, of A (B) when
+// A[p] (B[p]) is +1. Positions go in mirror pairs (d, L-1-d), so Pm holds the first and last
+// d positions (and the middle one at an odd length's leaf). Everything the search reads
+// (Dab, Kab, the class sums, sum A, sum B) is a popcount of these words, so removing a
+// position only clears its bits. The reference keeps Dab, Kab and the class sums
+// incrementally (fh_place / fh_unplace, wz_match.cpp:1127-1161); the values are the same.
+struct Uni {
+  uint64_t A, B, Pm;
+};
+
+// sum of the +-1 values placed at the positions of sel (A or B as X): 2 #(+1) - #placed
+__device__ __forceinline__ int ssum(uint64_t X, uint64_t Pm, uint64_t sel) {
+  return 2 * __popcll(X & sel) - __popcll(Pm & sel);
+}
+
+// Dab and Kab at the lane's shifts. The pairs (q, q+s) with both positions placed are the set
+// bits of Pm & Pm >> s; each adds a_q a_{q+s} + b_q b_{q+s} = 2 - 2 [a_q != a_{q+s}] -
+// 2 [b_q != b_{q+s}] to Dab[s] and takes 2 from Kab[s]. The search reads them only right
+// after a placement. two: whether shifts 33.. exist (n >= 33), uniform.
+__device__ __forceinline__ void corr(Lanes &v, const Uni &u, bool two) {
+  {
+    const uint64_t vv = u.Pm & (u.Pm >> v.s0);
+    const int np = __popcll(vv);
+    const int dis = __popcll((u.A ^ (u.A >> v.s0)) & vv) + __popcll((u.B ^ (u.B >> v.s0)) & vv);
+    v.D0 = 2 * (np - dis);
+    v.K0 = v.kb0 - 2 * np;
   }
-  if (v.s1) {
-    int q = p - v.s1;
-    if (q >= 0 && ((Pm >> q) & 1ULL)) { v.D1 += sign * (sgnbit(A, q) * av + sgnbit(B, q) * bv); v.K1 -= 2 * sign; }
-    q = p + v.s1;
-    if (q < L && ((Pm >> q) & 1ULL)) { v.D1 += sign * (sgnbit(A, q) * av + sgnbit(B, q) * bv); v.K1 -= 2 * sign; }
+  if (two) {
+    const uint64_t vv = u.Pm & (u.Pm >> v.s1);
+    const int np = __popcll(vv);
+    const int dis = __popcll((u.A ^ (u.A >> v.s1)) & vv) + __popcll((u.B ^ (u.B >> v.s1)) & vv);
+    v.D1 = 2 * (np - dis);
+    v.K1 = v.kb1 - 2 * np;
   }
 }
 
@@ -103,38 +120,18 @@ __device__ __forceinline__ int resid_at(const Lanes &v, int s) {
   return __shfl_sync(FULL_MASK, mine, (s - 1) & 31);
 }
 
-struct Uni {
-  uint64_t A, B, Pm;
-  uint64_t pa, pb, plc;  // class partial sums / placed counts, 8-bit fields (bias 64)
-  int sumA, sumB;
-};
-
-__device__ __forceinline__ void place(Uni &u, Lanes &v, int p, int av, int bv, int L, int m) {
-  lane_update(v, p, av, bv, u.A, u.B, u.Pm, L, +1);
-  u.Pm |= 1ULL << p;
-  if (av > 0) u.A |= 1ULL << p;
-  if (bv > 0) u.B |= 1ULL << p;
-  const int c = p % m;
-  u.pa += (uint64_t)(int64_t)av << (8 * c);
-  u.pb += (uint64_t)(int64_t)bv << (8 * c);
-  u.plc += 1ULL << (8 * c);
-  u.sumA += av;
-  u.sumB += bv;
+// place the quad (a1, b1) at the position of bit b1m and (a2, b2) at that of b2m
+__device__ __forceinline__ void place2(Uni &u, uint64_t b1m, uint64_t b2m, int a1, int b1, int a2, int b2) {
+  u.Pm |= b1m | b2m;
+  u.A |= (a1 > 0 ? b1m : 0ULL) | (a2 > 0 ? b2m : 0ULL);
+  u.B |= (b1 > 0 ? b1m : 0ULL) | (b2 > 0 ? b2m : 0ULL);
 }
-
-__device__ __forceinline__ void unplace(Uni &u, Lanes &v, int p, int L, int m) {
-  const int av = sgnbit(u.A, p), bv = sgnbit(u.B, p);
-  u.Pm &= ~(1ULL << p);
-  u.A &= ~(1ULL << p);
-  u.B &= ~(1ULL << p);
-  const int c = p % m;
-  u.pa -= (uint64_t)(int64_t)av << (8 * c);
-  u.pb -= (uint64_t)(int64_t)bv << (8 * c);
-  u.plc -= 1ULL << (8 * c);
-  u.sumA -= av;
-  u.sumB -= bv;
-  lane_update(v, p, av, bv, u.A, u.B, u.Pm, L, -1);
+__device__ __forceinline__ void clear_bits(Uni &u, uint64_t bits) {
+  u.Pm &= ~bits;
+  u.A &= ~bits;
+  u.B &= ~bits;
 }
+__device__ __forceinline__ uint64_t pair_bits(int d, int L) { return (1ULL << d) | (1ULL << (L - 1 - d)); }
 
 // Reversal-canon filter of wz_match.cpp:1222-1239 for quad (a1,b1,a2,b2) at level d with the
 // level's incoming ties. Returns false to skip; writes the outgoing ties.
@@ -162,37 +159,35 @@ __device__ __forceinline__ bool canon_ok(const AbParams &P, int d, uint32_t ties
 
 __device__ __forceinline__ uint32_t quad_bits(int d, int k) { return d == 0 ? kQNeg[k] : kQPos[k]; }
 
-// outer_mask, wz_match.cpp:601-618
-__device__ __forceinline__ unsigned outer_mask(const AbParams &P, const Uni &u, const Lanes &v, int d) {
+// outer_mask, wz_match.cpp:601-618, in two parts. outer_pat: the pattern of the k outermost
+// quads (levels 0..k-1), or -1 when the table does not apply; it is fixed while the search is
+// below level k, so it is taken once on the way down through level k.
+__device__ __forceinline__ int outer_pat(const AbParams &P, const Uni &u) {
   const int k = P.outer_k, L = P.L;
-  if (k < 2 || d < k || d + k > L / 2 || !(u.A & 1ULL) || !(u.B & 1ULL)) return 0xFFu;
+  if (!(u.A & 1ULL) || !(u.B & 1ULL)) return -1;
   int pat = (int)((u.A >> (L - 1)) & 1ULL), mul = 2;
   for (int t = 1; t < k; t++) {
     int sb = (int)(((u.A >> t) & 1) << 3 | ((u.B >> t) & 1) << 2 | ((u.A >> (L - 1 - t)) & 1) << 1 |
                    ((u.B >> (L - 1 - t)) & 1));
     int q = kPosOf[sb];
-    if (q < 0) return 0xFFu;
+    if (q < 0) return -1;
     pat += mul * q;
     mul *= 8;
   }
-  int R[3];
-  for (int j = 0; j < k; j++) {
-    R[j] = resid_at(v, L - 1 - d - j);
-    if ((R[j] & 1) || R[j] < -4 * (j + 1) || R[j] > 4 * (j + 1)) return 0u;
-  }
-  if (k == 2) return P.outer2[(pat * 5 + (R[0] / 2 + 2)) * 9 + (R[1] / 2 + 4)];
-  return P.outer3[((pat * 5 + (R[0] / 2 + 2)) * 9 + (R[1] / 2 + 4)) * 13 + (R[2] / 2 + 6)];
+  return pat;
 }
 
-// first quad index >= k at level d that passes the outer mask and the canon filter
-__device__ __forceinline__ int next_quad(const AbParams &P, int d, int k, unsigned omask, uint32_t ties) {
-  for (; k < 8; k++) {
-    if (d > 0 && !((omask >> k) & 1u)) continue;
-    uint32_t q = quad_bits(d, k), o;
-    int a1 = (q & 8) ? 1 : -1, b1 = (q & 4) ? 1 : -1, a2 = (q & 2) ? 1 : -1, b2 = (q & 1) ? 1 : -1;
-    if (canon_ok(P, d, ties, a1, b1, a2, b2, o)) return k;
-  }
-  return 8;
+// the mask at level d >= 1 from the pattern and the residuals at L-1-d-j (r0 at j = 0)
+__device__ __forceinline__ unsigned outer_mask(const AbParams &P, int pat, const Lanes &v, int d, int r0) {
+  const int k = P.outer_k, L = P.L;
+  if (k < 2 || d < k || d + k > L / 2 || pat < 0) return 0xFFu;
+  int R[3];
+  R[0] = r0;
+  for (int j = 1; j < k; j++) R[j] = resid_at(v, L - 1 - d - j);
+  for (int j = 0; j < k; j++)
+    if ((R[j] & 1) || R[j] < -4 * (j + 1) || R[j] > 4 * (j + 1)) return 0u;
+  if (k == 2) return P.outer2[(pat * 5 + (R[0] / 2 + 2)) * 9 + (R[1] / 2 + 4)];
+  return P.outer3[((pat * 5 + (R[0] / 2 + 2)) * 9 + (R[1] / 2 + 4)) * 13 + (R[2] / 2 + 6)];
 }
 
 // The level filter of the allowed rows (fh_abp_filter, wz_match.cpp:1055-1075): a row
@@ -242,7 +237,10 @@ __device__ __forceinline__ uint64_t all_rows(int w, int nrows) {
   return nrows - lo >= 64 ? ~0ULL : ((1ULL << (nrows - lo)) - 1ULL);
 }
 
-__global__ void __launch_bounds__(32 * AB_WARPS) ab_kernel(AbParams P) {
+// MINB: resident blocks per SM the register budget is cut for (2: up to 128 registers a
+// thread; 3: up to 85, with a few spills)
+template <int MINB>
+__global__ void __launch_bounds__(32 * AB_WARPS, MINB) ab_kernel(AbParams P) {
   // the quad loop's canon filter as tables (entry 16 is the root level d = 0): bit k of
   // s_elig[t] says quad k passes canon_ok with incoming ties t, s_ntie[t][k] its outgoing ties
   __shared__ uint8_t s_elig[17];
@@ -259,6 +257,16 @@ __global__ void __launch_bounds__(32 * AB_WARPS) ab_kernel(AbParams P) {
       s_ntie[t][k] = (uint8_t)o;
     }
     s_elig[t] = (uint8_t)elig;
+  }
+  __shared__ uint8_t s_cls[64];   // residue class of each position
+  __shared__ uint64_t s_cm[8];    // positions of each class, as bits
+  __shared__ int s_tic[8];        // positions in each class
+  if (threadIdx.x < 64) s_cls[threadIdx.x] = (uint8_t)(threadIdx.x % P.m);
+  if (threadIdx.x < 8) {
+    uint64_t cm = 0;
+    for (int p = threadIdx.x; p < P.L; p += P.m) cm |= 1ULL << p;
+    s_cm[threadIdx.x] = threadIdx.x < P.m ? cm : 0ULL;
+    s_tic[threadIdx.x] = P.tic[threadIdx.x];
   }
   __syncthreads();
   // first eligible quad >= k at level d (next_quad): the outer mask applies from d = 1
@@ -279,6 +287,8 @@ __global__ void __launch_bounds__(32 * AB_WARPS) ab_kernel(AbParams P) {
   int my_res = 0;
   uint64_t *lv = P.bits + (size_t)slot * (P.half + 1) * P.Wcap;
   const int L = P.L, n = P.n, half = P.half, m = P.m;
+  const bool two = n >= 33;  // a second shift slot per lane
+  const uint64_t ends = 1ULL | (1ULL << (L - 1));  // positions 0 and L-1 (the early check)
 
   while (true) {
     unsigned long long idx = 0;
@@ -309,17 +319,13 @@ __global__ void __launch_bounds__(32 * AB_WARPS) ab_kernel(AbParams P) {
       continue;
     }
     v.D0 = v.D1 = 0;
-    v.K0 = v.s0 ? 2 * (P.n1 - v.s0) : 0;
-    v.K1 = v.s1 ? 2 * (P.n1 - v.s1) : 0;
+    v.kb0 = v.s0 ? 2 * (P.n1 - v.s0) : 0;
+    v.kb1 = v.s1 ? 2 * (P.n1 - v.s1) : 0;
+    v.K0 = v.kb0;
+    v.K1 = v.kb1;
     Uni u;
     u.A = u.B = u.Pm = 0;
-    u.pa = u.pb = u.plc = 0;
-    for (int c = 0; c < 8; c++) {
-      u.pa |= 64ULL << (8 * c);
-      u.pb |= 64ULL << (8 * c);
-      u.plc |= 64ULL << (8 * c);
-    }
-    u.sumA = u.sumB = 0;
+    int opat = -1;  // outer_pat, taken when the search passes level outer_k
     long long nodes = 0, cur = 0;
     bool aborted = false, found = false, abandoned = false;
     const long long t_start = clock64();
@@ -342,7 +348,8 @@ __global__ void __launch_bounds__(32 * AB_WARPS) ab_kernel(AbParams P) {
       }
       if (d == half) {
         // ---- leaf: final_ok (and the free middle for odd length), wz_match.cpp:1178-1205 ----
-        auto final_ok = [&](int sA, int sB) -> bool {
+        auto final_ok = [&]() -> bool {
+          const int sA = 2 * __popcll(u.A) - __popcll(u.Pm), sB = 2 * __popcll(u.B) - __popcll(u.Pm);
           if (absi(sA) != P.absA || absi(sB) != P.absB) return false;
           bool eq = (!v.s0 || v.D0 == v.t0) && (!v.s1 || v.D1 == v.t1);
           if (!__all_sync(FULL_MASK, eq)) return false;
@@ -353,7 +360,7 @@ __global__ void __launch_bounds__(32 * AB_WARPS) ab_kernel(AbParams P) {
             for (int w = wlo[half] + lane; w < whi[half]; w += 32) {
               uint64_t x = lst[w];
               for (int c = 0; c < m; c++) {
-                const int pa = fld(u.pa, c), pb = fld(u.pb, c);
+                const int pa = ssum(u.A, u.Pm, s_cm[c]), pb = ssum(u.B, u.Pm, s_cm[c]);
                 x &= mask_of(P, cd, c, 0, pa)[w] & mask_of(P, cd, c, 1, pa)[w] &
                      mask_of(P, cd, c, 2, pb)[w] & mask_of(P, cd, c, 3, pb)[w];
               }
@@ -364,15 +371,16 @@ __global__ void __launch_bounds__(32 * AB_WARPS) ab_kernel(AbParams P) {
           return true;
         };
         if (L & 1) {
-          const int mid = half;
+          const uint64_t mb = 1ULL << half;
           for (int km = 0; km < 4 && !found; km++) {
-            int av = (km < 2) ? 1 : -1, bv = (km & 1) ? -1 : 1;
-            place(u, v, mid, av, bv, L, m);
+            const int av = (km < 2) ? 1 : -1, bv = (km & 1) ? -1 : 1;
+            place2(u, mb, 0ULL, av, bv, -1, -1);
+            corr(v, u, two);
             nodes++;
-            if (final_ok(u.sumA, u.sumB)) found = true;
-            else unplace(u, v, mid, L, m);
+            if (final_ok()) found = true;
+            else clear_bits(u, mb);
           }
-        } else if (final_ok(u.sumA, u.sumB)) {
+        } else if (final_ok()) {
           found = true;
         }
         if (found) break;
@@ -380,10 +388,8 @@ __global__ void __launch_bounds__(32 * AB_WARPS) ab_kernel(AbParams P) {
         d--;
         {
           uint32_t c0 = __shfl_sync(FULL_MASK, my_ctrl, d);
-          int k = c0 & 15;
-          unplace(u, v, L - 1 - d, L, m);
-          unplace(u, v, d, L, m);
-          if (lane == d) my_ctrl = (c0 & ~15u) | (uint32_t)(k + 1);
+          clear_bits(u, pair_bits(d, L));
+          if (lane == d) my_ctrl = (c0 & ~15u) | (uint32_t)((c0 & 15) + 1);
         }
         continue;
       }
@@ -395,8 +401,7 @@ __global__ void __launch_bounds__(32 * AB_WARPS) ab_kernel(AbParams P) {
         if (d == 0) break;  // clean exhaustion
         d--;
         uint32_t cp = __shfl_sync(FULL_MASK, my_ctrl, d);
-        unplace(u, v, L - 1 - d, L, m);
-        unplace(u, v, d, L, m);
+        clear_bits(u, pair_bits(d, L));
         if (lane == d) my_ctrl = (cp & ~15u) | (uint32_t)((cp & 15) + 1);
         continue;
       }
@@ -410,42 +415,50 @@ __global__ void __launch_bounds__(32 * AB_WARPS) ab_kernel(AbParams P) {
         aborted = true;
         break;
       }
-      // early outer-correlation check (wz_match.cpp:1256-1259)
+      // early outer-correlation check (wz_match.cpp:1256-1259): positions 0 and L-1 are placed
+      // from level 1 on, so the sum of the four products is 2 - 2 #mismatches per sequence
       if (P.early && d > 0) {
-        int lhs = sgnbit(u.A, 0) * a2 + sgnbit(u.B, 0) * b2 + sgnbit(u.A, L - 1) * a1 + sgnbit(u.B, L - 1) * b1;
+        const uint64_t qa = (a2 > 0 ? 1ULL : 0ULL) | (a1 > 0 ? (1ULL << (L - 1)) : 0ULL);
+        const uint64_t qb = (b2 > 0 ? 1ULL : 0ULL) | (b1 > 0 ? (1ULL << (L - 1)) : 0ULL);
+        const int lhs = 4 - 2 * (__popcll((u.A ^ qa) & ends) + __popcll((u.B ^ qb) & ends));
         if (lhs != __shfl_sync(FULL_MASK, my_res, d)) {
           if (lane == d) my_ctrl = (c0 & ~15u) | (uint32_t)(k + 1);
           continue;
         }
       }
-      place(u, v, d, a1, b1, L, m);
-      place(u, v, L - 1 - d, a2, b2, L, m);
+      const uint64_t pb2 = pair_bits(d, L);
+      place2(u, 1ULL << d, 1ULL << (L - 1 - d), a1, b1, a2, b2);
       const int rem = L - 2 * (d + 1);
-      bool prune = !(((absi(P.absA - u.sumA) <= rem) || (absi(-P.absA - u.sumA) <= rem)) &&
-                     ((absi(P.absB - u.sumB) <= rem) || (absi(-P.absB - u.sumB) <= rem)));
+      const int sumA = 2 * __popcll(u.A) - __popcll(u.Pm), sumB = 2 * __popcll(u.B) - __popcll(u.Pm);
+      bool prune = !(((absi(P.absA - sumA) <= rem) || (absi(-P.absA - sumA) <= rem)) &&
+                     ((absi(P.absB - sumB) <= rem) || (absi(-P.absB - sumB) <= rem)));
       if (!prune) {
+        corr(v, u, two);
         bool bad = (v.s0 && absi(v.t0 - v.D0) > v.K0) || (v.s1 && absi(v.t1 - v.D1) > v.K1);
         prune = __any_sync(FULL_MASK, bad);
       }
       if (!prune && rows) {
         // fh_abp_filter(d): the level-(d+1) list from the level-d list (all rows at d = 0)
-        const int c1 = d % m, c2 = (L - 1 - d) % m;
-        const int r1 = P.tic[c1] - fld(u.plc, c1), pa1 = fld(u.pa, c1), pb1 = fld(u.pb, c1);
-        const int r2 = P.tic[c2] - fld(u.plc, c2), pa2 = fld(u.pa, c2), pb2 = fld(u.pb, c2);
+        const int c1 = s_cls[d], c2 = s_cls[L - 1 - d];
+        const uint64_t m1 = s_cm[c1], m2 = s_cm[c2];
+        const int r1 = s_tic[c1] - __popcll(u.Pm & m1), pa1 = ssum(u.A, u.Pm, m1), pb1 = ssum(u.B, u.Pm, m1);
+        const int r2 = s_tic[c2] - __popcll(u.Pm & m2), pa2 = ssum(u.A, u.Pm, m2), pb2 = ssum(u.B, u.Pm, m2);
+        const uint64_t *src = lv + (size_t)d * P.Wcap;
+        uint64_t *dst = lv + (size_t)(d + 1) * P.Wcap;
+        const int lo = wlo[d], hi = whi[d];
+        int nlo, nhi;
         const uint64_t *k1a = mask_of(P, cd, c1, 0, pa1 - r1), *k1b = mask_of(P, cd, c1, 1, pa1 + r1);
         const uint64_t *q1a = mask_of(P, cd, c1, 2, pb1 - r1), *q1b = mask_of(P, cd, c1, 3, pb1 + r1);
         const uint64_t *k2a = mask_of(P, cd, c2, 0, pa2 - r2), *k2b = mask_of(P, cd, c2, 1, pa2 + r2);
         const uint64_t *q2a = mask_of(P, cd, c2, 2, pb2 - r2), *q2b = mask_of(P, cd, c2, 3, pb2 + r2);
-        const uint64_t *src = lv + (size_t)d * P.Wcap;
-        uint64_t *dst = lv + (size_t)(d + 1) * P.Wcap;
         int pa[8], pb[8];
         if (P.a2)
           for (int c = 0; c < 8; c++) {
-            pa[c] = c < m ? fld(u.pa, c) : 0;
-            pb[c] = c < m ? fld(u.pb, c) : 0;
+            pa[c] = c < m ? ssum(u.A, u.Pm, s_cm[c]) : 0;
+            pb[c] = c < m ? ssum(u.B, u.Pm, s_cm[c]) : 0;
           }
         int mylo = 1 << 30, myhi = -1;
-        for (int w = wlo[d] + lane; w < whi[d]; w += 32) {
+        for (int w = lo + lane; w < hi; w += 32) {
           uint64_t x = d == 0 ? all_rows(w, cd.nrows) : src[w];
           x &= k1a[w] & k1b[w] & q1a[w] & q1b[w];
           if (c2 != c1) x &= k2a[w] & k2b[w] & q2a[w] & q2b[w];
@@ -461,15 +474,15 @@ __global__ void __launch_bounds__(32 * AB_WARPS) ab_kernel(AbParams P) {
             myhi = w;
           }
         }
-        const int nlo = __reduce_min_sync(FULL_MASK, mylo), nhi = __reduce_max_sync(FULL_MASK, myhi);
+        nlo = __reduce_min_sync(FULL_MASK, mylo);
+        nhi = __reduce_max_sync(FULL_MASK, myhi);
         __syncwarp();
         wlo[d + 1] = nlo;  // the warp's uniform state: every lane writes the same value
         whi[d + 1] = nhi + 1;
         prune = nhi < 0;
       }
       if (prune) {
-        unplace(u, v, L - 1 - d, L, m);
-        unplace(u, v, d, L, m);
+        clear_bits(u, pb2);
         if (lane == d) my_ctrl = (c0 & ~15u) | (uint32_t)(k + 1);
         continue;
       }
@@ -479,12 +492,14 @@ __global__ void __launch_bounds__(32 * AB_WARPS) ab_kernel(AbParams P) {
       unsigned om = 0xFFu;
       int r_e = 0;
       if (nd < half) {
-        if (P.outer_k) om = outer_mask(P, u, v, nd);
         r_e = resid_at(v, L - 1 - nd);
+        if (P.outer_k) {
+          if (nd == P.outer_k) opat = outer_pat(P, u);
+          om = outer_mask(P, opat, v, nd, r_e);
+        }
       }
       if (om == 0u) {  // fh_ab_search(d+1) returns false at once: undo and try the next quad
-        unplace(u, v, L - 1 - d, L, m);
-        unplace(u, v, d, L, m);
+        clear_bits(u, pb2);
         if (lane == d) my_ctrl = (c0 & ~15u) | (uint32_t)(k + 1);
         continue;
       }
@@ -716,7 +731,7 @@ extern "C" int bs_complete_ab_batch(bs_ctx *ctx, const bs_ab_cand *cands, long l
     hc[i].mask_off = set_of[i] >= 0 ? offs[set_of[i]] : 0;
     hc[i].row_off = cands[i].nrows > 0 ? cands[i].row_off : 0;
   }
-  if (opt->blocks_per_sm < 0 || opt->blocks_per_sm > 2) return BS_ERR_ARG;
+  if (opt->blocks_per_sm < 0 || opt->blocks_per_sm > 3) return BS_ERR_ARG;
   const int grid = ctx->num_sms * (opt->blocks_per_sm ? opt->blocks_per_sm : 2);
   const long long slots = (long long)grid * AB_WARPS;
   rc = bs_ensure_dev((void **)&Bf->cands, &Bf->cand_cap, ncand, sizeof(AbCandDev));
@@ -777,7 +792,10 @@ extern "C" int bs_complete_ab_batch(bs_ctx *ctx, const bs_ab_cand *cands, long l
       for (int p = c; p < n1; p += opt->m) P.tic[c]++;
   }
   bs_timed_begin(ctx);
-  ab_kernel<<<grid, 32 * AB_WARPS, 0, s>>>(P);
+  if (opt->blocks_per_sm == 3)
+    ab_kernel<3><<<grid, 32 * AB_WARPS, 0, s>>>(P);
+  else
+    ab_kernel<2><<<grid, 32 * AB_WARPS, 0, s>>>(P);
   bs_timed_end(ctx);
   CK(cudaGetLastError());
   std::vector<uint64_t> ab(2 * ncand);

@@ -9,7 +9,8 @@ these sizes are picked by timing short probes of the workload itself:
   tune_stream(ctx, cell)       fine_nodes x dfs_blocks on the first `probe` survivors of one
                                cell (a front-only prefix, the lane's own unit of work), then
                                wave_nodes for the best pair
-  tune_completer(ctx, cands)   blocks_per_sm x chunk on a sample of drained candidates
+  tune_completer(ctx, cands)   blocks_per_sm x chunk on a sample of drained candidates, each
+                               charged at most 2^14 nodes
 
 Each returns (choice, table of every probe's rate). tune_lane() runs both on a lane's first
 kept cell and returns one dict for run_lane(tuning=...). Results are cached per (device,
@@ -25,7 +26,7 @@ from .stream import cd_stream
 FINE = (5e3, 2e4, 8e4)
 BLOCKS = (4, 5, 6)
 WAVES = (2e9, 8e9, 3.2e10)
-AB_BLOCKS = (1, 2)
+AB_BLOCKS = (1, 2, 3)
 CHUNKS = (8192, 65536)
 
 _CACHE = {}
@@ -71,33 +72,42 @@ def tune_stream(ctx, cell, m=6, probe=20000, pins=None):
     return out
 
 
-def tune_completer(ctx, cands, budget, rows=None, m=6, sample=4096):
+def tune_completer(ctx, cands, budget, rows=None, m=6, sample=16384, probe_budget=1 << 14):
     """cands: the drained candidates (int8 [k, 2, n] or words). Returns
-    ({blocks_per_sm, chunk}, probes), timing each setting on the same first `sample`."""
+    ({blocks_per_sm, chunk}, probes), timing each setting on the same first `sample`.
+
+    The probes charge at most `probe_budget` nodes per candidate: at the lane's own budget a
+    few candidates that run to it take seconds on one warp, and a probe that waits for them
+    measures that tail, not the rate of a full device. A setting within 3 % of the best is
+    taken as equal, and of equals the one with more resident warps wins."""
     cands = np.asarray(cands)[:sample]
-    key = ("complete", ctx.n, ctx.sig, budget, len(cands), hash(cands.tobytes()),
+    pb = min(budget, probe_budget) if budget > 0 else probe_budget
+    key = ("complete", ctx.n, ctx.sig, pb, len(cands), hash(cands.tobytes()),
            None if rows is None else hash(np.asarray(rows).tobytes()))
     if key in _CACHE:
         return _CACHE[key]
+    complete_ab(ctx, cands[:256], pb, rows=rows, m=m)  # warm-up
     probes = []
     for blocks in AB_BLOCKS:
         for chunk in CHUNKS:
             def fn(blocks=blocks, chunk=chunk):
                 nodes = 0
                 for c0 in range(0, len(cands), chunk):
-                    _, nd, _, _ = complete_ab(ctx, cands[c0:c0 + chunk], budget, rows=rows, m=m,
+                    _, nd, _, _ = complete_ab(ctx, cands[c0:c0 + chunk], pb, rows=rows, m=m,
                                               blocks_per_sm=blocks)
                     nodes += int(nd.sum())
                 return nodes
-            probes.append(dict(blocks_per_sm=blocks, chunk=chunk, nodes_per_s=_rate(fn, reps=1)))
-    best = max(probes, key=lambda p: p["nodes_per_s"])
+            probes.append(dict(blocks_per_sm=blocks, chunk=chunk, nodes_per_s=_rate(fn, reps=2)))
+    top = max(p["nodes_per_s"] for p in probes)
+    near = [p for p in probes if p["nodes_per_s"] >= 0.97 * top]
+    best = max(near, key=lambda p: (p["blocks_per_sm"], p["chunk"], p["nodes_per_s"]))
     out = (dict(blocks_per_sm=best["blocks_per_sm"], chunk=best["chunk"]), probes)
     _CACHE[key] = out
     return out
 
 
 def tune_lane(ctx, n, sig, listing, skip, end, budget, buf_cap=500000, drain_top=50000,
-              probe=20000, sample=4096):
+              probe=20000, sample=16384):
     """Work sizes for a lane over raw cells [skip, end): both probes on its first kept cell
     that has allowed rows. Returns (tuning dict for run_lane, report)."""
     from .cells import ab_rows

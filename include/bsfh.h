@@ -269,7 +269,7 @@ typedef struct {
                            977-1047, 1069-1072); mode 1, the reference's shadow instrument, is
                            not built (BS_ERR_ARG) */
   double max_seconds;   /* per-candidate wall limit on the device (0 = none) */
-  int32_t blocks_per_sm; /* resident completer blocks of 8 warps per SM: 1 or 2 (0 = 2) */
+  int32_t blocks_per_sm; /* resident completer blocks of 8 warps per SM: 1, 2 or 3 (0 = 2) */
   int32_t reserved;
 } bs_ab_opts;
 

@@ -22,7 +22,10 @@ def unpack(w, L):
     return np.where(bits == 1, 1, -1).astype(np.int8)
 
 
-def test_completions_golden(gpu):
+@pytest.mark.parametrize("blocks", [0, 3])
+def test_completions_golden(gpu, blocks):
+    """blocks: resident completer blocks per SM (0 = the default 2; 3 = the build whose
+    register budget is cut for three), which must not change a result."""
     from bs45_quantum_explorer_gb300.complete import complete_ab
     from bs45_quantum_explorer_gb300.hall import Context
     g = np.load(os.path.join(G, "complete_golden.npz"))
@@ -36,7 +39,7 @@ def test_completions_golden(gpu):
         ctx = Context(n, sig)
         cands = np.stack([cd[int(cases[i, 9])] for i in idx])
         rr = [rows[int(cases[i, 5]):int(cases[i, 5]) + int(cases[i, 6])] if use_rows else None for i in idx]
-        v, nodes, A, B = complete_ab(ctx, cands, budget, rows_per_cand=rr)
+        v, nodes, A, B = complete_ab(ctx, cands, budget, rows_per_cand=rr, blocks_per_sm=blocks)
         for t, i in enumerate(idx):
             assert (v[t], nodes[t]) == (cases[i, 7], cases[i, 8]), (n, a, b, budget, use_rows, t)
             if v[t] == 0:
