@@ -338,6 +338,9 @@ def run_first_hit(seconds, cpu_seconds=10.0, with_cpu=True, drain_top=50000, tun
            if res.complete_device_ms > 0 else None,
            "ab_nodes_per_s_api": res.total_ab_nodes / res.complete_s if res.complete_s > 0 else None,
            "dfs_nodes": res.dfs_nodes, "stream_s": res.stream_s,
+           "stream_device_s": res.stream_device_ms * 1e-3,
+           "gpu_busy_frac": ((res.complete_device_ms + res.stream_device_ms) * 1e-3 /
+                             res.timings["wall_s"]) if res.timings.get("wall_s") else None,
            "dfs_nodes_per_s": res.dfs_nodes / res.stream_s if res.stream_s > 0 else None,
            "wall_s": res.timings.get("wall_s"), "found": res.found}
     if tune_report is not None:

@@ -447,35 +447,55 @@ __global__ void __launch_bounds__(32 * AB_WARPS, MINB) ab_kernel(AbParams P) {
         uint64_t *dst = lv + (size_t)(d + 1) * P.Wcap;
         const int lo = wlo[d], hi = whi[d];
         int nlo, nhi;
-        const uint64_t *k1a = mask_of(P, cd, c1, 0, pa1 - r1), *k1b = mask_of(P, cd, c1, 1, pa1 + r1);
-        const uint64_t *q1a = mask_of(P, cd, c1, 2, pb1 - r1), *q1b = mask_of(P, cd, c1, 3, pb1 + r1);
-        const uint64_t *k2a = mask_of(P, cd, c2, 0, pa2 - r2), *k2b = mask_of(P, cd, c2, 1, pa2 + r2);
-        const uint64_t *q2a = mask_of(P, cd, c2, 2, pb2 - r2), *q2b = mask_of(P, cd, c2, 3, pb2 + r2);
-        int pa[8], pb[8];
-        if (P.a2)
-          for (int c = 0; c < 8; c++) {
-            pa[c] = c < m ? ssum(u.A, u.Pm, s_cm[c]) : 0;
-            pb[c] = c < m ? ssum(u.B, u.Pm, s_cm[c]) : 0;
+        if (!P.a2 && hi - lo <= 4) {
+          // up to four words: lane 8i + j loads mask j (class c1 for j < 4, c2 for j >= 4;
+          // kind j & 3) of word lo + i, and three butterfly steps AND the eight together
+          const int j = lane & 7, w = lo + (lane >> 3), kind = j & 3;
+          const int c = j < 4 ? c1 : c2, r = j < 4 ? r1 : r2;
+          const int pv = (kind < 2) ? (j < 4 ? pa1 : pa2) : (j < 4 ? pb1 : pb2);
+          const bool live = w < hi;
+          uint64_t x = live ? mask_of(P, cd, c, kind, (kind & 1) ? pv + r : pv - r)[w] : ~0ULL;
+          x &= __shfl_xor_sync(FULL_MASK, x, 1);
+          x &= __shfl_xor_sync(FULL_MASK, x, 2);
+          x &= __shfl_xor_sync(FULL_MASK, x, 4);
+          if (j == 0 && live) {
+            x &= d == 0 ? all_rows(w, cd.nrows) : src[w];
+            dst[w] = x;
           }
-        int mylo = 1 << 30, myhi = -1;
-        for (int w = lo + lane; w < hi; w += 32) {
-          uint64_t x = d == 0 ? all_rows(w, cd.nrows) : src[w];
-          x &= k1a[w] & k1b[w] & q1a[w] & q1b[w];
-          if (c2 != c1) x &= k2a[w] & k2b[w] & q2a[w] & q2b[w];
-          if (P.a2)  // A2 on the rows that passed the box, at depth d + 1
-            for (uint64_t y = x; y; y &= y - 1) {
-              const int bit = __ffsll((long long)y) - 1;
-              if (!a2_row(P, P.rows8 + 16 * (cd.row_off + (long long)w * 64 + bit), pa, pb, d + 1))
-                x &= ~(1ULL << bit);
+          const unsigned ball = __ballot_sync(FULL_MASK, j == 0 && live && x != 0);
+          nlo = ball ? lo + ((__ffs(ball) - 1) >> 3) : 1 << 30;
+          nhi = ball ? lo + ((31 - __clz(ball)) >> 3) : -1;
+        } else {
+          const uint64_t *k1a = mask_of(P, cd, c1, 0, pa1 - r1), *k1b = mask_of(P, cd, c1, 1, pa1 + r1);
+          const uint64_t *q1a = mask_of(P, cd, c1, 2, pb1 - r1), *q1b = mask_of(P, cd, c1, 3, pb1 + r1);
+          const uint64_t *k2a = mask_of(P, cd, c2, 0, pa2 - r2), *k2b = mask_of(P, cd, c2, 1, pa2 + r2);
+          const uint64_t *q2a = mask_of(P, cd, c2, 2, pb2 - r2), *q2b = mask_of(P, cd, c2, 3, pb2 + r2);
+          int pa[8], pb[8];
+          if (P.a2)
+            for (int c = 0; c < 8; c++) {
+              pa[c] = c < m ? ssum(u.A, u.Pm, s_cm[c]) : 0;
+              pb[c] = c < m ? ssum(u.B, u.Pm, s_cm[c]) : 0;
             }
-          dst[w] = x;
-          if (x) {
-            mylo = min(mylo, w);
-            myhi = w;
+          int mylo = 1 << 30, myhi = -1;
+          for (int w = lo + lane; w < hi; w += 32) {
+            uint64_t x = d == 0 ? all_rows(w, cd.nrows) : src[w];
+            x &= k1a[w] & k1b[w] & q1a[w] & q1b[w];
+            if (c2 != c1) x &= k2a[w] & k2b[w] & q2a[w] & q2b[w];
+            if (P.a2)  // A2 on the rows that passed the box, at depth d + 1
+              for (uint64_t y = x; y; y &= y - 1) {
+                const int bit = __ffsll((long long)y) - 1;
+                if (!a2_row(P, P.rows8 + 16 * (cd.row_off + (long long)w * 64 + bit), pa, pb, d + 1))
+                  x &= ~(1ULL << bit);
+              }
+            dst[w] = x;
+            if (x) {
+              mylo = min(mylo, w);
+              myhi = w;
+            }
           }
+          nlo = __reduce_min_sync(FULL_MASK, mylo);
+          nhi = __reduce_max_sync(FULL_MASK, myhi);
         }
-        nlo = __reduce_min_sync(FULL_MASK, mylo);
-        nhi = __reduce_max_sync(FULL_MASK, myhi);
         __syncwarp();
         wlo[d + 1] = nlo;  // the warp's uniform state: every lane writes the same value
         whi[d + 1] = nhi + 1;

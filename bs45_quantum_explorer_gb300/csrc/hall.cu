@@ -305,6 +305,18 @@ __device__ __forceinline__ bool mbar_wait(uint32_t a, uint32_t parity, volatile 
   }
   return true;
 }
+// arrive once on the mbarrier and add `bytes` to the transaction count of its current phase
+__device__ __forceinline__ void mbar_expect_tx(uint32_t a, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(a), "r"(bytes) : "memory");
+}
+// One contiguous global -> shared copy on the async proxy, completing `bytes` on the mbarrier:
+// both addresses 16-byte aligned, bytes a multiple of 16.
+__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void *src, uint32_t bytes, uint32_t mbar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+      "l"(src), "r"(bytes), "r"(mbar)
+      : "memory");
+}
 __device__ __forceinline__ void fence_async_smem() {
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
@@ -675,6 +687,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1) hall_tc_kernel(TcParams P) {
 // and that read, not the MMA, bounds it; on the microbench mix and on stream leaves about
 // 2-3 % of pairs survive the screen, so the full reads are paid for those alone.
 constexpr int SC_BUFS = 4;
+constexpr int SC_RUN = 256;  // survivors a screen epilogue warp holds before it writes them out
+constexpr int SC_RING = 4;   // tiles of packed words each screen producer has in flight
+constexpr int SC_RAW_BYTES = TC_TILE * 16;  // one tile of pairs: two 8-byte words each
 constexpr uint32_t SC_COLS = 128;  // TMEM columns per buffer (C then D, 64 each)
 
 __global__ void __launch_bounds__(TC_THREADS, 1) hall_screen_kernel(TcParams P) {
@@ -682,11 +697,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1) hall_screen_kernel(TcParams P) 
   uint8_t *base = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   uint8_t *sA = base;
   uint8_t *sB = sA + TC_STAGES * A_STAGE_BYTES;  // rows 0..63 of each part, 8 KB per part
-  uint64_t *bars = (uint64_t *)(sB + P.nparts * 64 * 128);
-  uint32_t *tmem_slot = (uint32_t *)(bars + 2 * TC_STAGES + 2 * SC_BUFS);
+  uint8_t *sraw = sB + P.nparts * 64 * 128;      // [TC_PRODUCERS][SC_RING] tiles of packed words
+  uint32_t *srun = (uint32_t *)(sraw + TC_PRODUCERS * SC_RING * SC_RAW_BYTES);  // [8][SC_RUN]
+  uint64_t *bars = (uint64_t *)(srun + 8 * SC_RUN);
+  uint32_t *tmem_slot = (uint32_t *)(bars + 2 * TC_STAGES + 2 * SC_BUFS + TC_PRODUCERS * SC_RING);
   volatile int *abort_flag = (volatile int *)(tmem_slot + 1);
   const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + TC_STAGES);
   const uint32_t tfull0 = smem_u32(bars + 2 * TC_STAGES), tempty0 = tfull0 + 8 * SC_BUFS;
+  const uint32_t raw0 = tempty0 + 8 * SC_BUFS;  // [TC_PRODUCERS][SC_RING]: a ring tile landed
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const long long G = gridDim.x;
 
@@ -706,6 +724,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) hall_screen_kernel(TcParams P) 
       mbar_init(tfull0 + 8 * b, 1);
       mbar_init(tempty0 + 8 * b, 4);  // the four warps of the group that reads the buffer
     }
+    for (int r = 0; r < TC_PRODUCERS * SC_RING; r++) mbar_init(raw0 + 8 * r, 1);
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -719,24 +738,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1) hall_screen_kernel(TcParams P) 
   if (warp < TC_PRODUCERS) {
     const uint32_t neg2 = P.one2 | 0x80008000u;
     const int nchunks = 2 * P.ksteps;
-    auto fetch = [&](long long pair) -> uint4 {
-      return pair < P.npairs ? load_pair(P.bits, pair, P.bits_a16) : make_uint4(0, 0, 0, 0);
-    };
+    const long long stride = (long long)TC_PRODUCERS * G;  // between this warp's tiles
     int it = warp;
     long long tile = blockIdx.x + (long long)it * G;
-    uint4 wv[4];
-#pragma unroll
-    for (int rr = 0; rr < 4; rr++) wv[rr] = tile < P.ntiles ? fetch(tile * TC_TILE + lane + 32 * rr) : make_uint4(0, 0, 0, 0);
-    while (tile < P.ntiles) {
-      const long long next = tile + TC_PRODUCERS * G;
-      uint4 nw[4];
-#pragma unroll
-      for (int rr = 0; rr < 4; rr++) nw[rr] = next < P.ntiles ? fetch(next * TC_TILE + lane + 32 * rr) : make_uint4(0, 0, 0, 0);
-      const int st = it % TC_STAGES;
-      if (!mbar_wait(empty0 + 8 * st, ((it / TC_STAGES) & 1) ^ 1, abort_flag)) {
-        if (!*abort_flag) { set_status(P.status, BS_ERR_TIMEOUT); *abort_flag = 1; }
-        break;
-      }
+    auto expand = [&](const uint4 *wv, int st) {
       uint8_t *AC = sA + st * A_STAGE_BYTES, *AD = AC + A_SEQ_BYTES;
 #pragma unroll
       for (int rr = 0; rr < 4; rr++) {
@@ -747,10 +752,82 @@ __global__ void __launch_bounds__(TC_THREADS, 1) hall_screen_kernel(TcParams P) 
       fence_async_smem();
       __syncwarp();
       if (lane == 0) mbar_arrive(full0 + 8 * st);
+    };
+    if (P.bits_a16) {
+      // The warp's tiles arrive by bulk copies into its ring, SC_RING tiles ahead of the one
+      // it expands; the j-th tile of the warp lands in slot j % SC_RING, phase (j / SC_RING) & 1.
+      // A tile is 128 pairs of two words, 2 KB, contiguous (the last one shorter).
+      uint8_t *ring = sraw + warp * SC_RING * SC_RAW_BYTES;
+      const uint32_t rbar = raw0 + 8 * warp * SC_RING;
+      auto issue = [&](long long t, int slot) {
+        const long long p0 = t * TC_TILE;
+        const long long np = P.npairs - p0 < TC_TILE ? P.npairs - p0 : TC_TILE;
+        const uint32_t bytes = (uint32_t)np * 16u;
+        mbar_expect_tx(rbar + 8 * slot, bytes);
+        bulk_g2s(smem_u32(ring + slot * SC_RAW_BYTES), P.bits + 2 * p0, bytes, rbar + 8 * slot);
+      };
+      long long issued = 0, j = 0;  // copies issued and tiles consumed by this warp (uniform)
+      for (int r = 0; r < SC_RING; r++)
+        if (tile + r * stride < P.ntiles) {
+          if (lane == 0) issue(tile + r * stride, r);
+          issued++;
+        }
+      while (tile < P.ntiles) {
+        const int slot = (int)(j % SC_RING);
+        if (!__all_sync(FULL_MASK, mbar_wait(rbar + 8 * slot, (uint32_t)(j / SC_RING) & 1, abort_flag))) {
+          if (!*abort_flag) { set_status(P.status, BS_ERR_TIMEOUT); *abort_flag = 1; }
+          break;
+        }
+        uint4 wv[4];
+        const uint4 *src = (const uint4 *)(ring + slot * SC_RAW_BYTES);
 #pragma unroll
-      for (int rr = 0; rr < 4; rr++) wv[rr] = nw[rr];
-      tile = next;
-      it += TC_PRODUCERS;
+        for (int rr = 0; rr < 4; rr++) wv[rr] = src[lane + 32 * rr];
+        __syncwarp();
+        j++;
+        const long long ahead = tile + SC_RING * stride;
+        if (ahead < P.ntiles) {  // refill the slot just read
+          if (lane == 0) {
+            fence_async_smem();
+            issue(ahead, slot);
+          }
+          issued++;
+        }
+        const int st = it % TC_STAGES;
+        if (!__all_sync(FULL_MASK, mbar_wait(empty0 + 8 * st, ((it / TC_STAGES) & 1) ^ 1, abort_flag))) {
+          if (!*abort_flag) { set_status(P.status, BS_ERR_TIMEOUT); *abort_flag = 1; }
+          break;
+        }
+        expand(wv, st);
+        tile += stride;
+        it += TC_PRODUCERS;
+      }
+      // after an abort: wait (bounded) for the copies still landing in the ring before the
+      // block exits
+      for (long long k = j; k < issued; k++)
+        mbar_wait(rbar + 8 * (int)(k % SC_RING), (uint32_t)(k / SC_RING) & 1, abort_flag, false);
+    } else {
+      auto fetch = [&](long long pair) -> uint4 {
+        return pair < P.npairs ? load_pair(P.bits, pair, 0) : make_uint4(0, 0, 0, 0);
+      };
+      uint4 wv[4];
+#pragma unroll
+      for (int rr = 0; rr < 4; rr++) wv[rr] = tile < P.ntiles ? fetch(tile * TC_TILE + lane + 32 * rr) : make_uint4(0, 0, 0, 0);
+      while (tile < P.ntiles) {
+        const long long next = tile + stride;
+        uint4 nw[4];
+#pragma unroll
+        for (int rr = 0; rr < 4; rr++) nw[rr] = next < P.ntiles ? fetch(next * TC_TILE + lane + 32 * rr) : make_uint4(0, 0, 0, 0);
+        const int st = it % TC_STAGES;
+        if (!mbar_wait(empty0 + 8 * st, ((it / TC_STAGES) & 1) ^ 1, abort_flag)) {
+          if (!*abort_flag) { set_status(P.status, BS_ERR_TIMEOUT); *abort_flag = 1; }
+          break;
+        }
+        expand(wv, st);
+#pragma unroll
+        for (int rr = 0; rr < 4; rr++) wv[rr] = nw[rr];
+        tile = next;
+        it += TC_PRODUCERS;
+      }
     }
   } else if (warp == TC_MMA_WARP) {
     if (lane == 0) {
@@ -787,6 +864,24 @@ __global__ void __launch_bounds__(TC_THREADS, 1) hall_screen_kernel(TcParams P) 
     const int q = warp & 3;
     const uint32_t lane_off = (uint32_t)(q * 32) << 16;
     const int row = q * 32 + lane;
+    // Survivors collect in the warp's own shared-memory run and go to the list in batches,
+    // one global atomic per batch, so no tile waits for an atomic's round trip.
+    uint32_t *run = srun + (warp - TC_MMA_WARP - 1) * SC_RUN;
+    int nrun = 0;
+    auto flush = [&]() {
+      __syncwarp();
+      unsigned long long base = 0;
+      if (lane == 0) base = atomicAdd(P.count + 4, (unsigned long long)nrun);
+      base = __shfl_sync(FULL_MASK, base, 0);
+      bool over = false;
+      for (int i = lane; i < nrun; i += 32) {
+        if (base + i < P.scr_cap) P.scr[base + i] = run[i];
+        else over = true;
+      }
+      if (__any_sync(FULL_MASK, over) && lane == 0) atomicExch(P.count + 2, 1ULL);
+      __syncwarp();
+      nrun = 0;
+    };
     for (int it = g;; it += 2) {
       const long long tile = blockIdx.x + (long long)it * G;
       if (tile >= P.ntiles) break;
@@ -815,17 +910,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1) hall_screen_kernel(TcParams P) 
       const bool keep = mine && mx < P.reject_above;
       if (mine && !keep) P.pass[pair] = 0;
       const unsigned ball = __ballot_sync(FULL_MASK, keep);
-      if (ball) {  // one atomic per warp for its survivors, in lane order
-        unsigned long long base = 0;
-        if (lane == 0) base = atomicAdd(P.count + 4, (unsigned long long)__popc(ball));
-        base = __shfl_sync(FULL_MASK, base, 0);
-        if (keep) {
-          const unsigned long long k = base + __popc(ball & ((1u << lane) - 1u));
-          if (k < P.scr_cap) P.scr[k] = (unsigned)pair;
-          else atomicExch(P.count + 2, 1ULL);
-        }
-      }
+      if (keep) run[nrun + __popc(ball & ((1u << lane) - 1u))] = (uint32_t)pair;
+      nrun += __popc(ball);
+      if (nrun > SC_RUN - 32) flush();
     }
+    if (nrun) flush();
   }
 
   tc_fence_before();
@@ -836,7 +925,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) hall_screen_kernel(TcParams P) 
 
 size_t screen_smem_bytes(int nparts) {
   return 1024 + (size_t)TC_STAGES * A_STAGE_BYTES + (size_t)nparts * 64 * 128 +
-         (2 * TC_STAGES + 2 * SC_BUFS) * 8 + 16;
+         (size_t)TC_PRODUCERS * SC_RING * SC_RAW_BYTES + sizeof(uint32_t) * 8 * SC_RUN +
+         (2 * TC_STAGES + 2 * SC_BUFS + TC_PRODUCERS * SC_RING) * 8 + 16;
 }
 
 size_t tc_smem_bytes(int nparts) {

@@ -49,6 +49,7 @@ class LaneResult:
     dfs_nodes: int = 0
     completions: int = 0
     stream_s: float = 0.0
+    stream_device_ms: float = 0.0  # the stream's timed kernels (DFS waves and Hall filters)
     complete_s: float = 0.0
     complete_device_ms: float = 0.0
     timings: dict = field(default_factory=dict)
@@ -112,10 +113,14 @@ def run_lane(ctx, n, sig, skip=0, end=0, shard=0, nshard=1, budget=200000, buf_c
         args = [(list(cells[q].tx[:m]), list(cells[q].ty[:m])) for q in group]
         pins = [(cells[q].pinX, cells[q].pinY) for q in group]
         t0 = time.perf_counter()
+        ctx.timing(True)
         surv, cidx, st = cd_stream(ctx, args, m=m, pins=pins, rev=rev, endpos=endpos,
                                    hall_mode=hall_mode, as_words=True, cd_prune=cd_prune,
                                    limit=cut if len(group) == 1 else 0, **stream_kw)
+        ms, _, _ = ctx.timing_read()
+        ctx.timing(False)
         res.stream_s += time.perf_counter() - t0
+        res.stream_device_ms += ms
         if len(group) == 1:
             streamed[group[0]] = (surv, st[0])
             return
