@@ -96,7 +96,8 @@ __device__ __forceinline__ int ssum(uint64_t X, uint64_t Pm, uint64_t sel) {
 // Dab and Kab at the lane's shifts. The pairs (q, q+s) with both positions placed are the set
 // bits of Pm & Pm >> s; each adds a_q a_{q+s} + b_q b_{q+s} = 2 - 2 [a_q != a_{q+s}] -
 // 2 [b_q != b_{q+s}] to Dab[s] and takes 2 from Kab[s]. The search reads them only right
-// after a placement. two: whether shifts 33.. exist (n >= 33), uniform.
+// after a placement. two: whether the shifts 33.. need recomputing (uniform): they exist
+// (n >= 33) and the placement can add a pair at one of them.
 __device__ __forceinline__ void corr(Lanes &v, const Uni &u, bool two) {
   {
     const uint64_t vv = u.Pm & (u.Pm >> v.s0);
@@ -287,8 +288,10 @@ __global__ void __launch_bounds__(32 * AB_WARPS, MINB) ab_kernel(AbParams P) {
   int my_res = 0;
   uint64_t *lv = P.bits + (size_t)slot * (P.half + 1) * P.Wcap;
   const int L = P.L, n = P.n, half = P.half, m = P.m;
-  const bool two = n >= 33;  // a second shift slot per lane
-  const uint64_t ends = 1ULL | (1ULL << (L - 1));  // positions 0 and L-1 (the early check)
+  // A second shift slot per lane when n >= 33. Its shifts s >= 33 pair position d only with
+  // d + s <= L - 1, so placing level d changes them only while d <= L - 34; after that their
+  // Dab is final (and was checked against the target with Kab = 0), so it is not recomputed.
+  const bool two = n >= 33;
 
   while (true) {
     unsigned long long idx = 0;
@@ -325,7 +328,8 @@ __global__ void __launch_bounds__(32 * AB_WARPS, MINB) ab_kernel(AbParams P) {
     v.K1 = v.kb1;
     Uni u;
     u.A = u.B = u.Pm = 0;
-    int opat = -1;  // outer_pat, taken when the search passes level outer_k
+    int opat = -1;   // outer_pat, taken when the search passes level outer_k
+    uint32_t e4 = 0;  // early check: A[L-1], B[L-1], A[0], B[0] as bits 3..0 (set at level 1)
     long long nodes = 0, cur = 0;
     bool aborted = false, found = false, abandoned = false;
     const long long t_start = clock64();
@@ -375,7 +379,7 @@ __global__ void __launch_bounds__(32 * AB_WARPS, MINB) ab_kernel(AbParams P) {
           for (int km = 0; km < 4 && !found; km++) {
             const int av = (km < 2) ? 1 : -1, bv = (km & 1) ? -1 : 1;
             place2(u, mb, 0ULL, av, bv, -1, -1);
-            corr(v, u, two);
+            corr(v, u, false);  // the middle pairs at shifts up to L - 1 - half < 33 only
             nodes++;
             if (final_ok()) found = true;
             else clear_bits(u, mb);
@@ -415,12 +419,11 @@ __global__ void __launch_bounds__(32 * AB_WARPS, MINB) ab_kernel(AbParams P) {
         aborted = true;
         break;
       }
-      // early outer-correlation check (wz_match.cpp:1256-1259): positions 0 and L-1 are placed
-      // from level 1 on, so the sum of the four products is 2 - 2 #mismatches per sequence
+      // early outer-correlation check (wz_match.cpp:1256-1259): A[0] a2 + B[0] b2 +
+      // A[L-1] a1 + B[L-1] b1, whose four products are +1 where the quad's bit (a1, b1, a2,
+      // b2 as bits 3..0) matches e4's and -1 where not
       if (P.early && d > 0) {
-        const uint64_t qa = (a2 > 0 ? 1ULL : 0ULL) | (a1 > 0 ? (1ULL << (L - 1)) : 0ULL);
-        const uint64_t qb = (b2 > 0 ? 1ULL : 0ULL) | (b1 > 0 ? (1ULL << (L - 1)) : 0ULL);
-        const int lhs = 4 - 2 * (__popcll((u.A ^ qa) & ends) + __popcll((u.B ^ qb) & ends));
+        const int lhs = 4 - 2 * __popc((e4 ^ q) & 15u);
         if (lhs != __shfl_sync(FULL_MASK, my_res, d)) {
           if (lane == d) my_ctrl = (c0 & ~15u) | (uint32_t)(k + 1);
           continue;
@@ -429,11 +432,12 @@ __global__ void __launch_bounds__(32 * AB_WARPS, MINB) ab_kernel(AbParams P) {
       const uint64_t pb2 = pair_bits(d, L);
       place2(u, 1ULL << d, 1ULL << (L - 1 - d), a1, b1, a2, b2);
       const int rem = L - 2 * (d + 1);
-      const int sumA = 2 * __popcll(u.A) - __popcll(u.Pm), sumB = 2 * __popcll(u.B) - __popcll(u.Pm);
+      // 2 (d + 1) positions are placed: sum = 2 #(+1) - 2 (d + 1)
+      const int sumA = 2 * (__popcll(u.A) - d - 1), sumB = 2 * (__popcll(u.B) - d - 1);
       bool prune = !(((absi(P.absA - sumA) <= rem) || (absi(-P.absA - sumA) <= rem)) &&
                      ((absi(P.absB - sumB) <= rem) || (absi(-P.absB - sumB) <= rem)));
       if (!prune) {
-        corr(v, u, two);
+        corr(v, u, two && d <= L - 34);
         bool bad = (v.s0 && absi(v.t0 - v.D0) > v.K0) || (v.s1 && absi(v.t1 - v.D1) > v.K1);
         prune = __any_sync(FULL_MASK, bad);
       }
@@ -511,6 +515,8 @@ __global__ void __launch_bounds__(32 * AB_WARPS, MINB) ab_kernel(AbParams P) {
       const int nd = d + 1;
       unsigned om = 0xFFu;
       int r_e = 0;
+      if (nd == 1)
+        e4 = (uint32_t)(((u.A >> (L - 1)) & 1) << 3 | ((u.B >> (L - 1)) & 1) << 2 | (u.A & 1) << 1 | (u.B & 1));
       if (nd < half) {
         r_e = resid_at(v, L - 1 - nd);
         if (P.outer_k) {
