@@ -121,11 +121,12 @@ __device__ __forceinline__ int resid_at(const Lanes &v, int s) {
   return __shfl_sync(FULL_MASK, mine, (s - 1) & 31);
 }
 
-// place the quad (a1, b1) at the position of bit b1m and (a2, b2) at that of b2m
-__device__ __forceinline__ void place2(Uni &u, uint64_t b1m, uint64_t b2m, int a1, int b1, int a2, int b2) {
+// place the quad q (sign bits: 3 = A at b1m's position, 2 = B there, 1 = A at b2m's, 0 = B
+// there; a set bit is +1)
+__device__ __forceinline__ void place2(Uni &u, uint64_t b1m, uint64_t b2m, uint32_t q) {
   u.Pm |= b1m | b2m;
-  u.A |= (a1 > 0 ? b1m : 0ULL) | (a2 > 0 ? b2m : 0ULL);
-  u.B |= (b1 > 0 ? b1m : 0ULL) | (b2 > 0 ? b2m : 0ULL);
+  u.A |= ((q & 8) ? b1m : 0ULL) | ((q & 2) ? b2m : 0ULL);
+  u.B |= ((q & 4) ? b1m : 0ULL) | ((q & 1) ? b2m : 0ULL);
 }
 __device__ __forceinline__ void clear_bits(Uni &u, uint64_t bits) {
   u.Pm &= ~bits;
@@ -280,10 +281,11 @@ __global__ void __launch_bounds__(32 * AB_WARPS, MINB) ab_kernel(AbParams P) {
   __shared__ int s_lo[AB_WARPS][AB_MAXLV];         // the level's row bitset: nonzero words
   __shared__ int s_hi[AB_WARPS][AB_MAXLV];         // lie in [lo, hi)
   int *wlo = s_lo[wib], *whi = s_hi[wib];
-  // Per-level control state, one level per lane (levels 0..half-1 <= 31): lane j holds
-  // level j's k | omask << 4 | ties << 12 and its early-check residual. A level's state is
-  // read with one shuffle from its lane and written by that lane alone (the values are
-  // warp-uniform), so no shared memory or warp barrier is involved.
+  // Per-level control state: k | omask << 4 | ties << 12 and the early-check residual. The
+  // current level's is held in registers (cur, cres, warp-uniform); the levels above it are
+  // saved one level per lane (levels 0..half-1 <= 31: lane j holds level j's), written by that
+  // lane when the search descends and read back with one shuffle when it returns, so no
+  // shared memory or warp barrier is involved.
   uint32_t my_ctrl = 0;
   int my_res = 0;
   uint64_t *lv = P.bits + (size_t)slot * (P.half + 1) * P.Wcap;
@@ -330,14 +332,12 @@ __global__ void __launch_bounds__(32 * AB_WARPS, MINB) ab_kernel(AbParams P) {
     u.A = u.B = u.Pm = 0;
     int opat = -1;   // outer_pat, taken when the search passes level outer_k
     uint32_t e4 = 0;  // early check: A[L-1], B[L-1], A[0], B[0] as bits 3..0 (set at level 1)
-    long long nodes = 0, cur = 0;
+    long long nodes = 0, spent = 0;  // nodes charged; the budget's count (fh_cur)
     bool aborted = false, found = false, abandoned = false;
     const long long t_start = clock64();
     int d = 0;
-    if (lane == 0) {
-      my_ctrl = 0u | (0xFFu << 4) | (5u << 12);  // ties: a_tied = b_tied = 1
-      my_res = 0;
-    }
+    uint32_t cur = 0u | (0xFFu << 4) | (5u << 12);  // level 0; ties: a_tied = b_tied = 1
+    int cres = 0;
     if (lane == 0) {
       wlo[0] = 0;
       whi[0] = cd.W;
@@ -377,8 +377,8 @@ __global__ void __launch_bounds__(32 * AB_WARPS, MINB) ab_kernel(AbParams P) {
         if (L & 1) {
           const uint64_t mb = 1ULL << half;
           for (int km = 0; km < 4 && !found; km++) {
-            const int av = (km < 2) ? 1 : -1, bv = (km & 1) ? -1 : 1;
-            place2(u, mb, 0ULL, av, bv, -1, -1);
+            // (A, B) of the middle: (+,+), (+,-), (-,+), (-,-)
+            place2(u, mb, 0ULL, (km < 2 ? 8u : 0u) | ((km & 1) ? 0u : 4u));
             corr(v, u, false);  // the middle pairs at shifts up to L - 1 - half < 33 only
             nodes++;
             if (final_ok()) found = true;
@@ -388,34 +388,32 @@ __global__ void __launch_bounds__(32 * AB_WARPS, MINB) ab_kernel(AbParams P) {
           found = true;
         }
         if (found) break;
-        // back to the parent level
+        // back to the parent level: its saved state, with the next quad
         d--;
-        {
-          uint32_t c0 = __shfl_sync(FULL_MASK, my_ctrl, d);
-          clear_bits(u, pair_bits(d, L));
-          if (lane == d) my_ctrl = (c0 & ~15u) | (uint32_t)((c0 & 15) + 1);
-        }
+        cur = __shfl_sync(FULL_MASK, my_ctrl, d);
+        cres = __shfl_sync(FULL_MASK, my_res, d);
+        clear_bits(u, pair_bits(d, L));
+        cur = (cur & ~15u) | ((cur & 15) + 1);
         continue;
       }
-      const uint32_t c0 = __shfl_sync(FULL_MASK, my_ctrl, d);
+      const uint32_t c0 = cur;
       const unsigned omask = (c0 >> 4) & 0xFF;
       const uint32_t ties = (c0 >> 12) & 15;
       int k = next_q(d, c0 & 15, omask, ties);
       if (k == 8) {
         if (d == 0) break;  // clean exhaustion
         d--;
-        uint32_t cp = __shfl_sync(FULL_MASK, my_ctrl, d);
+        cur = __shfl_sync(FULL_MASK, my_ctrl, d);
+        cres = __shfl_sync(FULL_MASK, my_res, d);
         clear_bits(u, pair_bits(d, L));
-        if (lane == d) my_ctrl = (cp & ~15u) | (uint32_t)((cp & 15) + 1);
+        cur = (cur & ~15u) | ((cur & 15) + 1);
         continue;
       }
-      const uint32_t q = quad_bits(d, k);
-      const int a1 = (q & 8) ? 1 : -1, b1 = (q & 4) ? 1 : -1, a2 = (q & 2) ? 1 : -1, b2 = (q & 1) ? 1 : -1;
+      const uint32_t q = quad_bits(d, k);  // a1, b1, a2, b2 as bits 3..0 (set: +1)
       const uint32_t nties = s_ntie[d == 0 ? 16 : ties][k];
       // charge the node before placing (wz_match.cpp:1243-1248)
       nodes++;
-      if (P.budget > 0 && ++cur > P.budget) {
-        if (lane == d) my_ctrl = (c0 & ~15u) | (uint32_t)k;
+      if (P.budget > 0 && ++spent > P.budget) {
         aborted = true;
         break;
       }
@@ -424,13 +422,13 @@ __global__ void __launch_bounds__(32 * AB_WARPS, MINB) ab_kernel(AbParams P) {
       // b2 as bits 3..0) matches e4's and -1 where not
       if (P.early && d > 0) {
         const int lhs = 4 - 2 * __popc((e4 ^ q) & 15u);
-        if (lhs != __shfl_sync(FULL_MASK, my_res, d)) {
-          if (lane == d) my_ctrl = (c0 & ~15u) | (uint32_t)(k + 1);
+        if (lhs != cres) {
+          cur = (c0 & ~15u) | (uint32_t)(k + 1);
           continue;
         }
       }
-      const uint64_t pb2 = pair_bits(d, L);
-      place2(u, 1ULL << d, 1ULL << (L - 1 - d), a1, b1, a2, b2);
+      const uint64_t pbits = pair_bits(d, L);
+      place2(u, 1ULL << d, 1ULL << (L - 1 - d), q);
       const int rem = L - 2 * (d + 1);
       // 2 (d + 1) positions are placed: sum = 2 #(+1) - 2 (d + 1)
       const int sumA = 2 * (__popcll(u.A) - d - 1), sumB = 2 * (__popcll(u.B) - d - 1);
@@ -444,32 +442,46 @@ __global__ void __launch_bounds__(32 * AB_WARPS, MINB) ab_kernel(AbParams P) {
       if (!prune && rows) {
         // fh_abp_filter(d): the level-(d+1) list from the level-d list (all rows at d = 0)
         const int c1 = s_cls[d], c2 = s_cls[L - 1 - d];
-        const uint64_t m1 = s_cm[c1], m2 = s_cm[c2];
-        const int r1 = s_tic[c1] - __popcll(u.Pm & m1), pa1 = ssum(u.A, u.Pm, m1), pb1 = ssum(u.B, u.Pm, m1);
-        const int r2 = s_tic[c2] - __popcll(u.Pm & m2), pa2 = ssum(u.A, u.Pm, m2), pb2 = ssum(u.B, u.Pm, m2);
         const uint64_t *src = lv + (size_t)d * P.Wcap;
         uint64_t *dst = lv + (size_t)(d + 1) * P.Wcap;
         const int lo = wlo[d], hi = whi[d];
         int nlo, nhi;
-        if (!P.a2 && hi - lo <= 4) {
-          // up to four words: lane 8i + j loads mask j (class c1 for j < 4, c2 for j >= 4;
-          // kind j & 3) of word lo + i, and three butterfly steps AND the eight together
-          const int j = lane & 7, w = lo + (lane >> 3), kind = j & 3;
-          const int c = j < 4 ? c1 : c2, r = j < 4 ? r1 : r2;
-          const int pv = (kind < 2) ? (j < 4 ? pa1 : pa2) : (j < 4 ? pb1 : pb2);
-          const bool live = w < hi;
-          uint64_t x = live ? mask_of(P, cd, c, kind, (kind & 1) ? pv + r : pv - r)[w] : ~0ULL;
-          x &= __shfl_xor_sync(FULL_MASK, x, 1);
-          x &= __shfl_xor_sync(FULL_MASK, x, 2);
-          x &= __shfl_xor_sync(FULL_MASK, x, 4);
-          if (j == 0 && live) {
-            x &= d == 0 ? all_rows(w, cd.nrows) : src[w];
-            dst[w] = x;
+        if (!P.a2 && hi - lo <= 24) {
+          // Narrow lists (the deep levels, where the nodes are): lane 8i + j loads mask j
+          // (class c1 for j < 4, c2 for j >= 4; kind j & 3: bounds on k_c = sum A or r_c =
+          // sum B over the class) of word base + i, four words per pass, and three butterfly
+          // steps AND the eight together. Each lane forms the one bound it needs: the class's
+          // placed sum pv and what its free positions can add, r.
+          const int j = lane & 7, kind = j & 3;
+          const int c = j < 4 ? c1 : c2;
+          const uint64_t mc = s_cm[c];
+          const int placed = __popcll(u.Pm & mc);
+          const int pv = 2 * __popcll((kind < 2 ? u.A : u.B) & mc) - placed;
+          const int r = s_tic[c] - placed;
+          const uint64_t *mk = mask_of(P, cd, c, kind, (kind & 1) ? pv + r : pv - r);
+          nlo = 1 << 30;
+          nhi = -1;
+          for (int base = lo; base < hi; base += 4) {
+            const int w = base + (lane >> 3);
+            const bool live = w < hi;
+            uint64_t x = live ? mk[w] : ~0ULL;
+            x &= __shfl_xor_sync(FULL_MASK, x, 1);
+            x &= __shfl_xor_sync(FULL_MASK, x, 2);
+            x &= __shfl_xor_sync(FULL_MASK, x, 4);
+            if (j == 0 && live) {
+              x &= d == 0 ? all_rows(w, cd.nrows) : src[w];
+              dst[w] = x;
+            }
+            const unsigned ball = __ballot_sync(FULL_MASK, j == 0 && live && x != 0);
+            if (ball) {
+              if (nhi < 0) nlo = base + ((__ffs(ball) - 1) >> 3);
+              nhi = base + ((31 - __clz(ball)) >> 3);
+            }
           }
-          const unsigned ball = __ballot_sync(FULL_MASK, j == 0 && live && x != 0);
-          nlo = ball ? lo + ((__ffs(ball) - 1) >> 3) : 1 << 30;
-          nhi = ball ? lo + ((31 - __clz(ball)) >> 3) : -1;
         } else {
+          const uint64_t m1 = s_cm[c1], m2 = s_cm[c2];
+          const int r1 = s_tic[c1] - __popcll(u.Pm & m1), pa1 = ssum(u.A, u.Pm, m1), pb1 = ssum(u.B, u.Pm, m1);
+          const int r2 = s_tic[c2] - __popcll(u.Pm & m2), pa2 = ssum(u.A, u.Pm, m2), pb2 = ssum(u.B, u.Pm, m2);
           const uint64_t *k1a = mask_of(P, cd, c1, 0, pa1 - r1), *k1b = mask_of(P, cd, c1, 1, pa1 + r1);
           const uint64_t *q1a = mask_of(P, cd, c1, 2, pb1 - r1), *q1b = mask_of(P, cd, c1, 3, pb1 + r1);
           const uint64_t *k2a = mask_of(P, cd, c2, 0, pa2 - r2), *k2b = mask_of(P, cd, c2, 1, pa2 + r2);
@@ -506,12 +518,11 @@ __global__ void __launch_bounds__(32 * AB_WARPS, MINB) ab_kernel(AbParams P) {
         prune = nhi < 0;
       }
       if (prune) {
-        clear_bits(u, pb2);
-        if (lane == d) my_ctrl = (c0 & ~15u) | (uint32_t)(k + 1);
+        clear_bits(u, pbits);
+        cur = (c0 & ~15u) | (uint32_t)(k + 1);
         continue;
       }
       // descend: the child level's entry work (its outer mask may end it immediately)
-      if (lane == d) my_ctrl = (c0 & ~15u) | (uint32_t)k;
       const int nd = d + 1;
       unsigned om = 0xFFu;
       int r_e = 0;
@@ -525,14 +536,16 @@ __global__ void __launch_bounds__(32 * AB_WARPS, MINB) ab_kernel(AbParams P) {
         }
       }
       if (om == 0u) {  // fh_ab_search(d+1) returns false at once: undo and try the next quad
-        clear_bits(u, pb2);
-        if (lane == d) my_ctrl = (c0 & ~15u) | (uint32_t)(k + 1);
+        clear_bits(u, pbits);
+        cur = (c0 & ~15u) | (uint32_t)(k + 1);
         continue;
       }
-      if (lane == nd) {
-        my_ctrl = 0u | (om << 4) | (nties << 12);
-        my_res = r_e;
+      if (lane == d) {  // save this level (at the quad taken) for the way back
+        my_ctrl = (c0 & ~15u) | (uint32_t)k;
+        my_res = cres;
       }
+      cur = 0u | (om << 4) | (nties << 12);
+      cres = r_e;
       d = nd;
     }
     if (aborted) {

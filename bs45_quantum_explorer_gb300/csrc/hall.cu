@@ -119,11 +119,12 @@ __global__ void __launch_bounds__(256) hall_fp64_recheck_kernel(
     const unsigned long long *list_len, unsigned long long list_cap, int L, double lim,
     const double *__restrict__ gc, const double *__restrict__ gs, uint8_t *__restrict__ pass,
     unsigned long long *pass_count) {
+  const unsigned long long n = *list_len;
+  const long long count = (long long)(n < list_cap ? n : list_cap);
+  if (count == 0) return;  // an empty band (the common case): no table to load
   extern __shared__ double tabs[];
   double *sc = tabs, *ss = tabs + 200 * L;
   load_tables64(sc, ss, gc, gs, L);
-  const unsigned long long n = *list_len;
-  const long long count = (long long)(n < list_cap ? n : list_cap);
   const int lane = threadIdx.x & 31;
   const long long w0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
@@ -153,46 +154,65 @@ __global__ void __launch_bounds__(256) hall_fix_band_kernel(
     const int64_t *__restrict__ tab, double pass_below, double reject_above,
     uint8_t *__restrict__ pass, unsigned long long *pass_count, unsigned *__restrict__ list2,
     unsigned long long *list2_len, unsigned long long list2_cap) {
-  extern __shared__ int64_t ftab[];
-  const int nt = 2 * BS_TC_NANG * L + 2 * BS_TC_NANG;
-  for (int i = threadIdx.x; i < nt; i += blockDim.x) {
-    // the device table is laid out for its length L: [cos][sin][sums]
-    ftab[i] = tab[i];
-  }
-  __syncthreads();
-  const int64_t *tc = ftab, *ts = ftab + BS_TC_NANG * L;
-  const int64_t *sc = ftab + 2 * BS_TC_NANG * L, *ss = sc + BS_TC_NANG;
   const unsigned long long n = *list_len;
   const long long count = (long long)(n < list_cap ? n : list_cap);
+  if (count == 0) return;
+  // The table in shared memory transposed to [position][angle] (cos rows, then sin rows), so
+  // that the lanes' reads at one position are consecutive words; then the row sums.
+  extern __shared__ int64_t ftab[];
+  int64_t *tc = ftab, *ts = ftab + BS_TC_NANG * L;
+  int64_t *sc = ftab + 2 * BS_TC_NANG * L, *ss = sc + BS_TC_NANG;
+  for (int k = threadIdx.x; k < BS_TC_NANG * L; k += blockDim.x) {
+    const int u = k / L, i = k - u * L;  // the device table is [angle][position]
+    tc[i * BS_TC_NANG + u] = tab[k];
+    ts[i * BS_TC_NANG + u] = tab[BS_TC_NANG * L + k];
+  }
+  for (int k = threadIdx.x; k < 2 * BS_TC_NANG; k += blockDim.x) sc[k] = tab[2 * BS_TC_NANG * L + k];
+  __syncthreads();
   const int lane = threadIdx.x & 31;
   const long long w0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+  constexpr int R = (BS_TC_NANG + 31) / 32;  // angles per lane: u = lane + 32 r
   unsigned local = 0;
   for (long long t = w0; t < count; t += nw) {
     const long long p = (long long)list[t];
     const uint64_t x = bits[2 * p], y = bits[2 * p + 1];
+    // one walk over each sequence's +1 positions feeds the lane's R angles at once
+    int64_t rx[R], ix[R], ry[R], iy[R];
+#pragma unroll
+    for (int r = 0; r < R; r++) rx[r] = ix[r] = ry[r] = iy[r] = 0;
+    for (uint64_t b = x; b; b &= b - 1) {
+      const int i = __ffsll((long long)b) - 1;
+      const int64_t *cr = tc + i * BS_TC_NANG + lane, *sr = ts + i * BS_TC_NANG + lane;
+#pragma unroll
+      for (int r = 0; r < R; r++)
+        if (lane + 32 * r < BS_TC_NANG) {
+          rx[r] += cr[32 * r];
+          ix[r] += sr[32 * r];
+        }
+    }
+    for (uint64_t b = y; b; b &= b - 1) {
+      const int i = __ffsll((long long)b) - 1;
+      const int64_t *cr = tc + i * BS_TC_NANG + lane, *sr = ts + i * BS_TC_NANG + lane;
+#pragma unroll
+      for (int r = 0; r < R; r++)
+        if (lane + 32 * r < BS_TC_NANG) {
+          ry[r] += cr[32 * r];
+          iy[r] += sr[32 * r];
+        }
+    }
     double mx = 0.0;
-    for (int u = lane; u < BS_TC_NANG; u += 32) {
-      const int64_t *cr = tc + u * L, *sr = ts + u * L;
-      int64_t rx = 0, ix = 0, ry = 0, iy = 0;
-      for (uint64_t b = x; b; b &= b - 1) {
-        const int i = __ffsll((long long)b) - 1;
-        rx += cr[i];
-        ix += sr[i];
+#pragma unroll
+    for (int r = 0; r < R; r++) {
+      const int u = lane + 32 * r;
+      if (u < BS_TC_NANG) {
+        const int64_t a0 = 2 * rx[r] - sc[u], b0 = 2 * ix[r] - ss[u];
+        const int64_t c0 = 2 * ry[r] - sc[u], d0 = 2 * iy[r] - ss[u];
+        const double a = (double)a0, b2 = (double)b0, c = (double)c0, d = (double)d0;
+        const double f = __dadd_rn(__dadd_rn(__dmul_rn(a, a), __dmul_rn(b2, b2)),
+                                   __dadd_rn(__dmul_rn(c, c), __dmul_rn(d, d))) * 0x1p-60;
+        mx = fmax(mx, f);
       }
-      for (uint64_t b = y; b; b &= b - 1) {
-        const int i = __ffsll((long long)b) - 1;
-        ry += cr[i];
-        iy += sr[i];
-      }
-      rx = 2 * rx - sc[u];
-      ix = 2 * ix - ss[u];
-      ry = 2 * ry - sc[u];
-      iy = 2 * iy - ss[u];
-      const double a = (double)rx, b2 = (double)ix, c = (double)ry, d = (double)iy;
-      const double f = __dadd_rn(__dadd_rn(__dmul_rn(a, a), __dmul_rn(b2, b2)),
-                                 __dadd_rn(__dmul_rn(c, c), __dmul_rn(d, d))) * 0x1p-60;
-      mx = fmax(mx, f);
     }
     for (int o = 16; o; o >>= 1) mx = fmax(mx, __shfl_xor_sync(FULL_MASK, mx, o));
     if (lane == 0) {
@@ -689,22 +709,32 @@ __global__ void __launch_bounds__(TC_THREADS, 1) hall_tc_kernel(TcParams P) {
 constexpr int SC_BUFS = 4;
 constexpr int SC_RUN = 256;  // survivors a screen epilogue warp holds before it writes them out
 constexpr int SC_RING = 4;   // tiles of packed words each screen producer has in flight
+// Warp roles of the screen: SC_PRODUCERS producer warps (the expansion of packed words to
+// operand rows is most of the kernel's instructions, so it is spread over the SM
+// sub-partitions), one MMA warp, and SC_GROUPS epilogue groups of four warps. With more than
+// two groups a warp reads its pair's 128 values in two halves of 64 to fit the register budget.
+constexpr int SC_PRODUCERS = 2;
+constexpr int SC_MMA_WARP = SC_PRODUCERS;
+constexpr int SC_GROUPS = 2;
+constexpr bool SC_HALVES = SC_GROUPS > 2;
+constexpr int SC_EPI = 4 * SC_GROUPS;  // epilogue warps
+constexpr int SC_THREADS = 32 * (SC_PRODUCERS + 1 + SC_EPI);
 constexpr int SC_RAW_BYTES = TC_TILE * 16;  // one tile of pairs: two 8-byte words each
 constexpr uint32_t SC_COLS = 128;  // TMEM columns per buffer (C then D, 64 each)
 
-__global__ void __launch_bounds__(TC_THREADS, 1) hall_screen_kernel(TcParams P) {
+__global__ void __launch_bounds__(SC_THREADS, 1) hall_screen_kernel(TcParams P) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t *base = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   uint8_t *sA = base;
   uint8_t *sB = sA + TC_STAGES * A_STAGE_BYTES;  // rows 0..63 of each part, 8 KB per part
-  uint8_t *sraw = sB + P.nparts * 64 * 128;      // [TC_PRODUCERS][SC_RING] tiles of packed words
-  uint32_t *srun = (uint32_t *)(sraw + TC_PRODUCERS * SC_RING * SC_RAW_BYTES);  // [8][SC_RUN]
-  uint64_t *bars = (uint64_t *)(srun + 8 * SC_RUN);
-  uint32_t *tmem_slot = (uint32_t *)(bars + 2 * TC_STAGES + 2 * SC_BUFS + TC_PRODUCERS * SC_RING);
+  uint8_t *sraw = sB + P.nparts * 64 * 128;      // [SC_PRODUCERS][SC_RING] tiles of packed words
+  uint32_t *srun = (uint32_t *)(sraw + SC_PRODUCERS * SC_RING * SC_RAW_BYTES);  // [SC_EPI][SC_RUN]
+  uint64_t *bars = (uint64_t *)(srun + SC_EPI * SC_RUN);
+  uint32_t *tmem_slot = (uint32_t *)(bars + 2 * TC_STAGES + 2 * SC_BUFS + SC_PRODUCERS * SC_RING);
   volatile int *abort_flag = (volatile int *)(tmem_slot + 1);
   const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + TC_STAGES);
   const uint32_t tfull0 = smem_u32(bars + 2 * TC_STAGES), tempty0 = tfull0 + 8 * SC_BUFS;
-  const uint32_t raw0 = tempty0 + 8 * SC_BUFS;  // [TC_PRODUCERS][SC_RING]: a ring tile landed
+  const uint32_t raw0 = tempty0 + 8 * SC_BUFS;  // [SC_PRODUCERS][SC_RING]: a ring tile landed
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const long long G = gridDim.x;
 
@@ -712,7 +742,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) hall_screen_kernel(TcParams P) 
     for (int p = 0; p < P.nparts; p++) {
       const uint4 *src = (const uint4 *)(P.image + (size_t)p * BS_TC_PART_BYTES);
       uint4 *dst = (uint4 *)(sB + p * 64 * 128);
-      for (int i = threadIdx.x; i < 64 * 128 / 16; i += TC_THREADS) dst[i] = src[i];
+      for (int i = threadIdx.x; i < 64 * 128 / 16; i += SC_THREADS) dst[i] = src[i];
     }
   }
   if (threadIdx.x == 0) {
@@ -724,21 +754,21 @@ __global__ void __launch_bounds__(TC_THREADS, 1) hall_screen_kernel(TcParams P) 
       mbar_init(tfull0 + 8 * b, 1);
       mbar_init(tempty0 + 8 * b, 4);  // the four warps of the group that reads the buffer
     }
-    for (int r = 0; r < TC_PRODUCERS * SC_RING; r++) mbar_init(raw0 + 8 * r, 1);
+    for (int r = 0; r < SC_PRODUCERS * SC_RING; r++) mbar_init(raw0 + 8 * r, 1);
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  if (warp == TC_MMA_WARP) tc_alloc(smem_u32(tmem_slot), TMEM_COLS);
+  if (warp == SC_MMA_WARP) tc_alloc(smem_u32(tmem_slot), TMEM_COLS);
   fence_async_smem();
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
 
-  if (warp < TC_PRODUCERS) {
+  if (warp < SC_PRODUCERS) {
     const uint32_t neg2 = P.one2 | 0x80008000u;
     const int nchunks = 2 * P.ksteps;
-    const long long stride = (long long)TC_PRODUCERS * G;  // between this warp's tiles
+    const long long stride = (long long)SC_PRODUCERS * G;  // between this warp's tiles
     int it = warp;
     long long tile = blockIdx.x + (long long)it * G;
     auto expand = [&](const uint4 *wv, int st) {
@@ -799,7 +829,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) hall_screen_kernel(TcParams P) 
         }
         expand(wv, st);
         tile += stride;
-        it += TC_PRODUCERS;
+        it += SC_PRODUCERS;
       }
       // after an abort: wait (bounded) for the copies still landing in the ring before the
       // block exits
@@ -826,10 +856,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1) hall_screen_kernel(TcParams P) 
 #pragma unroll
         for (int rr = 0; rr < 4; rr++) wv[rr] = nw[rr];
         tile = next;
-        it += TC_PRODUCERS;
+        it += SC_PRODUCERS;
       }
     }
-  } else if (warp == TC_MMA_WARP) {
+  } else if (warp == SC_MMA_WARP) {
     if (lane == 0) {
       const uint32_t a_base = smem_u32(sA), b_base = smem_u32(sB);
       int it = 0, last = -1;
@@ -859,14 +889,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1) hall_screen_kernel(TcParams P) 
     }
     __syncwarp();
   } else {
-    // ---- epilogue: group g reads the tiles it = g, g + 2, ... (buffer it % 4) ----
-    const int g = (warp - TC_MMA_WARP - 1) >> 2;
+    // ---- epilogue: group g reads the tiles it = g, g + SC_GROUPS, ... (buffer it % 4) ----
+    const int g = (warp - SC_MMA_WARP - 1) >> 2;
     const int q = warp & 3;
     const uint32_t lane_off = (uint32_t)(q * 32) << 16;
     const int row = q * 32 + lane;
     // Survivors collect in the warp's own shared-memory run and go to the list in batches,
     // one global atomic per batch, so no tile waits for an atomic's round trip.
-    uint32_t *run = srun + (warp - TC_MMA_WARP - 1) * SC_RUN;
+    uint32_t *run = srun + (warp - SC_MMA_WARP - 1) * SC_RUN;
     int nrun = 0;
     auto flush = [&]() {
       __syncwarp();
@@ -882,7 +912,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) hall_screen_kernel(TcParams P) 
       __syncwarp();
       nrun = 0;
     };
-    for (int it = g;; it += 2) {
+    for (int it = g;; it += SC_GROUPS) {
       const long long tile = blockIdx.x + (long long)it * G;
       if (tile >= P.ntiles) break;
       const int b = it % SC_BUFS;
@@ -893,17 +923,36 @@ __global__ void __launch_bounds__(TC_THREADS, 1) hall_screen_kernel(TcParams P) 
       }
       tc_fence_after();
       const uint32_t t0 = tmem + lane_off + b * SC_COLS;
-      float v[128];  // Re C, Im C, Re D, Im D at the 32 screening angles
-      tmem_ld_32x4(t0, t0 + 32, t0 + 64, t0 + 96, v);
-      tc_fence_before();
-      __syncwarp();
-      if (lane == 0) mbar_arrive(tempty0 + 8 * b);
       float mx = 0.0f;
+      if (SC_HALVES) {
 #pragma unroll
-      for (int k = 0; k < 32; k += 2) {
-        float f0, f1;
-        pair_psd2(v + k, v + 32 + k, v + 64 + k, v + 96 + k, f0, f1);
-        mx = fmax3(mx, f0, f1);
+        for (int h = 0; h < 2; h++) {
+          float v[64];  // Re C, Im C, Re D, Im D at screening angles 16h .. 16h + 15
+          tmem_ld_16x4(t0 + 16 * h, t0 + 32 + 16 * h, t0 + 64 + 16 * h, t0 + 96 + 16 * h, v);
+          if (h == 1) {
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(tempty0 + 8 * b);
+          }
+#pragma unroll
+          for (int k = 0; k < 16; k += 2) {
+            float f0, f1;
+            pair_psd2(v + k, v + 16 + k, v + 32 + k, v + 48 + k, f0, f1);
+            mx = fmax3(mx, f0, f1);
+          }
+        }
+      } else {
+        float v[128];  // Re C, Im C, Re D, Im D at the 32 screening angles
+        tmem_ld_32x4(t0, t0 + 32, t0 + 64, t0 + 96, v);
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(tempty0 + 8 * b);
+#pragma unroll
+        for (int k = 0; k < 32; k += 2) {
+          float f0, f1;
+          pair_psd2(v + k, v + 32 + k, v + 64 + k, v + 96 + k, f0, f1);
+          mx = fmax3(mx, f0, f1);
+        }
       }
       const long long pair = tile * TC_TILE + row;
       const bool mine = pair < P.npairs;
@@ -920,13 +969,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1) hall_screen_kernel(TcParams P) 
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
-  if (warp == TC_MMA_WARP) tc_dealloc(tmem, TMEM_COLS);
+  if (warp == SC_MMA_WARP) tc_dealloc(tmem, TMEM_COLS);
 }
 
 size_t screen_smem_bytes(int nparts) {
   return 1024 + (size_t)TC_STAGES * A_STAGE_BYTES + (size_t)nparts * 64 * 128 +
-         (size_t)TC_PRODUCERS * SC_RING * SC_RAW_BYTES + sizeof(uint32_t) * 8 * SC_RUN +
-         (2 * TC_STAGES + 2 * SC_BUFS + TC_PRODUCERS * SC_RING) * 8 + 16;
+         (size_t)SC_PRODUCERS * SC_RING * SC_RAW_BYTES + sizeof(uint32_t) * SC_EPI * SC_RUN +
+         (2 * TC_STAGES + 2 * SC_BUFS + SC_PRODUCERS * SC_RING) * 8 + 16;
 }
 
 size_t tc_smem_bytes(int nparts) {
@@ -1038,7 +1087,7 @@ static int launch_tc(bs_ctx *ctx, int mode, const uint64_t *d_bits, long long np
   if (!d_dump) {
     P.scr = ctx->d_scr;
     P.scr_cap = (unsigned long long)ctx->scr_cap;
-    hall_screen_kernel<<<(int)grid, TC_THREADS, screen_smem_bytes(F.nparts), ctx->stream>>>(P);
+    hall_screen_kernel<<<(int)grid, SC_THREADS, screen_smem_bytes(F.nparts), ctx->stream>>>(P);
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) { bs_timed_end(ctx); return bs_cuda_fail(e); }
     ctx->launches++;
@@ -1338,7 +1387,7 @@ extern "C" int bs_hall_filter_noalloc(int n, const uint64_t *d_bits, long long n
     // the screen, then the full test over its survivors (as bs_hall_filter_dev does)
     P.scr = (unsigned *)(S.scratch + NA_SCR_OFF);
     P.scr_cap = (unsigned long long)NOALLOC_MAX_PAIRS;
-    hall_screen_kernel<<<(int)grid, TC_THREADS, screen_smem_bytes(1), s>>>(P);
+    hall_screen_kernel<<<(int)grid, SC_THREADS, screen_smem_bytes(1), s>>>(P);
     CK(cudaGetLastError());
     P.list = P.scr;
     P.list_len = count + 4;

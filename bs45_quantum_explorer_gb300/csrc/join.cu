@@ -40,23 +40,36 @@ __global__ void npaf_kernel(const uint64_t *__restrict__ q, long long count, int
   }
 }
 
-// 64-bit key of an autocorrelation vector v[1..n] (|v[s]| <= 2n + 2 < 128): the values are
-// biased into bytes and packed eight to a word, and the words are folded with one
-// multiply-xorshift step each (a splitmix64-style finaliser spreads the result over the table).
-// Equal vectors give equal keys; the exact NPAF check after a key match rules collisions out.
+// Odd 64-bit multipliers of the key, one per shift (splitmix64 outputs, fixed).
+__constant__ uint64_t kKeyMul[64] = {
+    0x39E7EF6C1B54F617ULL, 0x29BB7C882170A7D7ULL, 0x45446DEFE0440477ULL, 0x9A0FC648C9C19C21ULL,
+    0xDB939B7D1D9E4ACFULL, 0x958796FCC2A073FDULL, 0x4F001AA287E5A101ULL, 0x19AD5ABED7952F1DULL,
+    0xB18BACE16B914A33ULL, 0x22CFCFEB9E985FBFULL, 0xDCC16F773BD10E33ULL, 0xE858FD9950CC3281ULL,
+    0xE082EAAA6D1427E9ULL, 0x9214C05752910273ULL, 0x12EB34A8184E5841ULL, 0x5E132981F11873DBULL,
+    0x1053A9814BC69167ULL, 0xA66BC82B20C5DCC5ULL, 0x1E5BCDFBD5B409E1ULL, 0xA80DF6AFAF6A81F5ULL,
+    0xB95F8C15A4FDD58BULL, 0x120146AB0808746DULL, 0xB004AF8618026361ULL, 0x254C98A925B77EE9ULL,
+    0x5BE0CC7CF6E85DA9ULL, 0xEADE1A126AC6190BULL, 0x34172784B4E05D37ULL, 0x1A4729CF3086F7F1ULL,
+    0x1A7FE47FE14700B3ULL, 0x57F470CD5207D86BULL, 0x3F7060EEF64F6BF7ULL, 0x47ED631F621F1B21ULL,
+    0x42946B3F061D3D05ULL, 0xB869F62456532C89ULL, 0x313D74B541ECD14FULL, 0xCC31EEA712C6DA7BULL,
+    0x9651FEC138130CF1ULL, 0x413DA377C06A6005ULL, 0x4D0ABC1748D12427ULL, 0xB571932ACCC61087ULL,
+    0x7B568766CB7755E3ULL, 0x574EFCA124FAEF0DULL, 0xA60EB03F3FBA60C7ULL, 0x9F27AA4A403F1B39ULL,
+    0xF829834DF712FB7BULL, 0xD823EA850CF4441BULL, 0x3C62A8E8AA8F6691ULL, 0x6EF181920695A531ULL,
+    0xC86C597ED57E94B9ULL, 0x09DB76C570325CE7ULL, 0x97D770D7BFC70C4FULL, 0xC4B9C52219209D7FULL,
+    0x245F3965340006EDULL, 0xA3351A49368E6ACFULL, 0x7755814858AE75F9ULL, 0x5FD53C5EDDF91E3BULL,
+    0x0BDAD738F57B5F1DULL, 0x9346372A11FB282FULL, 0xBFB1C8C156E4B5BBULL, 0xA57C8B14B20AB549ULL,
+    0x8F7753582ECC36E3ULL, 0x81C1BF1F8C532779ULL, 0xD3FD3EE04FB9C48DULL, 0x89444C017283BBFBULL,
+};
+
+// 64-bit key of an autocorrelation vector v[1..n]: the linear form sum_s v[s] * kKeyMul[s]
+// (mod 2^64), then a splitmix64-style finaliser to spread it over the table. One multiply-add
+// per shift. Equal vectors give equal keys; different vectors can share a key, and the exact
+// NPAF check after a key match rules those out.
 template <typename F>
 __device__ __forceinline__ uint64_t vec_key(F value, int n) {
-  uint64_t h = 0x9E3779B97F4A7C15ULL, w = 0;
-  int fill = 0;
-  for (int s = 1; s <= n; s++) {
-    w |= (uint64_t)(uint8_t)(value(s) + 128) << (8 * fill);
-    if (++fill == 8 || s == n) {
-      h = (h ^ w) * 0xBF58476D1CE4E5B9ULL;
-      h ^= h >> 31;
-      w = 0;
-      fill = 0;
-    }
-  }
+  uint64_t h = 0;
+  for (int s = 1; s <= n; s++) h += (uint64_t)(int64_t)value(s) * kKeyMul[s];
+  h ^= h >> 31;
+  h *= 0xBF58476D1CE4E5B9ULL;
   h ^= h >> 29;
   h *= 0x94D049BB133111EBULL;
   h ^= h >> 32;
