@@ -585,13 +585,17 @@ def run_join(n=24):
 
 def run_serving(n_jobs=12, tail=2, rate=2.0, slots=4, max_cells=4096, ref_seconds=0.0):
     """C5: a seeded Poisson stream of first-hit jobs, n uniform in 20..42 with a signature from
-    classes(n) and a contiguous ORDER=3 range of 1..max_cells raw cells (4,096: the workload's
-    stated range), plus `tail` n = 42 ranges; per-job budget 2^16, BUF_CAP 2000, DRAIN_TOP 64
-    (the per-cell work reduced from the production lane so that the mix ends in about a
-    minute). Lists are built before the clock starts, in parallel (a service keeps them).
-    Reports cells/s, nodes/s and p50/p99 job latency."""
+    classes(n) and a contiguous ORDER=3 range of 1..max_cells raw cells, plus `tail` n = 42
+    ranges; per-job budget 2^16, BUF_CAP 2000, DRAIN_TOP 64 (the per-cell work reduced from the
+    production lane). Lists are built before the clock starts, in parallel (a service keeps
+    them). Reports cells/s, nodes/s and p50/p99 job latency.
+
+    With ref_seconds > 0 the same jobs also run as the reference's own lane processes, all at
+    once on the host cores, stopped after ref_seconds; then our server runs exactly the raw
+    cells each reference process completed (all jobs submitted at once), so the two are timed
+    on the same work, and every job the reference finished is compared count for count."""
     import concurrent.futures as cf
-    from bs45_quantum_explorer_gb300.serve import Server, poisson_trace, serving_list
+    from bs45_quantum_explorer_gb300.serve import Job, Server, poisson_trace, serving_list
     plan = poisson_trace(nj=n_jobs, rate=rate, seed=SEED, n_range=(20, 42), max_cells=max_cells,
                          tail_n42=tail, classes=_classes, ncells_of=lambda n, sg: 1 << 30)
     t0 = time.perf_counter()
@@ -611,7 +615,24 @@ def run_serving(n_jobs=12, tail=2, rate=2.0, slots=4, max_cells=4096, ref_second
               "errors": sum(1 for j in out if j.error), "found": sum(1 for j in out if j.result and j.result.found),
               "peak_hbm_admitted_bytes": srv.peak_in_use})
     if ref_seconds > 0:
-        d["cpu_baseline"] = serving_reference(jobs, ref_seconds, out)
+        ref, per_job = serving_reference(jobs, ref_seconds, out)
+        d["cpu_baseline"] = ref
+        if per_job:
+            # the same work on our server: each job's cells the reference completed
+            same = [Job(jid=j.jid, n=j.n, sig=j.sig, skip=j.skip, end=j.end if fin else rpi,
+                        budget=j.budget, buf_cap=j.buf_cap, drain_top=j.drain_top,
+                        drain_batches=j.drain_batches, arrival=0.0)
+                    for j, (fin, rpi) in zip(jobs, per_job) if fin or (rpi is not None and rpi > j.skip)]
+            out2, st2 = Server(slots=slots).run_trace(same)
+            d["same_work"] = {
+                "jobs": len(same), "reference_cells_done": ref["cells_done"], "our_cells_done": st2.cells,
+                "reference_seconds": ref["seconds"], "reference_cores": ref["cores"],
+                "our_seconds": round(st2.makespan_s, 2),
+                "speedup": ref["seconds"] / st2.makespan_s if st2.makespan_s > 0 else None,
+                "errors": sum(1 for j in out2 if j.error),
+                "what": "the raw cells each reference lane process completed within its bound "
+                        "(its whole range when it finished), on our server with every job "
+                        "submitted at once, against the reference's wall time for them"}
     return d
 
 
@@ -619,15 +640,16 @@ def serving_reference(jobs, seconds, ours):
     """The same jobs through the reference's own lane binary (oracle/_ref/wz_match, the
     reference's wz_match.cpp compiled unmodified), one process per job as its SLURM lanes run
     them, all at once on the host cores, each stopped by SIGTERM after `seconds` (the
-    reference then prints its summary with lower-bound counts). Reports the jobs that
-    finished, their latency from their start, the cells done per second over the bound, and
-    for every finished job whether its summary counts equal ours."""
+    reference then prints its summary with the raw cell it would resume from). Returns (the
+    report: jobs that finished, their latency from their start, the cells done per second over
+    the bound, and for every finished job whether its summary counts equal ours; per job
+    (finished, resume_pi))."""
     import re
     import signal
     import subprocess
     exe = os.path.join(ROOT, "oracle", "_ref", "wz_match")
     if not os.path.exists(exe):
-        return {"unavailable": "oracle/_ref/wz_match was not built on this machine"}
+        return {"unavailable": "oracle/_ref/wz_match was not built on this machine"}, None
     base = {k: v for k, v in os.environ.items() if not k.startswith(("WZ_", "FH_"))}
     procs = []
     t0 = time.perf_counter()
@@ -650,10 +672,13 @@ def serving_reference(jobs, seconds, ours):
             p.send_signal(signal.SIGTERM)
     wall = time.perf_counter() - t0
     cells, same, done = 0, 0, 0
+    per_job = []
     for i, p in enumerate(procs):
         out, _ = p.communicate(timeout=600)
         m = re.search(r"cells_done=(\d+)", out)
         cells += int(m[1]) if m else 0
+        rp = re.search(r"resume_pi=(-?\d+)", out)
+        per_job.append((finish[i] is not None, int(rp[1]) if rp else None))
         if finish[i] is not None:
             done += 1
             r = ours[i].result
@@ -668,7 +693,7 @@ def serving_reference(jobs, seconds, ours):
                       f"unmodified), all started at once, stopped after {seconds:.0f} s",
             "jobs_finished": done, "cells_done": cells, "seconds": round(wall, 1),
             "finished_p50_s": float(np.percentile(lat, 50)) if lat else None,
-            "finished_jobs_equal_to_ours": same}
+            "finished_jobs_equal_to_ours": same}, per_job
 
 
 def main():
@@ -965,7 +990,9 @@ def main():
             line["search"]["cpu_baseline"] = cpu_search_rate(os.cpu_count() or 1, cell42)
         # ---- the n = 36 first-hit lane (bounded) and the serving mix ----
         line["first_hit"] = run_first_hit(args.fh_seconds, with_cpu=not args.no_cpu_baseline)
-        line["serving"] = run_serving(ref_seconds=0.0 if args.no_cpu_baseline else 45.0)
+        # ranges of 1..256 cells here so that the default run ends in minutes; `--serve`
+        # runs the stated 1..4096
+        line["serving"] = run_serving(max_cells=256, ref_seconds=0.0 if args.no_cpu_baseline else 45.0)
         line["completer_vs_reference_gpu_spike"] = run_spike()
         if not args.no_cpu_baseline:
             ncpu = os.cpu_count() or 1

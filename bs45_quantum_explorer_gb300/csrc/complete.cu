@@ -179,17 +179,25 @@ __device__ __forceinline__ int outer_pat(const AbParams &P, const Uni &u) {
   return pat;
 }
 
-// the mask at level d >= 1 from the pattern and the residuals at L-1-d-j (r0 at j = 0)
+// the mask at level d >= 1 from the pattern and the residuals at L-1-d-j (r0 at j = 0). A
+// residual must be even with |R_j| <= 4 (j + 1); then R_j / 2 is R_j >> 1.
 __device__ __forceinline__ unsigned outer_mask(const AbParams &P, int pat, const Lanes &v, int d, int r0) {
   const int k = P.outer_k, L = P.L;
   if (k < 2 || d < k || d + k > L / 2 || pat < 0) return 0xFFu;
-  int R[3];
-  R[0] = r0;
-  for (int j = 1; j < k; j++) R[j] = resid_at(v, L - 1 - d - j);
-  for (int j = 0; j < k; j++)
-    if ((R[j] & 1) || R[j] < -4 * (j + 1) || R[j] > 4 * (j + 1)) return 0u;
-  if (k == 2) return P.outer2[(pat * 5 + (R[0] / 2 + 2)) * 9 + (R[1] / 2 + 4)];
-  return P.outer3[((pat * 5 + (R[0] / 2 + 2)) * 9 + (R[1] / 2 + 4)) * 13 + (R[2] / 2 + 6)];
+  const int s1 = L - 2 - d;  // the shift of R_1
+  int r1, r2 = 0;
+  if (s1 <= 32) {  // every shift below 33: one slot (the common case)
+    const int mine = v.t0 - v.D0;
+    r1 = __shfl_sync(FULL_MASK, mine, s1 - 1);
+    if (k == 3) r2 = __shfl_sync(FULL_MASK, mine, s1 - 2);
+  } else {
+    r1 = resid_at(v, s1);
+    if (k == 3) r2 = resid_at(v, s1 - 1);
+  }
+  if ((r0 | r1 | r2) & 1) return 0u;
+  if ((unsigned)(r0 + 4) > 8u || (unsigned)(r1 + 8) > 16u || (unsigned)(r2 + 12) > 24u) return 0u;
+  if (k == 2) return P.outer2[pat * 45 + (r0 >> 1) * 9 + (r1 >> 1) + 22];
+  return P.outer3[pat * 585 + (r0 >> 1) * 117 + (r1 >> 1) * 13 + (r2 >> 1) + 292];
 }
 
 // The level filter of the allowed rows (fh_abp_filter, wz_match.cpp:1055-1075): a row
@@ -343,7 +351,7 @@ __global__ void __launch_bounds__(32 * AB_WARPS, MINB) ab_kernel(AbParams P) {
       whi[0] = cd.W;
     }
     __syncwarp();
-    unsigned long long steps = 0;
+    unsigned steps = 0;
     while (true) {
       if ((++steps & 1023) == 0) {
         bool stop = (long long)idx > *(volatile long long *)P.hit_min || *P.stop_flag ||
@@ -410,7 +418,6 @@ __global__ void __launch_bounds__(32 * AB_WARPS, MINB) ab_kernel(AbParams P) {
         continue;
       }
       const uint32_t q = quad_bits(d, k);  // a1, b1, a2, b2 as bits 3..0 (set: +1)
-      const uint32_t nties = s_ntie[d == 0 ? 16 : ties][k];
       // charge the node before placing (wz_match.cpp:1243-1248)
       nodes++;
       if (P.budget > 0 && ++spent > P.budget) {
@@ -544,7 +551,7 @@ __global__ void __launch_bounds__(32 * AB_WARPS, MINB) ab_kernel(AbParams P) {
         my_ctrl = (c0 & ~15u) | (uint32_t)k;
         my_res = cres;
       }
-      cur = 0u | (om << 4) | (nties << 12);
+      cur = 0u | (om << 4) | ((uint32_t)s_ntie[d == 0 ? 16 : ties][k] << 12);
       cres = r_e;
       d = nd;
     }
