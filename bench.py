@@ -613,7 +613,9 @@ def run_serving(n_jobs=12, tail=2, rate=2.0, slots=4, max_cells=4096, ref_second
                           f"{slots} slots; ranges of 1..{max_cells} raw cells; budget 2^16, BUF_CAP 2000, "
                           "DRAIN_TOP 64", "lists_prebuilt_s": round(list_s, 2),
               "errors": sum(1 for j in out if j.error), "found": sum(1 for j in out if j.result and j.result.found),
-              "peak_hbm_admitted_bytes": srv.peak_in_use})
+              "peak_hbm_admitted_bytes": srv.peak_in_use,
+              "peak_device_used_bytes": srv.peak_device_used,
+              "admissions_held_by_measured_memory": srv.waits_on_device_memory})
     if ref_seconds > 0:
         ref, per_job = serving_reference(jobs, ref_seconds, out)
         d["cpu_baseline"] = ref

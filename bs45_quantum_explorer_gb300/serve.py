@@ -6,11 +6,14 @@ contiguous raw cell range (lane.run_lane) and one server runs many of them on on
 
   - a fixed set of slots, each a host thread with its own GPU context: its own CUDA stream and
     device buffers (frontier and suspended DFS walks, leaf and survivor buffers, completer
-    stacks). A slot keeps its context across jobs and retargets it (bs_ctx_retarget), so no
-    job allocates device memory and the buffers stay resident;
-  - admission by HBM footprint: a job starts when a slot is free and its estimated device
-    footprint fits the budget beside the jobs already running; a job that arrives while
-    others run is admitted as soon as that holds (first fitting job in arrival order);
+    stacks). A slot keeps its context across jobs and retargets it (bs_ctx_retarget), so the
+    buffers stay resident and a job allocates only when it needs a buffer larger than any
+    job before it on that slot (the buffer then grows once);
+  - admission by HBM footprint: a job starts when a slot is free, its estimated device
+    footprint fits the budget beside the jobs already running, and that many bytes are free
+    on the device as the driver reports them (the estimate alone cannot see a buffer that
+    grows); a job that arrives while others run is admitted as soon as that holds (first
+    fitting job in arrival order);
   - jobs on different slots overlap on the device (different streams).
 A job's result does not depend on what runs beside it: the stream, the keep and the
 completions are deterministic per job, so its counts and its quad equal its run alone.
@@ -80,16 +83,28 @@ class ServeStats:
 
 
 class Server:
-    def __init__(self, slots=4, hbm_budget=None, device=0, lane_opts=None, runner=None):
+    def __init__(self, slots=4, hbm_budget=None, device=0, lane_opts=None, runner=None,
+                 mem_probe=None):
         """runner(slot_index, job) -> LaneResult replaces the GPU lane (host-side tests of
-        the admission and queueing logic); hbm_budget defaults to 80% of the free memory."""
-        if hbm_budget is None:
+        the admission and queueing logic); hbm_budget defaults to 80% of the free memory.
+
+        mem_probe() -> (free, total) device bytes as the driver reports them (by default
+        cudaMemGetInfo through torch; none with a runner unless given). Admission then also
+        needs the job's footprint free on the device: the footprint is an estimate, and a
+        slot's buffers grow when a job needs more than the slot has held, so the measured free
+        memory is checked as well. The largest measured use is reported (peak_device_used)."""
+        if mem_probe is None and runner is None:
             import torch
-            free, _ = torch.cuda.mem_get_info(device)
+            mem_probe = lambda: torch.cuda.mem_get_info(device)  # noqa: E731
+        self._mem_probe = mem_probe
+        if hbm_budget is None:
+            free, _ = mem_probe()
             hbm_budget = int(0.8 * free)
         self.hbm_budget = hbm_budget
         self._runner = runner
         self.peak_in_use = 0
+        self.peak_device_used = 0
+        self.waits_on_device_memory = 0  # admissions held back by the measured check
         if slots * SLOT_BASE_BYTES > self.hbm_budget:
             raise ValueError(f"{slots} slots need {slots * SLOT_BASE_BYTES} B, budget {self.hbm_budget} B")
         self.device = device
@@ -134,11 +149,23 @@ class Server:
             t.join()
 
     # ---- admission: first pending job, in arrival order, whose footprint fits ----
+    def _measured_free(self):
+        """Free device bytes now (None without a probe); records the peak measured use."""
+        if self._mem_probe is None:
+            return None
+        free, total = self._mem_probe()
+        self.peak_device_used = max(self.peak_device_used, total - free)
+        return free
+
     def _take(self):
         with self._cv:
             while True:
+                free = self._measured_free() if self._pending else None
                 for i, job in enumerate(self._pending):
                     if self._in_use + job.footprint() <= self.hbm_budget:
+                        if free is not None and free < job.footprint():
+                            self.waits_on_device_memory += 1
+                            continue
                         self._pending.pop(i)
                         self._in_use += job.footprint()
                         self.peak_in_use = max(self.peak_in_use, self._in_use)
@@ -150,6 +177,7 @@ class Server:
 
     def _release(self, job):
         with self._cv:
+            self._measured_free()
             self._in_use -= job.footprint()
             self.done.append(job)
             self._cv.notify_all()

@@ -84,3 +84,38 @@ def test_poisson_trace_is_seeded():
     assert all(j.n == 42 for j in a[-3:]) and all(20 <= j.n <= 26 for j in a[:-3])
     assert all(0 <= j.skip < j.end <= 1000 + j.n and j.end - j.skip <= 64 for j in a)
     assert all(x.arrival < y.arrival for x, y in zip(a, a[1:]))
+
+
+def test_admission_waits_for_measured_device_memory():
+    """The footprint is an estimate: a job is also held until the driver reports its footprint
+    free on the device. A fake probe reports room for the first job only until it finishes
+    (as when a buffer grew), so the second job, which fits the budget, waits for it; the peak
+    measured use is recorded."""
+    from bs45_quantum_explorer_gb300.lane import LaneResult
+    from bs45_quantum_explorer_gb300.serve import SLOT_BASE_BYTES, Job, Server
+    first_done = threading.Event()
+    order = []
+    jobs = [Job(jid=0, n=20, sig=(1, 5, 2, 6), skip=0, end=1, buf_cap=1000, arrival=0.0),
+            Job(jid=1, n=20, sig=(1, 5, 2, 6), skip=0, end=1, buf_cap=1 << 20, arrival=0.01)]
+    assert jobs[0].footprint() < jobs[1].footprint()
+    total = 1 << 36
+    busy = total - (jobs[0].footprint() + (1 << 20))  # leaves room for job 0 only
+
+    def probe():
+        used = 1 << 20 if first_done.is_set() else busy
+        return total - used, total
+
+    def runner(slot, job):
+        order.append(("start", job.jid))
+        time.sleep(0.05)
+        order.append(("end", job.jid))
+        if job.jid == 0:
+            first_done.set()
+        return LaneResult()
+
+    srv = Server(slots=2, hbm_budget=2 * SLOT_BASE_BYTES + (1 << 34), runner=runner, mem_probe=probe)
+    out, _ = srv.run_trace(jobs)
+    assert all(j.result is not None and j.error is None for j in out)
+    assert order.index(("end", 0)) < order.index(("start", 1))
+    assert srv.waits_on_device_memory > 0
+    assert srv.peak_device_used == busy
