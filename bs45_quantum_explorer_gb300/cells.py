@@ -63,13 +63,16 @@ def ab_rows(n, sig, m, cells):
     nrows = np.zeros(max(1, ncell), dtype=np.int32)
     total = C.c_longlong(0)
     a, b = sig[0], sig[1]
-    rc = lib().bs_ab_rows(n, a, b, m, arr, ncell, None, 0, row_off.ctypes.data, nrows.ctypes.data,
-                          C.byref(total))
-    if rc not in (BS_OK, BS_ERR_CAP):
-        check(rc, "ab_rows")
-    rows = np.zeros((max(1, total.value), 16), dtype=np.int8)
-    check(lib().bs_ab_rows(n, a, b, m, arr, ncell, rows.ctypes.data, total.value, row_off.ctypes.data,
-                           nrows.ctypes.data, C.byref(total)), "ab_rows")
+    # one call when the rows fit a first guess; the call reports the size when they do not
+    cap = max(1 << 16, 4096 * max(1, ncell))
+    rows = np.zeros((cap, 16), dtype=np.int8)
+    rc = lib().bs_ab_rows(n, a, b, m, arr, ncell, rows.ctypes.data, cap, row_off.ctypes.data,
+                          nrows.ctypes.data, C.byref(total))
+    if rc == BS_ERR_CAP:
+        rows = np.zeros((max(1, total.value), 16), dtype=np.int8)
+        rc = lib().bs_ab_rows(n, a, b, m, arr, ncell, rows.ctypes.data, total.value,
+                              row_off.ctypes.data, nrows.ctypes.data, C.byref(total))
+    check(rc, "ab_rows")
     return rows[:total.value], row_off[:ncell], nrows[:ncell]
 
 

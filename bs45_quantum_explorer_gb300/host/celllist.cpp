@@ -625,7 +625,7 @@ uint64_t AbpRows::cell_key_of(const Profile &p, int n, int m) {
 void AbpRows::build(const std::vector<uint64_t> &keys, int n, int sigA, int sigB, int m) {
   for (uint64_t k : keys) by_key.emplace(k, std::vector<int8_t>());
   const int hm = m / 2, n1 = n + 1, tgt = 4 * n + 2;
-  struct Tup { Vec v; int norm; int ca[3]; };
+  struct Tup { Vec v; int norm; Vec ca; };
   auto tups = [&](int sig) {
     std::vector<Tup> out;
     for (int sgn = 1; sgn >= (sig ? -1 : 1); sgn -= 2)
@@ -634,6 +634,7 @@ void AbpRows::build(const std::vector<uint64_t> &keys, int n, int sigA, int sigB
         t.v = v;
         t.norm = norm_vec(v);
         if (t.norm > tgt) continue;
+        t.ca.assign(hm, 0);
         for (int s = 1; s <= hm; s++) t.ca[s - 1] = autocorr_vec(v, s) + autocorr_vec(v, m - s);
         out.push_back(std::move(t));
       }
@@ -642,23 +643,48 @@ void AbpRows::build(const std::vector<uint64_t> &keys, int n, int sigA, int sigB
   const auto Kt = tups(sigA), Rt = tups(sigB);
   nK = Kt.size();
   nR = Rt.size();
-  Vec Tsum(hm);
+  // The reference pairs every (k, r) tuple and keeps the pair when auto_key(k.ca + r.ca,
+  // k.norm + r.norm) is a wanted key. auto_key packs the norm and each residue into its own
+  // 16-bit field, so it is one-to-one on these values: for a given k and wanted key (need, T)
+  // the pair matches exactly when r has norm need - k.norm and residues T - k.ca. So the r
+  // tuples are indexed by auto_key(r.ca, r.norm), and each k looks up, per wanted key, the r
+  // that complete it (in r order, so every key's rows come out in the reference's order).
+  std::unordered_map<uint64_t, std::vector<int>> r_of;
+  for (int j = 0; j < (int)Rt.size(); j++) r_of[auto_key(Rt[j].ca, Rt[j].norm)].push_back(j);
+  struct Want { uint64_t key; int need; Vec T; std::vector<int8_t> *out; };
+  std::vector<Want> wants;
+  for (auto &kv : by_key) {
+    Want w;
+    w.key = kv.first;
+    w.need = (int)(kv.first & 0xFFFF);
+    w.T.assign(hm, 0);
+    for (int i = 0; i < hm && i < 3; i++) w.T[i] = (int)((kv.first >> (16 * (i + 1))) & 0xFFFF) - 8192;
+    w.out = &kv.second;
+    wants.push_back(std::move(w));
+  }
+  Vec need_ca(hm);
   for (const auto &kt : Kt)
-    for (const auto &rt : Rt) {
-      const int nn2 = kt.norm + rt.norm;
-      if (nn2 > tgt) continue;
-      for (int s = 0; s < hm; s++) Tsum[s] = kt.ca[s] + rt.ca[s];
-      auto it = by_key.find(auto_key(Tsum, nn2));
-      if (it == by_key.end()) continue;
-      if (!thm212_ok(kt.v, rt.v, m, n, true)) continue;
-      int8_t row[16] = {0};
-      for (int c = 0; c < m; c++) {
-        row[c] = (int8_t)kt.v[c];
-        row[8 + c] = (int8_t)rt.v[c];
+    for (const auto &w : wants) {
+      if (w.need > tgt) continue;  // every pair's norm sum is above the target
+      for (int s = 0; s < hm; s++) need_ca[s] = w.T[s] - kt.ca[s];
+      auto it = r_of.find(auto_key(need_ca, w.need - kt.norm));
+      if (it == r_of.end()) continue;
+      for (int j : it->second) {
+        const auto &rt = Rt[j];
+        // the key fields are exact, but check the sums themselves all the same
+        bool same = rt.norm + kt.norm == w.need;
+        for (int s = 0; s < hm && same; s++) same = kt.ca[s] + rt.ca[s] == w.T[s];
+        if (!same) continue;
+        if (!thm212_ok(kt.v, rt.v, m, n, true)) continue;
+        int8_t row[16] = {0};
+        for (int c = 0; c < m; c++) {
+          row[c] = (int8_t)kt.v[c];
+          row[8 + c] = (int8_t)rt.v[c];
+        }
+        w.out->insert(w.out->end(), row, row + 16);
+        rows++;
+        max_list = std::max(max_list, w.out->size() / 16);
       }
-      it->second.insert(it->second.end(), row, row + 16);
-      rows++;
-      max_list = std::max(max_list, it->second.size() / 16);
     }
 }
 

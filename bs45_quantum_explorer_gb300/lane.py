@@ -100,7 +100,9 @@ def run_lane(ctx, n, sig, skip=0, end=0, shard=0, nshard=1, budget=200000, buf_c
     t_start = time.perf_counter()
     live = [pi for pi in owned if kept[pi]]
     # allowed A,B rows of every owned kept cell (the reference's abpMap), one host call
+    t_rows = time.perf_counter()
     rows, row_off, nrows = ab_rows(n, sig, m, [cells[pi] for pi in live]) if live else (None, [], [])
+    res.timings["rows_s"] = time.perf_counter() - t_rows
     slot = {pi: j for j, pi in enumerate(live)}
     if batch_cells is None:
         batch_cells = 32 if n <= 30 else 1
@@ -159,7 +161,9 @@ def run_lane(ctx, n, sig, skip=0, end=0, shard=0, nshard=1, budget=200000, buf_c
             lo, hi = b * buf_cap, min(nout, (b + 1) * buf_cap)
             cand = cs_start + hi          # survivors counted when this batch is drained
             keep = min(hi - lo, drain_top) if drain_top > 0 else hi - lo
+            t_k = time.perf_counter()
             order, _ = flat_topk(ctx, surv[lo:hi], hi - lo, keep)
+            res.timings["topk_s"] = res.timings.get("topk_s", 0.0) + time.perf_counter() - t_k
             for c0 in range(0, len(order), chunk):
                 idx = lo + order[c0:c0 + chunk]
                 t1 = time.perf_counter()
