@@ -50,14 +50,19 @@ def complete_ab(ctx, cands, budget, rows_per_cand=None, m=6, outer_k=3, early=Tr
         arr["nrows"][:k] = all_rows.shape[0]
         off = all_rows.shape[0]
     else:
-        parts, off = [], 0
+        # one copy of each row set: candidates given the same array share its rows (and the
+        # library builds its bitset masks once)
+        parts, off, seen = [], 0, {}
         for i in range(k):
             r = None if rows_per_cand is None else rows_per_cand[i]
             if r is not None and len(r):
-                r = np.ascontiguousarray(r, np.int8).reshape(-1, 16)
-                arr["row_off"][i], arr["nrows"][i] = off, r.shape[0]
-                parts.append(r)
-                off += r.shape[0]
+                key = id(r)
+                if key not in seen:
+                    rr = np.ascontiguousarray(r, np.int8).reshape(-1, 16)
+                    seen[key] = (off, rr.shape[0], r)  # r kept alive so its id stays unique
+                    parts.append(rr)
+                    off += rr.shape[0]
+                arr["row_off"][i], arr["nrows"][i] = seen[key][0], seen[key][1]
         all_rows = np.concatenate(parts) if parts else np.zeros((1, 16), np.int8)
     all_rows = np.ascontiguousarray(all_rows)
     opt = AbOpts(budget=budget, outer_k=outer_k, early=int(early), canon=int(canon), m=m,

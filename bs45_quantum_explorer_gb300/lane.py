@@ -131,58 +131,70 @@ def run_lane(ctx, n, sig, skip=0, end=0, shard=0, nshard=1, budget=200000, buf_c
             w = surv[int(bounds[k]):int(bounds[k + 1])]
             streamed[q] = (w[:cut] if cut else w, st[k])
 
-    cand = 0
-    for pi in owned:
-        if max_seconds > 0 and time.perf_counter() - t_start > max_seconds:
-            break
-        if not kept[pi]:
-            res.cells_orbit_dup += 1
-            continue
-        j = slot[pi]
-        nr = int(nrows[j])
-        if nr == 0:
-            res.cells_prof_dead += 1
-            res.cells_done += 1
-            continue
-        cell_rows = rows[row_off[j]:row_off[j] + nr] if nr <= abp_cap else None
-        if cell_rows is None:
-            res.cells_prof_uncap += 1
-        if pi not in streamed:
-            stream_from(j)
-        surv, st0 = streamed.pop(pi)
-        res.dfs_nodes += st0["nodes"]
-        nout = len(surv)
-        cs_start = cand
-        nb = (nout + buf_cap - 1) // buf_cap
-        if drain_top > 0:
-            nb = min(nb, drain_batches)
-        found = False
-        for b in range(nb):
-            lo, hi = b * buf_cap, min(nout, (b + 1) * buf_cap)
-            cand = cs_start + hi          # survivors counted when this batch is drained
-            keep = min(hi - lo, drain_top) if drain_top > 0 else hi - lo
-            t_k = time.perf_counter()
-            order, _ = flat_topk(ctx, surv[lo:hi], hi - lo, keep)
-            res.timings["topk_s"] = res.timings.get("topk_s", 0.0) + time.perf_counter() - t_k
-            for c0 in range(0, len(order), chunk):
-                idx = lo + order[c0:c0 + chunk]
+    # The cells' effects go to a queue in cell order and are applied when the queued
+    # completions have run: the kept candidates of several cells (each with its own allowed
+    # rows) go to the completer in one call once at least FLUSH of them wait, so that small
+    # per-cell keeps (DRAIN_TOP 64) fill the device. The call runs in first-hit mode over the
+    # candidates in cell order, and the queue is replayed in that order up to the first hit,
+    # so every count, the hit and its quad are those of completing cell by cell; cells after
+    # a hit are streamed but never counted.
+    FLUSH = 4096
+    queue = []    # ("count", {field: increment}) | ("batch", item) | ("cell", {...})
+    pend = []     # the batch items waiting for the completer, in order
+    npend = 0
+
+    def flush():
+        """Completes the queued candidates and replays the queue; True on a hit."""
+        nonlocal npend
+        if pend:
+            words = np.concatenate([it["words"] for it in pend])
+            rpc = []
+            for it in pend:
+                rpc.extend([it["rows"] if it["rows"] is not None else np.zeros((0, 16), np.int8)] *
+                           len(it["words"]))
+            out = []
+            for c0 in range(0, len(words), chunk):
                 t1 = time.perf_counter()
                 ctx.timing(True)
-                v, nd, A, B = complete_ab(ctx, surv[idx], budget, rows=cell_rows, m=m,
-                                          outer_k=outer_k, early=early, canon=canon,
-                                          first_hit=True, a2=a2, **ab_kw)
+                out.append(complete_ab(ctx, words[c0:c0 + chunk], budget, rows_per_cand=rpc[c0:c0 + chunk],
+                                       m=m, outer_k=outer_k, early=early, canon=canon,
+                                       first_hit=True, a2=a2, **ab_kw))
                 ms, _, _ = ctx.timing_read()
                 ctx.timing(False)
                 res.complete_s += time.perf_counter() - t1
                 res.complete_device_ms += ms
-                for t in range(len(idx)):
-                    r = int(v[t])
+                if (out[-1][0] == 0).any():
+                    break  # a hit: later chunks are never reached in cell order
+            v = np.concatenate([o[0] for o in out])
+            nd = np.concatenate([o[1] for o in out])
+            A = np.concatenate([o[2] for o in out])
+            B = np.concatenate([o[3] for o in out])
+            base = 0
+            for it in pend:
+                it["v"], it["nd"], it["A"], it["B"] = (v[base:base + len(it["words"])],
+                                                       nd[base:base + len(it["words"])],
+                                                       A[base:base + len(it["words"])],
+                                                       B[base:base + len(it["words"])])
+                base += len(it["words"])
+        found = False
+        for kind, x in queue:
+            if kind == "count":
+                for f, inc in x.items():
+                    setattr(res, f, getattr(res, f) + inc)
+            elif kind == "cell":
+                res.cells_capped += x["capped"]
+                res.candidates_streamed = x["cand"]
+                res.cells_done += 1
+                res.cells_empty += x["empty"]
+            else:
+                for t in range(len(x["words"])):
+                    r = int(x["v"][t]) if t < len(x["v"]) else -1
                     if r < 0:
                         raise RuntimeError(f"candidate {t} of a batch was not completed ({r})")
                     if r == 4:
                         raise RuntimeError("completer found a quad whose NPAF recheck failed")
                     res.completions += 1
-                    res.total_ab_nodes += int(nd[t])
+                    res.total_ab_nodes += int(x["nd"][t])
                     if r >= 2 or r == 0:  # the summary counts the hit as entered too
                         res.backtracks_entered += 1
                     if r == 1:
@@ -192,26 +204,65 @@ def run_lane(ctx, n, sig, skip=0, end=0, shard=0, nshard=1, budget=200000, buf_c
                     elif r == 3:
                         res.budget_aborted += 1
                     elif r == 0:
-                        cw = unpack(surv[idx[t]:idx[t] + 1], n)[0]
-                        res.found, res.hit_idx, res.profile_rank = True, cand, pi
-                        res.quad = (A[t].copy(), B[t].copy(), cw[0].copy(), cw[1].copy())
-                        res.nodes_this_cand = int(nd[t])
+                        cw = unpack(x["words"][t:t + 1], n)[0]
+                        res.found, res.hit_idx, res.profile_rank = True, x["cand"], x["pi"]
+                        res.quad = (x["A"][t].copy(), x["B"][t].copy(), cw[0].copy(), cw[1].copy())
+                        res.nodes_this_cand = int(x["nd"][t])
+                        res.candidates_streamed = x["cand"]
                         found = True
                         break
                 if found:
                     break
+        queue.clear()
+        pend.clear()
+        npend = 0
+        return found
+
+    cand = 0
+    found = False
+    for pi in owned:
+        if max_seconds > 0 and time.perf_counter() - t_start > max_seconds:
+            break
+        if not kept[pi]:
+            queue.append(("count", {"cells_orbit_dup": 1}))
+            continue
+        j = slot[pi]
+        nr = int(nrows[j])
+        if nr == 0:
+            queue.append(("count", {"cells_prof_dead": 1, "cells_done": 1}))
+            continue
+        cell_rows = rows[row_off[j]:row_off[j] + nr] if nr <= abp_cap else None
+        if cell_rows is None:
+            queue.append(("count", {"cells_prof_uncap": 1}))
+        if pi not in streamed:
+            stream_from(j)
+        surv, st0 = streamed.pop(pi)
+        queue.append(("count", {"dfs_nodes": st0["nodes"]}))
+        nout = len(surv)
+        cs_start = cand
+        nb = (nout + buf_cap - 1) // buf_cap
+        if drain_top > 0:
+            nb = min(nb, drain_batches)
+        for b in range(nb):
+            lo, hi = b * buf_cap, min(nout, (b + 1) * buf_cap)
+            cand = cs_start + hi          # survivors counted when this batch is drained
+            keep = min(hi - lo, drain_top) if drain_top > 0 else hi - lo
+            t_k = time.perf_counter()
+            order, _ = flat_topk(ctx, surv[lo:hi], hi - lo, keep)
+            res.timings["topk_s"] = res.timings.get("topk_s", 0.0) + time.perf_counter() - t_k
+            item = {"words": surv[lo + order], "rows": cell_rows, "cand": cand, "pi": pi}
+            queue.append(("batch", item))
+            pend.append(item)
+            npend += len(order)
+        # the lane counts a cell as capped once it has drained its last allowed batch
+        cand = cs_start + (min(nout, drain_batches * buf_cap) if drain_top > 0 else nout)
+        queue.append(("cell", {"capped": int(drain_top > 0 and nout > 0 and -(-nout // buf_cap) >= drain_batches),
+                               "cand": cand, "empty": int(nout == 0)}))
+        if npend >= FLUSH:
+            found = flush()
             if found:
                 break
-        if found:
-            res.candidates_streamed = cand
-            break
-        # the lane counts a cell as capped once it has drained its last allowed batch
-        if drain_top > 0 and nout > 0 and -(-nout // buf_cap) >= drain_batches:
-            res.cells_capped += 1
-        res.candidates_streamed = cand = cs_start + (min(nout, drain_batches * buf_cap)
-                                                     if drain_top > 0 else nout)
-        res.cells_done += 1
-        if nout == 0:
-            res.cells_empty += 1
+    if not found:
+        flush()
     res.timings["wall_s"] = time.perf_counter() - t_start
     return res

@@ -51,15 +51,18 @@ def _fakes(oracle):
         return order, sc[order]
 
     def complete(ctx, words, budget, rows=None, m=6, outer_k=3, early=True, canon=True,
-                 first_hit=False, **kw):
+                 first_hit=False, rows_per_cand=None, **kw):
         X = unpack(np.asarray(words).reshape(-1, 2), ctx.n)
         out = [[], [], [], []]
         hit = False
-        for C, D in X:
+        for i, (C, D) in enumerate(X):
+            r = rows if rows_per_cand is None else rows_per_cand[i]
+            if r is not None and not len(r):
+                r = None
             if hit:
                 v, nd, a, b = -1, 0, np.zeros(ctx.n + 1, np.int8), np.zeros(ctx.n + 1, np.int8)
             else:
-                v, nd, a, b = oracle.complete_ab(ctx.n, ctx.sig[0], ctx.sig[1], C, D, budget, rows=rows,
+                v, nd, a, b = oracle.complete_ab(ctx.n, ctx.sig[0], ctx.sig[1], C, D, budget, rows=r,
                                                  m=m, outer_k=outer_k, early=early, canon=canon)
                 hit = first_hit and v == 0
             for lst, x in zip(out, (v, nd, a, b)):
