@@ -583,7 +583,8 @@ def run_join(n=24):
             "probe_algorithmic_gb_per_s": alg / (probe_ms * 1e-3) / 1e9 if probe_ms > 0 else None}
 
 
-def run_serving(n_jobs=12, tail=2, rate=2.0, slots=4, max_cells=4096, ref_seconds=0.0):
+def run_serving(n_jobs=12, tail=2, rate=2.0, slots=4, max_cells=4096, ref_seconds=0.0,
+                lane_opts=None):
     """C5: a seeded Poisson stream of first-hit jobs, n uniform in 20..42 with a signature from
     classes(n) and a contiguous ORDER=3 range of 1..max_cells raw cells, plus `tail` n = 42
     ranges; per-job budget 2^16, BUF_CAP 2000, DRAIN_TOP 64 (the per-cell work reduced from the
@@ -606,7 +607,7 @@ def run_serving(n_jobs=12, tail=2, rate=2.0, slots=4, max_cells=4096, ref_second
     jobs = poisson_trace(nj=n_jobs, rate=rate, seed=SEED, n_range=(20, 42), max_cells=max_cells,
                          tail_n42=tail, classes=_classes, ncells_of=lambda n, sg: len(lists[(n, sg)][1]),
                          budget=1 << 16, buf_cap=2000, drain_top=64)
-    srv = Server(slots=slots)
+    srv = Server(slots=slots, lane_opts=lane_opts)
     out, st = srv.run_trace(jobs)
     d = st.as_dict()
     d.update({"workload": f"{len(jobs)} jobs ({tail} of them n=42), Poisson rate {rate}/s, seed {SEED:#x}, "
@@ -625,9 +626,11 @@ def run_serving(n_jobs=12, tail=2, rate=2.0, slots=4, max_cells=4096, ref_second
                         budget=j.budget, buf_cap=j.buf_cap, drain_top=j.drain_top,
                         drain_batches=j.drain_batches, arrival=0.0)
                     for j, (fin, rpi) in zip(jobs, per_job) if fin or (rpi is not None and rpi > j.skip)]
-            out2, st2 = Server(slots=slots).run_trace(same)
+            # one slot per job, as the reference runs one process per job
+            out2, st2 = Server(slots=min(len(same), 16), lane_opts=lane_opts).run_trace(same)
             d["same_work"] = {
-                "jobs": len(same), "reference_cells_done": ref["cells_done"], "our_cells_done": st2.cells,
+                "jobs": len(same), "slots": min(len(same), 16),
+                "reference_cells_done": ref["cells_done"], "our_cells_done": st2.cells,
                 "reference_seconds": ref["seconds"], "reference_cores": ref["cores"],
                 "our_seconds": round(st2.makespan_s, 2),
                 "speedup": ref["seconds"] / st2.makespan_s if st2.makespan_s > 0 else None,
