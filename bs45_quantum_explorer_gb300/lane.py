@@ -76,8 +76,9 @@ def run_lane(ctx, n, sig, skip=0, end=0, shard=0, nshard=1, budget=200000, buf_c
              max_seconds=0.0, listing=None, batch_cells=None, cd_prune=0, a2=0, tuning=None):
     """Runs the lane over raw cells [skip, end) of its shard (end = 0: to the list's end).
     The list options are the lane's WZ_FH_* list settings (cells.cell_list); the cells must
-    be mod-6 cells (the lane's buffered order). max_seconds > 0 stops between cells once
-    exceeded (the result then says found=False and its counts cover the cells done).
+    be mod-6 cells (the lane's buffered order). max_seconds > 0 takes no new cell once
+    exceeded; the cells already taken are completed (their queued candidates included, which
+    can still give the hit), and the counts cover those cells.
     listing: a cell_list() result to reuse. batch_cells: cells streamed per device call
     (default 32 up to n = 30, where cells are small, else 1); a batch is streamed whole and
     each cell cut to its front-only prefix on the host, which is the same prefix.
@@ -156,7 +157,12 @@ def run_lane(ctx, n, sig, skip=0, end=0, shard=0, nshard=1, budget=200000, buf_c
             for c0 in range(0, len(words), chunk):
                 t1 = time.perf_counter()
                 ctx.timing(True)
-                out.append(complete_ab(ctx, words[c0:c0 + chunk], budget, rows_per_cand=rpc[c0:c0 + chunk],
+                part = rpc[c0:c0 + chunk]
+                # one shared row set (a lane's one large cell): no per-candidate list
+                one = len({id(x) for x in part}) == 1
+                out.append(complete_ab(ctx, words[c0:c0 + chunk], budget,
+                                       rows=part[0] if one and len(part[0]) else None,
+                                       rows_per_cand=None if one else part,
                                        m=m, outer_k=outer_k, early=early, canon=canon,
                                        first_hit=True, a2=a2, **ab_kw))
                 ms, _, _ = ctx.timing_read()
