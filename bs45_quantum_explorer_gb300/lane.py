@@ -73,7 +73,8 @@ def run_lane(ctx, n, sig, skip=0, end=0, shard=0, nshard=1, budget=200000, buf_c
              drain_top=0, drain_batches=1, endpos=False, orbit_canon=True, orbit_q=1, qprune=True,
              prof_order=3, m6=None, thm211b=None, thm212=None, abp_cap=20000, outer_k=3,
              early=True, canon=True, rev=False, hall_mode="tc_fp16", chunk=65536,
-             max_seconds=0.0, listing=None, batch_cells=None, cd_prune=0, a2=0, tuning=None):
+             max_seconds=0.0, listing=None, batch_cells=None, cd_prune=0, a2=0, tuning=None,
+             flush_cands=4096):
     """Runs the lane over raw cells [skip, end) of its shard (end = 0: to the list's end).
     The list options are the lane's WZ_FH_* list settings (cells.cell_list); the cells must
     be mod-6 cells (the lane's buffered order). max_seconds > 0 takes no new cell once
@@ -85,7 +86,8 @@ def run_lane(ctx, n, sig, skip=0, end=0, shard=0, nshard=1, budget=200000, buf_c
     cd_prune: WZ_FH_CD_PRUNE for the streams (fewer DFS nodes, the same candidates).
     a2: WZ_FH_A2 (2 = the A2 row prune in the completer).
     tuning: work sizes from tune.py (stream fine_nodes / wave_nodes / dfs_blocks, completer
-    blocks_per_sm and chunk); none of them changes a result."""
+    blocks_per_sm and chunk); none of them changes a result.
+    flush_cands: kept candidates queued (over whole cells) before one completer call."""
     tuning = dict(tuning or {})
     stream_kw = {k: tuning[k] for k in ("fine_nodes", "wave_nodes", "dfs_blocks") if k in tuning}
     ab_kw = {k: tuning[k] for k in ("blocks_per_sm",) if k in tuning}
@@ -139,7 +141,7 @@ def run_lane(ctx, n, sig, skip=0, end=0, shard=0, nshard=1, budget=200000, buf_c
     # candidates in cell order, and the queue is replayed in that order up to the first hit,
     # so every count, the hit and its quad are those of completing cell by cell; cells after
     # a hit are streamed but never counted.
-    FLUSH = 4096
+    FLUSH = max(1, int(flush_cands))
     queue = []    # ("count", {field: increment}) | ("batch", item) | ("cell", {...})
     pend = []     # the batch items waiting for the completer, in order
     npend = 0

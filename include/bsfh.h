@@ -115,9 +115,10 @@ int bs_hall_filter_dev(bs_ctx *ctx, const uint64_t *d_bits, long long npairs, in
  * receives the decisions, both device memory owned by the caller; at most 1,048,576 pairs
  * per call (BS_ERR_CAP beyond); npairs = 0 only checks the set-up. The work is enqueued on
  * `stream` (a cudaStream_t; NULL is the legacy default stream), and every call ends by
- * synchronising that stream to read the status word back. The first call on a device, and
- * the first call with a new n, set the scratch up (device symbol address, kernel attributes,
- * tables uploaded from static host arrays); make that first call before any stream capture.
+ * synchronising that stream to read the status word back, so no call can be made inside
+ * stream capture. The first call on a device, and the first call with a new n, set the
+ * scratch up (device symbol address, kernel attributes, tables uploaded from static host
+ * arrays).
  * Calls share the one array and keep the last call's tables and band list; the counters are
  * cleared by every call. Calls that overlap on the GPU (other streams, other host threads)
  * race and must be serialised by the caller. */
