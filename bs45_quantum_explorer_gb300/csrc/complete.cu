@@ -286,9 +286,6 @@ __global__ void __launch_bounds__(32 * AB_WARPS, MINB) ab_kernel(AbParams P) {
   };
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const long long slot = (long long)blockIdx.x * AB_WARPS + wib;
-  __shared__ int s_lo[AB_WARPS][AB_MAXLV];         // the level's row bitset: nonzero words
-  __shared__ int s_hi[AB_WARPS][AB_MAXLV];         // lie in [lo, hi)
-  int *wlo = s_lo[wib], *whi = s_hi[wib];
   // Per-level control state: k | omask << 4 | ties << 12 and the early-check residual. The
   // current level's is held in registers (cur, cres, warp-uniform); the levels above it are
   // saved one level per lane (levels 0..half-1 <= 31: lane j holds level j's), written by that
@@ -296,6 +293,9 @@ __global__ void __launch_bounds__(32 * AB_WARPS, MINB) ab_kernel(AbParams P) {
   // shared memory or warp barrier is involved.
   uint32_t my_ctrl = 0;
   int my_res = 0;
+  // and the level's row bitset range: its nonzero words lie in [lo, hi), saved as lo | hi << 16
+  // (W < 65536 words, checked on the host); the current level's in clo, chi
+  uint32_t my_rng = 0;
   uint64_t *lv = P.bits + (size_t)slot * (P.half + 1) * P.Wcap;
   const int L = P.L, n = P.n, half = P.half, m = P.m;
   // A second shift slot per lane when n >= 33. Its shifts s >= 33 pair position d only with
@@ -346,11 +346,7 @@ __global__ void __launch_bounds__(32 * AB_WARPS, MINB) ab_kernel(AbParams P) {
     int d = 0;
     uint32_t cur = 0u | (0xFFu << 4) | (5u << 12);  // level 0; ties: a_tied = b_tied = 1
     int cres = 0;
-    if (lane == 0) {
-      wlo[0] = 0;
-      whi[0] = cd.W;
-    }
-    __syncwarp();
+    int clo = 0, chi = cd.W;
     unsigned steps = 0;
     while (true) {
       if ((++steps & 1023) == 0) {
@@ -369,7 +365,7 @@ __global__ void __launch_bounds__(32 * AB_WARPS, MINB) ab_kernel(AbParams P) {
             // fh_abp_leaf_ok: a row of the last list equals the placed class sums exactly
             const uint64_t *lst = lv + (size_t)half * P.Wcap;
             bool any = false;
-            for (int w = wlo[half] + lane; w < whi[half]; w += 32) {
+            for (int w = clo + lane; w < chi; w += 32) {
               uint64_t x = lst[w];
               for (int c = 0; c < m; c++) {
                 const int pa = ssum(u.A, u.Pm, s_cm[c]), pb = ssum(u.B, u.Pm, s_cm[c]);
@@ -400,6 +396,11 @@ __global__ void __launch_bounds__(32 * AB_WARPS, MINB) ab_kernel(AbParams P) {
         d--;
         cur = __shfl_sync(FULL_MASK, my_ctrl, d);
         cres = __shfl_sync(FULL_MASK, my_res, d);
+        {
+          const uint32_t rg = __shfl_sync(FULL_MASK, my_rng, d);
+          clo = (int)(rg & 0xFFFFu);
+          chi = (int)(rg >> 16);
+        }
         clear_bits(u, pair_bits(d, L));
         cur = (cur & ~15u) | ((cur & 15) + 1);
         continue;
@@ -413,6 +414,11 @@ __global__ void __launch_bounds__(32 * AB_WARPS, MINB) ab_kernel(AbParams P) {
         d--;
         cur = __shfl_sync(FULL_MASK, my_ctrl, d);
         cres = __shfl_sync(FULL_MASK, my_res, d);
+        {
+          const uint32_t rg = __shfl_sync(FULL_MASK, my_rng, d);
+          clo = (int)(rg & 0xFFFFu);
+          chi = (int)(rg >> 16);
+        }
         clear_bits(u, pair_bits(d, L));
         cur = (cur & ~15u) | ((cur & 15) + 1);
         continue;
@@ -446,12 +452,13 @@ __global__ void __launch_bounds__(32 * AB_WARPS, MINB) ab_kernel(AbParams P) {
         bool bad = (v.s0 && absi(v.t0 - v.D0) > v.K0) || (v.s1 && absi(v.t1 - v.D1) > v.K1);
         prune = __any_sync(FULL_MASK, bad);
       }
+      int child_lo = 0, child_hi = 0;  // the child level's row range (from the filter)
       if (!prune && rows) {
         // fh_abp_filter(d): the level-(d+1) list from the level-d list (all rows at d = 0)
         const int c1 = s_cls[d], c2 = s_cls[L - 1 - d];
         const uint64_t *src = lv + (size_t)d * P.Wcap;
         uint64_t *dst = lv + (size_t)(d + 1) * P.Wcap;
-        const int lo = wlo[d], hi = whi[d];
+        const int lo = clo, hi = chi;
         int nlo, nhi;
         if (!P.a2 && hi - lo <= 24) {
           // Narrow lists (the deep levels, where the nodes are): lane 8i + j loads mask j
@@ -519,9 +526,8 @@ __global__ void __launch_bounds__(32 * AB_WARPS, MINB) ab_kernel(AbParams P) {
           nlo = __reduce_min_sync(FULL_MASK, mylo);
           nhi = __reduce_max_sync(FULL_MASK, myhi);
         }
-        __syncwarp();
-        wlo[d + 1] = nlo;  // the warp's uniform state: every lane writes the same value
-        whi[d + 1] = nhi + 1;
+        child_lo = nlo;
+        child_hi = nhi + 1;
         prune = nhi < 0;
       }
       if (prune) {
@@ -550,6 +556,11 @@ __global__ void __launch_bounds__(32 * AB_WARPS, MINB) ab_kernel(AbParams P) {
       if (lane == d) {  // save this level (at the quad taken) for the way back
         my_ctrl = (c0 & ~15u) | (uint32_t)k;
         my_res = cres;
+        my_rng = (uint32_t)clo | ((uint32_t)chi << 16);
+      }
+      if (rows) {
+        clo = child_lo;
+        chi = child_hi;
       }
       cur = 0u | (om << 4) | ((uint32_t)s_ntie[d == 0 ? 16 : ties][k] << 12);
       cres = r_e;
@@ -736,6 +747,7 @@ extern "C" int bs_complete_ab_batch(bs_ctx *ctx, const bs_ab_cand *cands, long l
   }
   int Wcap = 1;
   for (auto &k : sets) Wcap = std::max(Wcap, (k.second + 63) / 64);
+  if (Wcap > 65535) return BS_ERR_CAP;  // a row range is kept in 16-bit halves
   if (!same && !sets.empty()) {
     long long total = 0;
     for (size_t k = 0; k < sets.size(); k++) {
