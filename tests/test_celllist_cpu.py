@@ -167,3 +167,48 @@ def test_ab_rows_match_the_rule(built_lib, n, sig, m6):
         got = [tuple(int(x) for x in r) for r in rows[row_off[j]:row_off[j] + nrows[j]]]
         want = _rows_brute(n, sig, m, list(px), list(py))
         assert got == want, (n, sig, px, py)
+
+
+def _rows_grouped(n, sig, m, cells):
+    """The same rule at production n: a pair (k, r) is kept when its norms sum to the cell's
+    need, its residues to the cell's needT, and Thm 2.12 holds, in k-then-r order. The r tuples
+    are grouped by (norm, residues), so each k looks up only the r that can complete it."""
+    tgt, hm = 4 * n + 2, m // 2
+
+    def side(sg):
+        return [v for s in ((1, -1) if sg else (1,)) for v in _enum_cs(n + 1, s * sg, m)]
+
+    def info(v):
+        return sum(x * x for x in v), tuple(_acf(v, s) + _acf(v, m - s) for s in range(1, hm + 1))
+    K = [(v,) + info(v) for v in side(sig[0])]
+    R = side(sig[1])
+    by = {}
+    for r in R:
+        by.setdefault(info(r), []).append(r)
+    out = []
+    for px, py in cells:
+        need = tgt - sum(v * v for v in px) - sum(v * v for v in py)
+        needT = [-(_acf(px, s) + _acf(py, s) + _acf(px, m - s) + _acf(py, m - s)) for s in range(1, hm + 1)]
+        rows = []
+        for k, kn, kT in K:
+            for r in by.get((need - kn, tuple(t - a for t, a in zip(needT, kT))), ()):
+                if _ab_side_212(k, r, m, n):
+                    rows.append(tuple(k) + (0,) * (8 - m) + tuple(r) + (0,) * (8 - m))
+        out.append(rows)
+    return out
+
+
+@pytest.mark.parametrize("n,sig", [(30, (1, 7, 6, 6)), (36, (5, 11, 0, 0))])
+def test_ab_rows_match_the_rule_at_production_n(built_lib, n, sig):
+    from bs45_quantum_explorer_gb300.cells import ab_rows, cell_tuple
+    from bs45_quantum_explorer_gb300.lane import lane_list
+    cells, kept, _, m = lane_list(n, sig, m6=True, thm211b=True, thm212=True)
+    idx = [i for i in range(len(kept)) if kept[i]]
+    pick = idx[:: max(1, len(idx) // 6)][:6]
+    sub = [cells[i] for i in pick]
+    rows, row_off, nrows = ab_rows(n, sig, m, sub)
+    want = _rows_grouped(n, sig, m, [tuple(map(list, cell_tuple(c, m))) for c in sub])
+    assert sum(len(w) for w in want) > 0
+    for j in range(len(sub)):
+        got = [tuple(int(x) for x in r) for r in rows[row_off[j]:row_off[j] + nrows[j]]]
+        assert got == want[j], (n, sig, j)
