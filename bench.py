@@ -525,13 +525,33 @@ def run_c3(max_cells=0, batch=32, topk=256, workers=3):
     surv_total = sum(p[2] for p in parts)
     kept_total = sum(p[3] for p in parts)
     alg = 32 * nodes + 16 * leaves + 24 * surv_total
+    cpu = c3_reference_rate([cells[i] for i in live], m)
     return {"workload": f"C,D stream n={n} sig={sig}: {len(live)} kept cells of the ORDER=3 list "
                         f"({len(kept)} cells, digest {digest}) streamed whole, flattest-{topk} per cell; "
                         f"batches of {batch} cells on {workers} host threads with their own contexts",
             "cells": len(live), "dfs_nodes": nodes, "leaves": leaves, "survivors": surv_total,
             "kept_topk": kept_total, "seconds": dt, "dfs_nodes_per_s": nodes / dt,
             "filtered_cands_per_s": leaves / dt, "cells_per_s": len(live) / dt,
-            "algorithmic_bytes": alg, "algorithmic_gb_per_s": alg / dt / 1e9}
+            "algorithmic_bytes": alg, "algorithmic_gb_per_s": alg / dt / 1e9, "cpu_baseline": cpu}
+
+
+def c3_reference_rate(cells, m, seconds=20.0, n=30, sig=(1, 7, 6, 6)):
+    """The reference's C,D stream (count_pairs22 with hall_ok_pair_fast, wz_match.cpp:678-784)
+    over the same kept cells in list order, one single-threaded arm per host core taking the
+    next cell from a shared queue, bounded to `seconds` (the cells in flight are cut there):
+    DFS nodes/s and whole cells/s, as the reference's arms work through a range."""
+    ncpu = os.cpu_count() or 1
+    arms = _ref_arms(ncpu, n=n, sig=sig)
+    if arms is None:
+        return {"unavailable": "oracle/_ref/libref.so was not built on this machine"}
+    todo = [(list(c.tx[:m]), list(c.ty[:m]), c.pinX, c.pinY) for c in cells]
+    r = arms.stream_cells_for(todo, seconds, m=m)
+    arms.close()
+    return {"value": r["nodes"] / r["seconds"], "unit": "DFS nodes/s", "cores": ncpu,
+            "kind": "reference", "cells_per_s": r["cells_done"] / r["seconds"],
+            "sample": f"{ncpu} single-threaded arms of count_pairs22 (src/solver/wz_match.cpp "
+                      f"compiled unmodified) over the same kept cells in list order for "
+                      f"{r['seconds']:.0f} s: {r['cells_done']} whole cells, {r['nodes']} nodes"}
 
 
 def run_join(n=24):

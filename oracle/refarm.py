@@ -124,6 +124,46 @@ class Arms:
         return {"nodes": sum(r[0] for r in res), "leaves": sum(r[1] for r in res),
                 "ok": sum(r[2] for r in res), "survivors": sum(r[3] for r in res), "seconds": dt}
 
+    def stream_cells_for(self, cells, seconds, m=6):
+        """The arms take cells ((tx, ty, pinX, pinY) of the C,D side) in order from a shared
+        queue and stream each whole until `seconds` have passed (the cell in flight is cut at
+        the deadline), as the reference's single-core arms work through a range. Returns
+        dict(nodes, leaves, ok, survivors, cells_done, seconds)."""
+        lock = threading.Lock()
+        nxt = [0]
+        t_end = time.perf_counter() + seconds
+
+        def one(i, _):
+            got = [0, 0, 0, 0, 0]
+            while True:
+                left = t_end - time.perf_counter()
+                if left <= 0:
+                    break
+                with lock:
+                    k = nxt[0]
+                    nxt[0] += 1
+                if k >= len(cells):
+                    break
+                tx, ty, pin_x, pin_y = cells[k]
+                ax, px = _ints(tx)  # the arrays stay alive while their pointers are used
+                ay, py = _ints(ty)
+                nodes, leaves, ok = C.c_longlong(0), C.c_longlong(0), C.c_longlong(0)
+                t0 = time.perf_counter()
+                s = self.libs[i].refh_stream_for(self.n, px, py, m, int(pin_x), int(pin_y), left,
+                                                 C.byref(nodes), C.byref(leaves), C.byref(ok))
+                got[0] += nodes.value
+                got[1] += leaves.value
+                got[2] += ok.value
+                got[3] += s
+                got[4] += time.perf_counter() - t0 < left  # finished before the deadline
+            return got
+        t0 = time.perf_counter()
+        res = self._parallel(one, [None] * self.narms)
+        dt = time.perf_counter() - t0
+        return {"nodes": sum(r[0] for r in res), "leaves": sum(r[1] for r in res),
+                "ok": sum(r[2] for r in res), "survivors": sum(r[3] for r in res),
+                "cells_done": sum(r[4] for r in res), "seconds": dt}
+
     # ---- the A,B completer (fh_complete_ab, wz_match.cpp:1298-1341) ----
     def complete_for(self, cands, budget, seconds, rows=None, m=6):
         """Completes candidates (int8 [K, 2, n]: C, D) in order from a shared queue on every

@@ -48,3 +48,29 @@ def test_reference_arm_under_torchrun_prints_on_rank0_only(built_lib):
     assert len(lines) == 1
     d = json.loads(lines[0])
     assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["value"] > 0
+
+
+def test_reference_arms_stream_a_range_of_cells(built_lib, oracle):
+    """The C3 baseline's arms (refarm.Arms.stream_cells_for): cells taken in order from a
+    shared queue and streamed whole through the reference's count_pairs22; with a generous
+    bound every cell finishes and the summed node and leaf counts equal the oracle's."""
+    import refarm
+    if not refarm.available():
+        pytest.skip("oracle/_ref/libref.so was not built here (the reference sources are absent)")
+    from bs45_quantum_explorer_gb300.cells import cell_list
+    n, sig = 20, (1, 9, 0, 0)  # 1 + 81 = 4n + 2
+    cells, kept, _, m = cell_list(n, sig, m6=True, thm211b=True, thm212=True)
+    live = [cells[i] for i in range(len(kept)) if kept[i]][:12]
+    todo = [(list(c.tx[:m]), list(c.ty[:m]), c.pinX, c.pinY) for c in live]
+    arms = refarm.Arms(3, n, sig)
+    try:
+        r = arms.stream_cells_for(todo, 120.0, m=m)
+    finally:
+        arms.close()
+    assert r["cells_done"] == len(todo)
+    want_nodes = want_leaves = 0
+    for tx, ty, px, py in todo:
+        _, _, st = oracle.cd_stream(n, tx, ty, m=m, pinX=bool(px), pinY=bool(py))
+        want_nodes += st["nodes"]
+        want_leaves += st["leaves"]
+    assert (r["nodes"], r["leaves"]) == (want_nodes, want_leaves)
