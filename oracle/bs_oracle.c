@@ -38,18 +38,31 @@ void or_hall_tables(int n, double *ct, double *st) {
   }
 }
 
+/* Angles 1..200 in a spread order: repeated halving of the range, so that neighbouring
+ * (nearly equal) tests come late and a rejected pair is usually found within a few angles. */
+static int HALL_ORDER[200];
+static pthread_once_t hall_order_once = PTHREAD_ONCE_INIT;
+static void build_hall_order(void) {
+  int seen[201] = {0}, k = 0;
+  for (int step = 128; step >= 1; step /= 2)
+    for (int j = step; j <= 200; j += step)
+      if (!seen[j]) { seen[j] = 1; HALL_ORDER[k++] = j; }
+}
+
 /* The decision of hall_ok_pair_fast (wz_match.cpp:143-168): at every angle, in the
  * reference's expressions, X alone, Y alone, then the pair; reject at the first failure.
  * The angle visiting order of the reference is adaptive but a conjunction does not depend
- * on it, so the natural order 1..200 gives the same decision. */
+ * on it, so any order of all 200 angles gives the same decision (HALL_ORDER here). */
 int or_hall_pair(int n, const int8_t *X, const int8_t *Y, int L, const double *ct,
                  const double *st, double *max_pair, double *min_margin) {
+  pthread_once(&hall_order_once, build_hall_order);
   const int w = n + 1;
   const double limit = 4.0 * n + 2.0;
   const double lim = limit + 0.5;
   int pass = 1;
   double mx = -1.0, mm = 1e300;
-  for (int j = 1; j <= 200; j++) {
+  for (int jj = 0; jj < 200; jj++) {
+    const int j = HALL_ORDER[jj];
     const double *cj = ct + (size_t)j * w, *sj = st + (size_t)j * w;
     double rx = 0, ix = 0, ry = 0, iy = 0;
     for (int i = 0; i < L; i++) { rx += X[i] * cj[i]; ix += X[i] * sj[i]; }
