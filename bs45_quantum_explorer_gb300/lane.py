@@ -195,31 +195,33 @@ def run_lane(ctx, n, sig, skip=0, end=0, shard=0, nshard=1, budget=200000, buf_c
                 res.cells_done += 1
                 res.cells_empty += x["empty"]
             else:
-                for t in range(len(x["words"])):
-                    r = int(x["v"][t]) if t < len(x["v"]) else -1
-                    if r < 0:
-                        raise RuntimeError(f"candidate {t} of a batch was not completed ({r})")
-                    if r == 4:
+                # the batch's verdicts up to and including its first hit, tallied at once
+                v, nd = x["v"], x["nd"]
+                hits = np.flatnonzero(v == 0)
+                stop = int(hits[0]) + 1 if len(hits) else len(x["words"])
+                if len(v) < stop:
+                    raise RuntimeError(f"candidate {len(v)} of a batch was not completed (-1)")
+                seg, segn = v[:stop], nd[:stop]
+                bad = np.flatnonzero((seg < 0) | (seg == 4))
+                if len(bad):
+                    t = int(bad[0])
+                    if seg[t] == 4:
                         raise RuntimeError("completer found a quad whose NPAF recheck failed")
-                    res.completions += 1
-                    res.total_ab_nodes += int(x["nd"][t])
-                    if r >= 2 or r == 0:  # the summary counts the hit as entered too
-                        res.backtracks_entered += 1
-                    if r == 1:
-                        res.pre_filter_rejected += 1
-                    elif r == 2:
-                        res.clean_no_ab += 1
-                    elif r == 3:
-                        res.budget_aborted += 1
-                    elif r == 0:
-                        cw = unpack(x["words"][t:t + 1], n)[0]
-                        res.found, res.hit_idx, res.profile_rank = True, x["cand"], x["pi"]
-                        res.quad = (x["A"][t].copy(), x["B"][t].copy(), cw[0].copy(), cw[1].copy())
-                        res.nodes_this_cand = int(x["nd"][t])
-                        res.candidates_streamed = x["cand"]
-                        found = True
-                        break
-                if found:
+                    raise RuntimeError(f"candidate {t} of a batch was not completed ({int(seg[t])})")
+                res.completions += stop
+                res.total_ab_nodes += int(segn.sum())
+                res.backtracks_entered += int(((seg >= 2) | (seg == 0)).sum())  # the hit too
+                res.pre_filter_rejected += int((seg == 1).sum())
+                res.clean_no_ab += int((seg == 2).sum())
+                res.budget_aborted += int((seg == 3).sum())
+                if len(hits):
+                    t = int(hits[0])
+                    cw = unpack(x["words"][t:t + 1], n)[0]
+                    res.found, res.hit_idx, res.profile_rank = True, x["cand"], x["pi"]
+                    res.quad = (x["A"][t].copy(), x["B"][t].copy(), cw[0].copy(), cw[1].copy())
+                    res.nodes_this_cand = int(segn[t])
+                    res.candidates_streamed = x["cand"]
+                    found = True
                     break
         queue.clear()
         pend.clear()
