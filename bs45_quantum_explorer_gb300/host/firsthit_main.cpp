@@ -9,7 +9,9 @@
 // Not carried over (measurement-only instruments of the reference): FH_TELEM telemetry,
 // HALLSTAT adaptive-order statistics, the A2 shadow (WZ_FH_A2=1; the A2 prune, WZ_FH_A2=2,
 // runs on the device), LOCATE / ORBIT_AUDIT / OUTER_DUMP / TARGET canaries. WZ_FH_CD_PRUNE prunes the device stream as the reference's DFS does (same stream,
-// CDSTAT counts the pruned walk); WZ_FH_HALL_FAST changes no stream and is accepted.
+// CDSTAT counts the pruned walk); WZ_FH_HALL_FAST changes no stream and is accepted, and so is
+// WZ_FH_MID_SOLVE, which changes only the reference's node statistics (the counts here are
+// those without it; verdicts, hits and completion counts are the same either way).
 // WZ_FH_WALL_SEC abandons a cell whose stream finds no survivor for that many seconds (its
 // partial buffer is still drained, and it counts in cells_walled), and SIGTERM raises the
 // context's stop flag, which stops a running stream or completion within one device round.
