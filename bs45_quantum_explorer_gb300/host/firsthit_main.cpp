@@ -129,14 +129,17 @@ int main(int argc, char **argv) {
   if (n1 > 64) { std::cerr << "ERROR: bs_firsthit supports n <= 63\n"; return 1; }
   bool thm211b = env("WZ_THM211B") != nullptr, thm212 = env("WZ_THM212") != nullptr;
   const bool endpos = env_on("WZ_FH_ENDPOS");
-  const int outer_k = env_i("WZ_FH_OUTER_K", 3);
+  // the reference applies its outer-lag tables only for K >= 2 (wz_match.cpp:602-603): any
+  // smaller K runs without them, as K = 0 does; K > 3 has no table and is refused below
+  const int outer_k_env = env_i("WZ_FH_OUTER_K", 3);  // printed as given
+  const int outer_k = outer_k_env < 2 ? 0 : outer_k_env;
   const int a2_mode = env_i("WZ_FH_A2", 0);
   if (a2_mode != 0 && a2_mode != 2) {
     printf("RESULT: WZ_FH_A2=%d (the A2 shadow instrument) is not built on the GPU lane — refusing\n", a2_mode);
     return 2;
   }
-  if (outer_k != 0 && outer_k != 2 && outer_k != 3) {
-    printf("RESULT: WZ_FH_OUTER_K must be 0, 2 or 3\n");
+  if (outer_k > 3) {
+    printf("RESULT: WZ_FH_OUTER_K must be at most 3\n");
     return 2;
   }
   const bool cand_log = env_on("WZ_FH_CAND_LOG");
@@ -379,7 +382,7 @@ int main(int argc, char **argv) {
       return 3;
     }
     if (rc) return fail_gpu(rc, "bs_complete_ab_batch");
-    printf("COMPLETE_ONLY r=%d nodes=%lld budget=%lld outer_k=%d a2=%d sec=%g\n", v, nd, budget, outer_k, a2_mode,
+    printf("COMPLETE_ONLY r=%d nodes=%lld budget=%lld outer_k=%d a2=%d sec=%g\n", v, nd, budget, outer_k_env, a2_mode,
            secs_since(t0c));
     if (v == 0) {
       std::vector<int> A(n1), B(n1);
