@@ -6,7 +6,9 @@ checkpoint IGNORED (<forged> != <CFGSIG>)` line, so a checkpoint written by eith
 on the other exactly when the reference would resume it. The `[firsthit] profiles=` and
 `[abprof]` lines (list size, settings, allowed-row counts) are compared too. All of this runs
 before the binary opens its GPU context; the search that follows needs the GPU and is checked
-by the -m gpu lane tests (checkpoint bytes included)."""
+by the -m gpu lane tests (checkpoint bytes included). The cases include one arm of the
+reference's first n = 44 and n = 45 production lanes with the environment its lane driver
+gives it (the manifest's digest is expected, and matches)."""
 import json
 import os
 import re
@@ -21,7 +23,7 @@ def test_lane_binary_cfgsig_matches_reference(built_lib):
     from bs45_quantum_explorer_gb300.build import build_host
     exe = build_host()
     cases = json.load(open(os.path.join(HERE, "golden", "cfgsig_golden.json")))
-    assert len(cases) >= 15
+    assert len(cases) >= 20 and sum("PRODUCTION" in c["settings"] for c in cases) == 2
     suffixes = set()
     for c in cases:
         want = c["lines"]

@@ -42,3 +42,29 @@ def test_plan_refuses_even_arm_counts_and_builds_arm_env():
     assert env["WZ_FH_PROF_SKIP"] == "2" and env["WZ_FH_PROF_END"] == str(min(4, cls["windows"]))
     assert env["WZ_FH_STREAM_REV"] == "1" and env["WZ_FH_EXPECT_DIGEST"] == cls["digest"]
     assert env["WZ_FH_CKPT_DIR"] == "/ck" and env["WZ_FH_PROF_ORDER"] == "3"
+
+
+def _production():
+    g = json.load(open(os.path.join(HERE, "golden", "production_manifest_golden.json")))
+    return [(p, c) for p in g for c in p["classes"]]
+
+
+# Six of the 22 production classes run by default (about 5 s each); BS_ALL_PRODUCTION=1 runs
+# all of them (about two minutes on 8 host threads).
+PRODUCTION_SAMPLE = (0, 5, 11, 12, 17, 21)
+
+
+@pytest.mark.parametrize("i", range(22))
+def test_plan_matches_reference_production_manifest(i):
+    """The reference's own production manifests (Pass H, n = 44 and n = 45, from its planner's
+    list-only solver runs; tests/golden/production_manifest_golden.json): the same raw and
+    kept cell counts, windows, list:kept digest and lanes for each class."""
+    from bs45_quantum_explorer_gb300.manifest import plan_class
+    cases = _production()
+    assert len(cases) == 22
+    if i not in PRODUCTION_SAMPLE and not os.environ.get("BS_ALL_PRODUCTION"):
+        pytest.skip("sampled: BS_ALL_PRODUCTION=1 runs every class")
+    p, c = cases[i]
+    got = plan_class(p["n"], tuple(c["sig"]), c["S"], p["narms"], endpos=p["endpos"])
+    for k in ("cells", "kept", "windows", "digest", "lanes"):
+        assert got[k] == c[k], (c["sig"], k)
