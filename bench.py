@@ -392,6 +392,15 @@ def run_first_hit(seconds, cpu_seconds=10.0, with_cpu=True, drain_top=50000, tun
     return out
 
 
+def guarded(fn, *a, **kw):
+    """One extra leg of the default run: an exception in it is reported in its place, so the
+    headline line (measured before the extras) is still printed."""
+    try:
+        return fn(*a, **kw)
+    except Exception as e:  # noqa: BLE001 - any failure of an extra leg
+        return {"error": f"{type(e).__name__}: {e}"}
+
+
 def run_spike(budget=1 << 20, ncand=2048):
     """The reference's own GPU completer (src/solver/gpu/fh_gpu_spike.cu, compiled unmodified
     for sm_103a into oracle/_ref/fh_gpu_spike) beside ours on the same candidates: the first
@@ -1012,13 +1021,15 @@ def main():
                 "same_as_50000_prefix": bool(np.array_equal(surv_c, surv[:CMP_LIMIT]))},
         }
         if not args.no_cpu_baseline:
-            line["search"]["cpu_baseline"] = cpu_search_rate(os.cpu_count() or 1, cell42)
+            line["search"]["cpu_baseline"] = guarded(cpu_search_rate, os.cpu_count() or 1, cell42)
         # ---- the n = 36 first-hit lane (bounded) and the serving mix ----
-        line["first_hit"] = run_first_hit(args.fh_seconds, with_cpu=not args.no_cpu_baseline)
+        line["first_hit"] = guarded(run_first_hit, args.fh_seconds,
+                                    with_cpu=not args.no_cpu_baseline)
         # ranges of 1..256 cells here so that the default run ends in minutes; `--serve`
         # runs the stated 1..4096
-        line["serving"] = run_serving(max_cells=256, ref_seconds=0.0 if args.no_cpu_baseline else 45.0)
-        line["completer_vs_reference_gpu_spike"] = run_spike()
+        line["serving"] = guarded(run_serving, max_cells=256,
+                                  ref_seconds=0.0 if args.no_cpu_baseline else 45.0)
+        line["completer_vs_reference_gpu_spike"] = guarded(run_spike)
         if not args.no_cpu_baseline:
             ncpu = os.cpu_count() or 1
             words = d_words.cpu().numpy().view(np.uint64).reshape(-1, 2)
