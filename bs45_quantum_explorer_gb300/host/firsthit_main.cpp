@@ -509,7 +509,13 @@ int main(int argc, char **argv) {
     auto handle_result = [&](const int *Ci, const int *Di, int r, long long nodes, const int8_t *A8,
                              const int8_t *B8, long long rank) {
       if (r == 4 || (r == 0 && test_ierr)) {
-        printf("FH_INTERNAL_ERROR: completer FOUND but NPAF recheck failed\n");
+        // the first shift whose NPAF is not zero (under the test hook, the first shift), as
+        // the reference's check names it (wz_match.cpp:1328-1335)
+        int A[64], B[64], bad = 1;
+        for (int i = 0; i < n1; i++) { A[i] = A8[i]; B[i] = B8[i]; }
+        if (!test_ierr)
+          while (bad < n && npaf_at(A, B, n1, Ci, Di, n, bad) == 0) bad++;
+        printf("FH_INTERNAL_ERROR: completer FOUND but NPAF[%d] != 0\n", bad);
         printf("RESULT: INTERNAL ERROR at candidate idx=%lld pi=%lld — arm stopped, candidate NOT marked attempted, checkpoint NOT advanced\n",
                cand, pi);
         fflush(stdout);
