@@ -70,7 +70,7 @@ CASES = [
 
 # The production lanes' arms (the reference's Pass H submissions, docs/plans/passh_submit_fir.txt
 # and passh45_submit_fir.txt, through cluster_firsthit_probe.sh): the first line of each, as
-# arm 1 of its lane with an empty per-arm WZ_FH_SCORE_MAX (the driver's ungated tier).
+# arm 1 of its lane with an empty per-arm WZ_FH_SCORE_MAX (the lane driver's ungated tier).
 SUBMITS = (("docs/plans/passh_submit_fir.txt", 44), ("docs/plans/passh45_submit_fir.txt", 45))
 DRIVER_EXPORTS = ("WZ_FH_AB_BUDGET", "WZ_FH_PROF_ORDER", "WZ_FH_SCORE_MAX", "WZ_FH_STREAM_TOTAL",
                   "WZ_FH_PROF_SKIP", "WZ_FH_AB_PROF", "WZ_FH_RESUME", "WZ_FH_BUF_CAP",
