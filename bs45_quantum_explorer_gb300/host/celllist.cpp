@@ -34,6 +34,37 @@ static int parallel_parts(size_t n, F f, size_t min_per_part = 256) {
   return (int)parts;
 }
 
+// std::sort on all host threads: contiguous parts sorted at once, then merged pairwise. The
+// result is sorted by `cmp`; elements that compare equal may come out in another order than a
+// serial std::sort would leave them (callers sort by keys that are distinct, or do not
+// depend on the order of ties).
+template <class T, class Cmp>
+static void parallel_sort(std::vector<T> &v, Cmp cmp) {
+  const size_t n = v.size();
+  const unsigned hw = std::thread::hardware_concurrency();
+  size_t parts = 1;
+  while (parts * 2 <= std::min<size_t>(hw ? hw : 1, 64)) parts *= 2;
+  if (parts <= 1 || n < ((size_t)1 << 16)) {
+    std::sort(v.begin(), v.end(), cmp);
+    return;
+  }
+  std::vector<size_t> b(parts + 1);
+  for (size_t i = 0; i <= parts; i++) b[i] = n * i / parts;
+  std::vector<std::thread> th;
+  for (size_t i = 0; i < parts; i++)
+    th.emplace_back([&, i] { std::sort(v.begin() + b[i], v.begin() + b[i + 1], cmp); });
+  for (auto &x : th) x.join();
+  for (size_t w = 1; w < parts; w *= 2) {
+    th.clear();
+    for (size_t i = 0; i + w < parts; i += 2 * w)
+      th.emplace_back([&, i, w] {
+        std::inplace_merge(v.begin() + b[i], v.begin() + b[i + w],
+                           v.begin() + b[std::min(i + 2 * w, parts)], cmp);
+      });
+    for (auto &x : th) x.join();
+  }
+}
+
 int class_count(int L, int c, int m) {
   int k = 0;
   for (int p = c; p < L; p += m) k++;
@@ -112,36 +143,85 @@ bool thm212_ok(const Vec &x, const Vec &y, int m, int n, bool abSide) {
   return true;
 }
 
+// The set of norm(k) + norm(r) <= 4n+2 over every (k, r) pair depends only on the distinct
+// norms on each side, so the pairs are taken over those.
 void NormSet::build(int L, int a, int b, int m, int n) {
   const auto K = enum_class_sums(L, a, m), R = enum_class_sums(L, b, m);
   const int tgt = 4 * n + 2;
-  std::vector<int> rn(R.size());
-  for (size_t j = 0; j < R.size(); j++) rn[j] = norm_vec(R[j]);
+  std::vector<char> kn(tgt + 1, 0), rn(tgt + 1, 0);
   for (const auto &kv : K) {
-    const int kn = norm_vec(kv);
-    if (kn > tgt) continue;
-    for (int r : rn)
-      if (kn + r <= tgt) vals.insert(kn + r);
+    const int v = norm_vec(kv);
+    if (v <= tgt) kn[v] = 1;
   }
+  for (const auto &rv : R) {
+    const int v = norm_vec(rv);
+    if (v <= tgt) rn[v] = 1;
+  }
+  vals.assign(tgt + 1, 0);
+  for (int x = 0; x <= tgt; x++)
+    if (kn[x])
+      for (int y = 0; x + y <= tgt; y++)
+        if (rn[y]) vals[x + y] = 1;
 }
 
+// One side's share of pair_auto at shift s: pair_auto(x, y, s) = side_auto(x, s) + side_auto(y, s).
+static inline int side_auto(const Vec &v, int s) {
+  return autocorr_vec(v, s) + autocorr_vec(v, (int)v.size() - s);
+}
+
+namespace {
+// What a class-sum vector contributes to a (k, r) pair's 2.11b key and 2.12 test: its norm,
+// its shares of the residue autocorrelations, and its entries mod 4 (thm212_ok reads sums of
+// entries mod 4 only). Vectors with equal features give equal keys and verdicts in every pair.
+struct SideFeat {
+  int norm;
+  int ca[3];
+  uint32_t mod4;  // two bits per entry
+  bool operator==(const SideFeat &o) const {
+    return norm == o.norm && ca[0] == o.ca[0] && ca[1] == o.ca[1] && ca[2] == o.ca[2] && mod4 == o.mod4;
+  }
+};
+struct SideFeatHash {
+  size_t operator()(const SideFeat &f) const {
+    uint64_t h = (uint64_t)(uint32_t)f.norm * 0x9E3779B97F4A7C15ULL;
+    for (int v : f.ca) h = (h ^ (uint32_t)v) * 0xBF58476D1CE4E5B9ULL;
+    return (size_t)((h ^ f.mod4) * 0x94D049BB133111EBULL);
+  }
+};
+// The distinct features of `vs` (norm <= tgt), each with the first vector that has them.
+std::vector<std::pair<SideFeat, const Vec *>> distinct_features(const std::vector<Vec> &vs, int half,
+                                                                int tgt) {
+  std::unordered_set<SideFeat, SideFeatHash> seen;
+  std::vector<std::pair<SideFeat, const Vec *>> out;
+  for (const Vec &v : vs) {
+    SideFeat f{norm_vec(v), {0, 0, 0}, 0};
+    if (f.norm > tgt) continue;
+    for (int s = 1; s <= half && s <= 3; s++) f.ca[s - 1] = side_auto(v, s);
+    for (size_t c = 0; c < v.size(); c++) f.mod4 |= (uint32_t)(((v[c] % 4) + 4) % 4) << (2 * c);
+    if (seen.insert(f).second) out.push_back({f, &v});
+  }
+  return out;
+}
+}  // namespace
+
+// Every key auto_key(T(k, r), norm(k) + norm(r)) over the (k, r) pairs that pass, taken over
+// the distinct features of each side (the key set is the same as over all pairs).
 void AutoSet::build(int L, int a, int b, int m, int n, bool thm212) {
   const auto K = enum_class_sums(L, a, m), R = enum_class_sums(L, b, m);
   const int tgt = 4 * n + 2, half = m / 2;
   const bool abSide = (L == n + 1);
+  const auto FK = distinct_features(K, half, tgt), FR = distinct_features(R, half, tgt);
   std::vector<std::unordered_set<uint64_t>> part(64);
-  parallel_parts(K.size(), [&](size_t lo, size_t hi, size_t t) {
+  parallel_parts(FK.size(), [&](size_t lo, size_t hi, size_t t) {
     Vec T(half);
     for (size_t i = lo; i < hi; i++) {
-      const Vec &kv = K[i];
-      const int kn = norm_vec(kv);
-      if (kn > tgt) continue;
-      for (const auto &rv : R) {
-        const int rn = norm_vec(rv);
-        if (kn + rn > tgt) continue;
-        if (thm212 && !thm212_ok(kv, rv, m, n, abSide)) continue;
-        for (int s = 1; s <= half; s++) T[s - 1] = pair_auto(kv, rv, s);
-        part[t].insert(auto_key(T, kn + rn));
+      const SideFeat &fk = FK[i].first;
+      for (const auto &r : FR) {
+        const SideFeat &fr = r.first;
+        if (fk.norm + fr.norm > tgt) continue;
+        if (thm212 && !thm212_ok(*FK[i].second, *r.second, m, n, abSide)) continue;
+        for (int s = 1; s <= half && s <= 3; s++) T[s - 1] = fk.ca[s - 1] + fr.ca[s - 1];
+        part[t].insert(auto_key(T, fk.norm + fr.norm));
       }
     }
   }, 16);
@@ -157,33 +237,50 @@ std::vector<Profile> survive_profiles3(int L, int sigX, int sigY, int n, const N
   const bool abSide = (L == n + 1);
   const auto PX3 = enum_class_sums(L, sigX, 3), PY3 = enum_class_sums(L, sigY, 3);
   const auto PX6 = enum_class_sums(L, sigX, 6), PY6 = enum_class_sums(L, sigY, 6);
-  std::vector<Vec> PX6r(PX6.size()), PY6r(PY6.size());
-  for (size_t i = 0; i < PX6.size(); i++) PX6r[i] = reduce63(PX6[i]);
-  for (size_t i = 0; i < PY6.size(); i++) PY6r[i] = reduce63(PY6[i]);
+  // the mod-6 refinements of each mod-3 vector, in enumeration order, with their norms and
+  // residue-autocorrelation shares (the existential search below visits only these)
+  std::unordered_map<std::string, std::vector<size_t>> x_of, y_of;
+  for (size_t i = 0; i < PX6.size(); i++) x_of[cell_key(reduce63(PX6[i]), Vec())].push_back(i);
+  for (size_t j = 0; j < PY6.size(); j++) y_of[cell_key(reduce63(PY6[j]), Vec())].push_back(j);
+  auto shares = [](const std::vector<Vec> &V, std::vector<int> &nv, std::vector<int> &ca) {
+    nv.resize(V.size());
+    ca.resize(3 * V.size());
+    for (size_t i = 0; i < V.size(); i++) {
+      nv[i] = norm_vec(V[i]);
+      for (int s = 1; s <= 3; s++) ca[3 * i + s - 1] = side_auto(V[i], s);
+    }
+  };
+  std::vector<int> nx6, cax6, ny6, cay6;
+  shares(PX6, nx6, cax6);
+  shares(PY6, ny6, cay6);
+  static const std::vector<size_t> none;
   std::vector<std::vector<Profile>> part(64);
   parallel_parts(PX3.size(), [&](size_t lo, size_t hi, size_t t) {
   std::vector<Profile> &out = part[t];
+  Vec needT(3);
   for (size_t ix = lo; ix < hi; ix++) {
     const Vec &px = PX3[ix];
     const int npx = norm_vec(px);
     if (npx > tgt) continue;
+    auto xi = x_of.find(cell_key(px, Vec()));
+    const std::vector<size_t> &xs = xi == x_of.end() ? none : xi->second;
     for (const auto &py : PY3) {
       const int need = tgt - npx - norm_vec(py);
       if (need < 0 || !comp3.has(need)) continue;
       if (thm212 && !thm212_ok(px, py, 3, n, abSide)) continue;
+      auto yi = y_of.find(cell_key(py, Vec()));
+      const std::vector<size_t> &ys = yi == y_of.end() ? none : yi->second;
       bool ok6 = false;
-      for (size_t i = 0; i < PX6.size() && !ok6; i++) {
-        if (PX6r[i] != px) continue;
-        const int npx6 = norm_vec(PX6[i]);
+      for (size_t ii = 0; ii < xs.size() && !ok6; ii++) {
+        const size_t i = xs[ii];
+        const int npx6 = nx6[i];
         if (npx6 > tgt) continue;
-        for (size_t j = 0; j < PY6.size(); j++) {
-          if (PY6r[j] != py) continue;
-          const int need6 = tgt - npx6 - norm_vec(PY6[j]);
+        for (size_t j : ys) {
+          const int need6 = tgt - npx6 - ny6[j];
           if (need6 < 0) continue;
           if (thm212 && !thm212_ok(PX6[i], PY6[j], 6, n, abSide)) continue;
           if (thm211b && comp6auto) {
-            Vec needT(3);
-            for (int s = 1; s <= 3; s++) needT[s - 1] = -pair_auto(PX6[i], PY6[j], s);
+            for (int s = 0; s < 3; s++) needT[s] = -(cax6[3 * i + s] + cay6[3 * j + s]);
             if (comp6auto->has(needT, need6)) { ok6 = true; break; }
           } else if (comp6.has(need6)) {
             ok6 = true;
@@ -206,20 +303,24 @@ std::vector<Profile> survive_profiles6(int L, int sigX, int sigY, int n, const N
   const int tgt = 4 * n + 2;
   const bool abSide = (L == n + 1);
   const auto PX = enum_class_sums(L, sigX, 6), PY = enum_class_sums(L, sigY, 6);
-  std::vector<int> npy(PY.size()), npy3(PY.size());
+  std::vector<int> npy(PY.size()), npy3(PY.size()), cay(3 * PY.size());
   for (size_t j = 0; j < PY.size(); j++) {
     npy[j] = norm_vec(PY[j]);
     npy3[j] = norm_vec(reduce63(PY[j]));
+    for (int s = 1; s <= 3; s++) cay[3 * j + s - 1] = side_auto(PY[j], s);
   }
   std::vector<std::vector<Profile>> part(64);
   parallel_parts(PX.size(), [&](size_t lo, size_t hi, size_t t) {
     std::vector<Profile> &out = part[t];
+    Vec needT(3);
     for (size_t ix = lo; ix < hi && out.size() < cap; ix++) {
       const Vec &px = PX[ix];
       const int npx = norm_vec(px);
       if (npx > tgt) continue;
       const int npx3 = norm_vec(reduce63(px));
       if (npx3 > tgt) continue;
+      int cax[3];
+      for (int s = 1; s <= 3; s++) cax[s - 1] = side_auto(px, s);
       for (size_t j = 0; j < PY.size(); j++) {
         const auto &py = PY[j];
         const int need = tgt - npx - npy[j];
@@ -228,8 +329,7 @@ std::vector<Profile> survive_profiles6(int L, int sigX, int sigY, int n, const N
         const int need3 = tgt - npx3 - npy3[j];
         if (need3 < 0 || !comp3.has(need3)) continue;
         if (thm211b && comp6auto) {
-          Vec needT(3);
-          for (int s = 1; s <= 3; s++) needT[s - 1] = -pair_auto(px, py, s);
+          for (int s = 0; s < 3; s++) needT[s] = -(cax[s] + cay[3 * j + s]);
           if (!comp6auto->has(needT, need)) continue;
         }
         out.push_back({px, py});
@@ -341,19 +441,38 @@ static inline void quad_switch(int *px, int *py, int m, int n) {
 }
 
 // Smallest key over the orbit of (px, py): negations, reversals, the swap, and with 64
-// variants also the quad switch, applied in the order of wz_match.cpp:1721-1730.
+// variants also the quad switch, applied in the order of wz_match.cpp:1721-1730 (variant bit
+// 32 the quad switch first, then bits 1 / 2 negate px / py, bits 4 / 8 reverse them, bit 16
+// swaps them in the key). A negation or reversal acts on one side only and the two commute,
+// so each side's four forms are packed once (one byte per class, as CellKeyOrder::pack packs a
+// side) and every variant's key is two packed halves.
 static u128 orbit_id(const int *px0, const int *py0, int m, int n, int nvar, const CellKeyOrder &ko) {
+  auto halves = [&](const int *v, uint64_t h[4]) {  // [neg | 2 * rev]
+    int r[8];
+    rev_classes(v, r, m, n);
+    for (int f = 0; f < 4; f++) {
+      const int *src = (f & 2) ? r : v;
+      const int sg = (f & 1) ? -1 : 1;
+      uint64_t k = 0;
+      for (int c = 0; c < m; c++) k = (k << 8) | ko.rank[(sg * src[c] + 128) & 255];
+      h[f] = k;
+    }
+  };
   u128 best = ~(u128)0;
-  for (int var = 0; var < nvar; var++) {
-    int px[8], py[8], t[8];
-    for (int c = 0; c < m; c++) { px[c] = px0[c]; py[c] = py0[c]; }
-    if (var & 32) quad_switch(px, py, m, n);
-    if (var & 1) for (int c = 0; c < m; c++) px[c] = -px[c];
-    if (var & 2) for (int c = 0; c < m; c++) py[c] = -py[c];
-    if (var & 4) { rev_classes(px, t, m, n); for (int c = 0; c < m; c++) px[c] = t[c]; }
-    if (var & 8) { rev_classes(py, t, m, n); for (int c = 0; c < m; c++) py[c] = t[c]; }
-    const u128 k = (var & 16) ? ko.pack(py, px, m) : ko.pack(px, py, m);
-    if (k < best) best = k;
+  int bx[8], by[8];
+  for (int c = 0; c < m; c++) { bx[c] = px0[c]; by[c] = py0[c]; }
+  for (int base = 0; base < (nvar > 32 ? 2 : 1); base++) {
+    if (base) quad_switch(bx, by, m, n);
+    uint64_t hx[4], hy[4];
+    halves(bx, hx);
+    halves(by, hy);
+    for (int fx = 0; fx < 4; fx++)
+      for (int fy = 0; fy < 4; fy++) {
+        const u128 a = ((u128)hx[fx] << (8 * m)) | hy[fy];  // (px, py)
+        const u128 b = ((u128)hy[fy] << (8 * m)) | hx[fx];  // swapped
+        if (a < best) best = a;
+        if (b < best) best = b;
+      }
   }
   return best;
 }
@@ -457,7 +576,7 @@ int build_cell_list(int n, int SA, int SB, int SC, int SD, const ListOptions &op
   // group the cells by orbit; the orbit's representative is its smallest own key
   std::vector<uint32_t> by_orbit(N);
   for (size_t i = 0; i < N; i++) by_orbit[i] = (uint32_t)i;
-  std::sort(by_orbit.begin(), by_orbit.end(), [&](uint32_t x, uint32_t y) {
+  parallel_sort(by_orbit, [&](uint32_t x, uint32_t y) {
     if (oid[x] != oid[y]) return oid[x] < oid[y];
     return own[x] < own[y];
   });
@@ -480,7 +599,7 @@ int build_cell_list(int n, int SA, int SB, int SC, int SD, const ListOptions &op
       // Q-closure orbit elimination, wz_match.cpp:1745-1802
       out.qp_active = true;
       std::vector<u128> S(own);
-      std::sort(S.begin(), S.end());
+      parallel_sort(S, [](const u128 &x, const u128 &y) { return x < y; });
       int ccnt[8];
       for (int c = 0; c < m; c++) ccnt[c] = class_count(n, c, m);
       auto realizable = [&](const int *p) {
@@ -586,10 +705,17 @@ int build_cell_list(int n, int SA, int SB, int SC, int SD, const ListOptions &op
     cells.swap(sorted);
     out.kept.swap(skept);
   }
+  // the list digest hashes every cell key in list order: the keys of contiguous parts are
+  // formed on all host threads, then hashed one part after the other
+  std::vector<std::string> keys_of(64);
+  parallel_parts(N, [&](size_t lo, size_t hi, size_t t) {
+    std::string &k = keys_of[t];
+    for (size_t i = lo; i < hi; i++) k += cell_key(cells[i].px, cells[i].py);
+  }, 4096);
   uint64_t dl = 1469598103934665603ULL, dk = 1469598103934665603ULL;
+  for (const std::string &k : keys_of) dl = fnv_str(dl, k);
   long long kept_n = 0;
   for (size_t i = 0; i < N; i++) {
-    dl = fnv_str(dl, cell_key(cells[i].px, cells[i].py));
     kept_n += out.kept[i];
     dk = fnv_str(dk, out.kept[i] ? "1" : "0");
   }

@@ -41,9 +41,9 @@ bool thm212_ok(const Vec &x, const Vec &y, int m, int n, bool abSide);
 
 // Achievable norm(K)+norm(R) of one side (2.11a), wz_match.cpp:233-249.
 struct NormSet {
-  std::unordered_set<int> vals;
+  std::vector<char> vals;  // vals[v] != 0: v is achievable (0 <= v <= 4n+2)
   void build(int L, int a, int b, int m, int n);
-  bool has(int need) const { return vals.count(need) != 0; }
+  bool has(int need) const { return need >= 0 && (size_t)need < vals.size() && vals[need]; }
 };
 
 // Achievable (2.11b tuple, norm) keys of one side, wz_match.cpp:324-350.
