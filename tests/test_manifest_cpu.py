@@ -49,11 +49,6 @@ def _production():
     return [(p, c) for p in g for c in p["classes"]]
 
 
-# Six of the 22 production classes run by default (about 5 s each); BS_ALL_PRODUCTION=1 runs
-# all of them (about two minutes on 8 host threads).
-PRODUCTION_SAMPLE = (0, 5, 11, 12, 17, 21)
-
-
 @pytest.mark.parametrize("i", range(22))
 def test_plan_matches_reference_production_manifest(i):
     """The reference's own production manifests (Pass H, n = 44 and n = 45, from its planner's
@@ -62,8 +57,6 @@ def test_plan_matches_reference_production_manifest(i):
     from bs45_quantum_explorer_gb300.manifest import plan_class
     cases = _production()
     assert len(cases) == 22
-    if i not in PRODUCTION_SAMPLE and not os.environ.get("BS_ALL_PRODUCTION"):
-        pytest.skip("sampled: BS_ALL_PRODUCTION=1 runs every class")
     p, c = cases[i]
     got = plan_class(p["n"], tuple(c["sig"]), c["S"], p["narms"], endpos=p["endpos"])
     for k in ("cells", "kept", "windows", "digest", "lanes"):
