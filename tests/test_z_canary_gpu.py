@@ -4,7 +4,8 @@ against the reference's own run of it (tests/golden/canary_n29_golden.json): exi
 semantic lines (FIRSTHIT idx=26694 profile_rank=588, the summary counts, the quad), per raw cell
 the completions, verdicts and charged nodes, and the hit cell's drain sequence with
 WZ_FH_CAND_LOG on; and the hit cell alone with the outer-lag tables and the early check off,
-where nodes_this_cand is the archived 81,320."""
+where nodes_this_cand is the archived 81,320. (The file name has it collected after the other
+lane tests and before the allocation-free filter's test, which is collected last.)"""
 import json
 import os
 import sys
