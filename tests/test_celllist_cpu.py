@@ -82,6 +82,32 @@ def test_cell_list_longer_than_its_first_buffer(built_lib, monkeypatch):
         C.string_at(C.addressof(cells), C.sizeof(cells))
 
 
+def test_cell_list_kept_after_a_short_buffer_serves_only_its_own_request(built_lib, monkeypatch):
+    """The list a short-buffer call built is handed to the same request made again with room
+    for it, never to another request; a request made in between gets its own list."""
+    import bs45_quantum_explorer_gb300.cells as cl
+    kw = dict(m6=True, orbit_canon=True, orbit_q=1, prof_order=3)
+    a, b = (17, _sigs(17)[0]), (17, _sigs(17)[1])
+    want_a, want_b = cl.cell_list(*a, **kw), cl.cell_list(*b, **kw)
+    assert want_a[2] != want_b[2]
+    monkeypatch.setattr(cl, "LIST_GUESS", 8)
+    lib = cl.lib()
+    o = cl.ListOpts(m6=1, thm211b=0, thm212=0, endpos=0, orbit_canon=1, orbit_q=1, qprune=0,
+                    prof_order=3, nshard=1)
+    ncells = cl.C.c_longlong(0)
+    # a short call for a, then a whole call for b: b is built, not served a's list
+    assert lib.bs_cell_list(17, *a[1], cl.C.byref(o), None, None, 1, cl.C.byref(ncells),
+                            None) == cl.BS_ERR_CAP
+    got_b = cl.cell_list(*b, **kw)
+    assert got_b[2] == want_b[2] and np.array_equal(got_b[1], want_b[1])
+    # a again, short twice, then whole: the same list as a single build
+    for _ in range(2):
+        assert lib.bs_cell_list(17, *a[1], cl.C.byref(o), None, None, 1, cl.C.byref(ncells),
+                                None) == cl.BS_ERR_CAP
+    got_a = cl.cell_list(*a, **kw)
+    assert got_a[2] == want_a[2] and np.array_equal(got_a[1], want_a[1])
+
+
 def _sigs(n):
     from make_golden import classes
     return [tuple(s) for s in classes(n)]
