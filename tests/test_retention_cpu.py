@@ -7,8 +7,8 @@ reference's results/champions and results/reference), the cell of its C,D (class
 is looked up in the list bs_cell_list builds for its class with the production settings:
 mod-6 cells, Thm 2.11b and 2.12, orbit canon with the quad switch Q where it is proven safe,
 the Q-closure prune and ORDER=3, with WZ_FH_ENDPOS at odd n as the reference's n = 45 lanes
-run. Retained means that some cell of the solution's orbit (the 32 or 64 variants the
-reference's canonicalisation ranges over, wz_match.cpp:1714-1730) is in the list and kept.
+run. Retained means that some cell of the solution's orbit (under the 32- or 64-element group
+the reference's canonicalisation uses, wz_match.cpp:1714-1730) is in the list and kept.
 At odd n the solution's endpoint quad is positive, as ENDPOS requires."""
 import json
 import os
@@ -21,42 +21,39 @@ def _class_sums(x, m):
 
 
 def _rev(p, n, m):
-    """Class c of the reversed sequence is class (n-1-c) mod m of the original."""
-    q = [0] * m
-    for c in range(m):
-        q[(n - 1 - c) % m] = p[c]
-    return q
+    """Class sums of the reversed sequence: position i goes to n-1-i, so class c goes to class
+    (n-1-c) mod m."""
+    return tuple(p[(n - 1 - c) % m] for c in range(m))
 
 
 def _quad_switch(px, py, n, m):
-    """Q(C,D) = (U+RV, U-RV), U = (C+D)/2, V = (C-D)/2, on class sums (always integral)."""
+    """The quad switch on class sums: with U = (C+D)/2 and V = (C-D)/2 it maps (C, D) to
+    (U + rev V, U - rev V); on class sums the halves are always whole numbers."""
     rx, ry = _rev(px, n, m), _rev(py, n, m)
-    sx = [px[c] + py[c] + rx[c] - ry[c] for c in range(m)]
-    sy = [px[c] + py[c] - rx[c] + ry[c] for c in range(m)]
-    assert all(v % 2 == 0 for v in sx + sy)
-    return [v // 2 for v in sx], [v // 2 for v in sy]
+    two_x = [px[c] + py[c] + rx[c] - ry[c] for c in range(m)]
+    two_y = [px[c] + py[c] - rx[c] + ry[c] for c in range(m)]
+    assert all(v % 2 == 0 for v in two_x + two_y)
+    return tuple(v // 2 for v in two_x), tuple(v // 2 for v in two_y)
 
 
 def _orbit(px0, py0, n, m, nvar):
-    """The cells the reference's orbit id ranges over: variant bits 32 (Q first), 1 / 2 negate
-    px / py, 4 / 8 reverse them, 16 swaps them."""
-    out = set()
-    for var in range(nvar):
-        px, py = list(px0), list(py0)
-        if var & 32:
-            px, py = _quad_switch(px, py, n, m)
-        if var & 1:
-            px = [-v for v in px]
-        if var & 2:
-            py = [-v for v in py]
-        if var & 4:
-            px = _rev(px, n, m)
-        if var & 8:
-            py = _rev(py, n, m)
-        if var & 16:
-            px, py = py, px
-        out.add((tuple(px), tuple(py)))
-    return out
+    """The orbit of a cell under the lane's symmetry group: negating either side, reversing
+    either side, swapping the sides, and (nvar = 64) the quad switch. Built as the closure
+    under those generators; it equals the set of 32 or 64 variants the reference's
+    canonicalisation ranges over (wz_match.cpp:1714-1730)."""
+    start = (tuple(px0), tuple(py0))
+    seen, todo = {start}, [start]
+    while todo:
+        x, y = todo.pop()
+        images = [(tuple(-v for v in x), y), (x, tuple(-v for v in y)),
+                  (_rev(x, n, m), y), (x, _rev(y, n, m)), (y, x)]
+        if nvar == 64:
+            images.append(_quad_switch(x, y, n, m))
+        for im in images:
+            if im not in seen:
+                seen.add(im)
+                todo.append(im)
+    return seen
 
 
 def test_known_solutions_are_retained_by_the_lane_list(built_lib):

@@ -2,9 +2,9 @@
 tools/test_orbit_q_retention.py, which brute-forces every BS(n+1, n) at n = 6, 8, 10 and asks
 its LOCATE instrument whether some image of each solution lies in a kept cell).
 
-Here the solutions come from the same brute force, restated (every C,D pair's summed
-aperiodic autocorrelation against the negated vectors of every A,B pair), one per
-(signed A,B sums, 64-orbit of C,D). For each, with mod-3 and mod-6 cells, 2.11b and 2.12, orbit
+Here every solution comes from a brute force of our own: every unordered C,D pair whose
+summed aperiodic autocorrelation (packed exactly into one integer) is the negation of some
+unordered A,B pair's. For each, with mod-3 and mod-6 cells, 2.11b and 2.12, orbit
 canon, and the 32-group, the 64-group (Q, where the reference enables it: c + d = 0 mod 4)
 and Q with the closure prune, the list bs_cell_list builds for the solution's own signed
 signature must hold the solution's cell, and some cell of its orbit must be kept."""
@@ -14,72 +14,56 @@ import numpy as np
 import pytest
 
 
-def _all_seqs(L):
-    idx = np.arange(1 << L, dtype=np.int64)[:, None]
-    return (1 - 2 * ((idx >> np.arange(L)) & 1)).astype(np.int8)
+def _seqs(L):
+    """Every +-1 sequence of length L, one per row."""
+    return np.array(list(itertools.product((1, -1), repeat=L)), dtype=np.int8)
 
 
-def _acf(X, n):
-    L = X.shape[1]
-    return np.stack([(X[:, :L - s].astype(np.int32) * X[:, s:]).sum(1) if s < L
-                     else np.zeros(len(X), np.int32) for s in range(1, n + 1)], 1).astype(np.int32)
+def _keys(X, Y, n, negate=False):
+    """For every pair (X[i], Y[i]), its summed aperiodic autocorrelation at shifts 1..n (values
+    within +-2(n+1)) packed exactly into one int64, negated first when asked."""
+    base, off = 4 * n + 9, 2 * n + 4
+    key = np.zeros(len(X), np.int64)
+    for s in range(n, 0, -1):
+        v = np.zeros(len(X), np.int64)
+        for Z in (X, Y):
+            if s < Z.shape[1]:
+                v += np.einsum("ij,ij->i", Z[:, :-s].astype(np.int64), Z[:, s:].astype(np.int64))
+        key = key * base + ((-v if negate else v) + off)
+    return key
 
 
 def _solutions(n):
-    """[(C, D, {(sum A, sum B), ...})]: every C,D pair (C <= D in enumeration order) with an
-    A,B pair whose autocorrelation cancels it at every shift 1..n."""
-    S, T = _all_seqs(n), _all_seqs(n + 1)
-    aS, aT = _acf(S, n), _acf(T, n)
-    ia = np.triu_indices(len(T))
-    ab = aT[ia[0]] + aT[ia[1]]
-    sums = np.stack([T[ia[0]].sum(1), T[ia[1]].sum(1)], 1).astype(int)
-    want = {}
-    for k in range(len(ab)):
-        want.setdefault(ab[k].tobytes(), set()).add((int(sums[k, 0]), int(sums[k, 1])))
-    iu = np.triu_indices(len(S))
-    neg = -(aS[iu[0]] + aS[iu[1]])
+    """[(C, D, sum A, sum B)] over every base sequence quad of BS(n+1, n): each unordered C,D
+    pair whose summed autocorrelation is cancelled by some unordered A,B pair, with the signed
+    sums of every such A,B."""
+    S, T = _seqs(n), _seqs(n + 1)
+    i, j = np.triu_indices(len(T))
+    ab = _keys(T[i], T[j], n)
+    p, q = np.triu_indices(len(S))
+    cd = _keys(S[p], S[q], n, negate=True)
+    hit = np.isin(cd, ab)
+    wanted = np.isin(ab, cd[hit])
+    sums = {}
+    for k, a, b in zip(ab[wanted], T[i[wanted]].sum(1), T[j[wanted]].sum(1)):
+        sums.setdefault(int(k), set()).add((int(a), int(b)))
     out = []
-    for k in range(len(neg)):
-        hit = want.get(neg[k].tobytes())
-        if hit:
-            out.append((S[iu[0][k]].astype(int), S[iu[1][k]].astype(int), hit))
+    for k in np.flatnonzero(hit):
+        C, D = S[p[k]].astype(int), S[q[k]].astype(int)
+        for a, b in sorted(sums[int(cd[k])]):
+            out.append((C, D, a, b))
     return out
-
-
-def _canon64(C, D):
-    """The smallest form of (C, D) under negations, reversals, the swap and (where it maps
-    +-1 sequences to +-1 sequences) the quad switch: one representative per orbit."""
-    L = len(C)
-    C, D = tuple(int(x) for x in C), tuple(int(x) for x in D)
-    forms = {(C, D)}
-    qc = tuple((C[i] + D[i] + C[L - 1 - i] - D[L - 1 - i]) // 2 for i in range(L))
-    qd = tuple((C[i] + D[i] - C[L - 1 - i] + D[L - 1 - i]) // 2 for i in range(L))
-    if all(x in (1, -1) for x in qc + qd):
-        forms.add((qc, qd))
-    best = None
-    for c, d in forms:
-        for nc, nd, rc, rd, sw in itertools.product(range(2), repeat=5):
-            x = tuple(-v for v in c) if nc else c
-            y = tuple(-v for v in d) if nd else d
-            x = x[::-1] if rc else x
-            y = y[::-1] if rd else y
-            k = (y, x) if sw else (x, y)
-            best = k if best is None or k < best else best
-    return best
 
 
 @pytest.mark.parametrize("n", [6, 8, 10])
 def test_every_solution_orbit_is_kept(built_lib, n):
     from test_retention_cpu import _class_sums, _orbit
     from bs45_quantum_explorer_gb300.cells import cell_list
-    reps = {}
-    for C, D, abs_ in _solutions(n):
-        for a, b in abs_:
-            reps.setdefault((a, b, _canon64(C, D)), (C, D, a, b))
-    assert reps
-    lists = {}
+    sols = _solutions(n)
+    assert sols
+    lists, orbits = {}, {}
     checked = 0
-    for C, D, a, b in reps.values():
+    for C, D, a, b in sols:
         c, d = int(C.sum()), int(D.sum())
         for m6, q in itertools.product((0, 1), (0, 1, 2)):
             key = (a, b, c, d, m6, q)
@@ -93,7 +77,9 @@ def test_every_solution_orbit_is_kept(built_lib, n):
             own = (_class_sums(C, m), _class_sums(D, m))
             assert own in listed, (n, a, b, c, d, m6, "a true solution's cell is not listed")
             nvar = 64 if q and (c + d) % 4 == 0 else 32
-            orbit = _orbit(own[0], own[1], n, m, nvar)
+            if (own, m, nvar) not in orbits:
+                orbits[own, m, nvar] = _orbit(own[0], own[1], n, m, nvar)
+            orbit = orbits[own, m, nvar]
             assert any(listed.get(cell, 0) for cell in orbit), (n, a, b, c, d, m6, q, own)
             checked += 1
-    assert checked == 6 * len(reps)
+    assert checked == 6 * len(sols)
