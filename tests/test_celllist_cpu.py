@@ -238,3 +238,17 @@ def test_ab_rows_match_the_rule_at_production_n(built_lib, n, sig):
     for j in range(len(sub)):
         got = [tuple(int(x) for x in r) for r in rows[row_off[j]:row_off[j] + nrows[j]]]
         assert got == want[j], (n, sig, j)
+
+
+def test_lane_binary_qprune_audit_files_match_reference(built_lib):
+    """WZ_FH_QPRUNE_DUMP: the lane binary writes the same audit files as the reference (the
+    raw index of every cell the Q-closure prune removes, and one certificate per dead orbit;
+    tests/golden/qprune_dump_golden.json, from make_qprune_dump_golden.py), byte for byte."""
+    from make_qprune_dump_golden import record
+    from bs45_quantum_explorer_gb300.build import build_host
+    exe = build_host()
+    cases = json.load(open(os.path.join(HERE, "golden", "qprune_dump_golden.json")))
+    assert len(cases) >= 8 and all(c["files"]["dump"][1] > 0 for c in cases)
+    for c in cases:
+        rc, files = record(exe, c["n"], tuple(c["sig"]))
+        assert (rc, files) == (c["rc"], c["files"]), (c["n"], c["sig"])
