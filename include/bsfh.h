@@ -194,8 +194,9 @@ typedef struct { long long nodes, leaves, ok; } bs_cell_stats;
  * representative under canon; always 1 without). Nothing is printed. Returns BS_ERR_CAP
  * (with *ncells set) when cap is too small, 2 where the reference refuses (truncated list,
  * duplicate keys). digest (may be NULL) receives up to 40 bytes, "" unless prof_order 3.
- * A call that returns BS_ERR_CAP keeps the list it built (one list, process-wide), so the
- * same call repeated with a large enough buffer copies it instead of building it again. */
+ * A call that returns BS_ERR_CAP keeps the list it built (one list, process-wide, until the
+ * next bs_cell_list call), so the same call repeated with a large enough buffer copies it
+ * instead of building it again. */
 typedef struct {
   int32_t m6;           /* WZ_FH_M6 (the lane's default is n >= 36) */
   int32_t thm211b;      /* WZ_THM211B (forced at n >= 36) */
