@@ -109,3 +109,16 @@ def test_lane_host_logic_checkpoint_resume_matches_reference(oracle):
             assert first == (c["rc"], c["semantic"], c["ckpt"]), ctx
             assert second == (c["rc2"], c["semantic2"], c["ckpt2"]), ctx
             assert dump == (c["dump_sha256"], c["dump_len"]), ctx
+
+
+def test_lane_host_logic_internal_error_exit_matches_reference(oracle):
+    """WZ_FH_TEST_INTERNAL_ERROR (tests/golden/internal_error_golden.json): the first completion
+    is reported as failing the NPAF check, and the binary prints the reference's
+    FH_INTERNAL_ERROR and RESULT lines, exits 5 and leaves the same checkpoint file."""
+    from make_internal_error_golden import record
+    exe = _hostcheck_binary()
+    cases = json.load(open(os.path.join(HERE, "golden", "internal_error_golden.json")))
+    assert len(cases) >= 6 and all(c["rc"] == 5 for c in cases)
+    for c in cases:
+        rc, lines, files = record(exe, c["n"], tuple(c["sig"]), c["settings"])
+        assert (rc, lines, files) == (c["rc"], c["lines"], c["files"]), (c["n"], c["sig"], c["settings"])
