@@ -122,3 +122,28 @@ def test_lane_host_logic_internal_error_exit_matches_reference(oracle):
     for c in cases:
         rc, lines, files = record(exe, c["n"], tuple(c["sig"]), c["settings"])
         assert (rc, lines, files) == (c["rc"], c["lines"], c["files"]), (c["n"], c["sig"], c["settings"])
+
+
+def test_lane_host_logic_other_knobs_match_reference(oracle):
+    """The knobs lane_golden.json leaves at their defaults (tests/golden/lane_knobs_golden.json:
+    MAX_CAND, CELL_ORDER=0, AB_PROF off or capped, NO_CANON, a shard of a skip/end range, the
+    production list settings, buffered mod-3 cells, HALL_FAST=0, a score gate) and a resume
+    with WZ_FH_RESUME=0."""
+    from make_lane_golden import semantic
+    exe = _hostcheck_binary()
+    cases = json.load(open(os.path.join(HERE, "golden", "lane_knobs_golden.json")))
+    runs = [c for c in cases if not c.get("resume")]
+    assert len(runs) >= 200
+    _replay(exe, runs)
+    with tempfile.TemporaryDirectory() as tmp:
+        for c in [c for c in cases if c.get("resume")]:
+            ck = tempfile.mkdtemp(dir=tmp)
+            rc1, out1, _, _ = _run(exe, c["n"], c["sig"], c["settings"], tmp, ck)
+            files = sorted(os.listdir(ck))
+            ckpt1 = open(os.path.join(ck, files[0])).read() if files else ""
+            rc2, out2, dh, dl = _run(exe, c["n"], c["sig"], c["settings2"], tmp, ck)
+            ckpt2 = open(os.path.join(ck, files[0])).read() if files else ""
+            ctx = (c["n"], c["sig"], c["settings"], c["settings2"])
+            assert (rc1, semantic(out1), ckpt1) == (c["rc"], c["semantic"], c["ckpt"]), ctx
+            assert (rc2, semantic(out2), ckpt2) == (c["rc2"], c["semantic2"], c["ckpt2"]), ctx
+            assert (dh, dl) == (c["dump_sha256"], c["dump_len"]), ctx
