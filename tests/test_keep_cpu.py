@@ -32,7 +32,13 @@ def test_keep_matches_reference_drain(built_lib, oracle):
         surv, _, _ = oracle.cd_stream(n, list(c.tx[:m]), list(c.ty[:m]), m=m, pinX=bool(c.pinX),
                                       pinY=bool(c.pinY))
         assert 256 <= len(surv) <= st["WZ_FH_BUF_CAP"]
-        score = np.array([oracle.flat_score(x[0], x[1]) for x in surv])
+        # flat scores of every survivor at once (sum over s of |N_C(s) + N_D(s)|), checked
+        # against the oracle's flat_score on the first 512
+        X = surv.astype(np.int64)
+        score = np.zeros(len(surv), np.int64)
+        for s in range(1, n):
+            score += np.abs((X[:, 0, :-s] * X[:, 0, s:]).sum(1) + (X[:, 1, :-s] * X[:, 1, s:]).sum(1))
+        assert all(score[i] == oracle.flat_score(surv[i][0], surv[i][1]) for i in range(512))
         order = np.argsort(score, kind="stable")[:st["WZ_FH_DRAIN_TOP"]]
         got = []
         for ci, t in enumerate(order):
