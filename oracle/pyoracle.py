@@ -121,7 +121,7 @@ def cd_stream(n, tx, ty, m=6, pinX=False, pinY=False, rev=False, endpos=False, c
     L = n + 1 if ab_side else n
     # the walk writes at most `room` rows and returns the full count; a stream longer than
     # the first buffer is walked a second time into one of its size
-    room = min(cap, 1 << 18) if cap is not None else 1 << 18
+    room = min(cap, 1 << 18) if cap is not None else 1 << 16
     for _ in range(2):
         out = np.zeros(max(1, room) * 2 * L, np.int8)
         flags = np.zeros(max(1, room), np.uint8)

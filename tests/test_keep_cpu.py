@@ -30,7 +30,7 @@ def test_keep_matches_reference_drain(built_lib, oracle):
         rows, off, nr = ab_rows(n, sig, m, [c])
         r = rows[off[0]:off[0] + nr[0]]
         surv, _, _ = oracle.cd_stream(n, list(c.tx[:m]), list(c.ty[:m]), m=m, pinX=bool(c.pinX),
-                                      pinY=bool(c.pinY))
+                                      pinY=bool(c.pinY), cap=st["WZ_FH_BUF_CAP"])
         assert 256 <= len(surv) <= st["WZ_FH_BUF_CAP"]
         # flat scores of every survivor at once (sum over s of |N_C(s) + N_D(s)|), checked
         # against the oracle's flat_score on the first 512

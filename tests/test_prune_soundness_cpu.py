@@ -25,9 +25,10 @@ def _cells(lst):
 
 
 def _survivors(oracle, n, cell):
-    surv, _, _ = oracle.cd_stream(n, list(cell.tx[:6]), list(cell.ty[:6]), m=6,
-                                  pinX=bool(cell.pinX), pinY=bool(cell.pinY), endpos=True)
-    return len(surv)
+    """The cell's survivor count under ENDPOS (only the count is kept)."""
+    _, _, st = oracle.cd_stream(n, list(cell.tx[:6]), list(cell.ty[:6]), m=6, pinX=bool(cell.pinX),
+                                pinY=bool(cell.pinY), endpos=True, cap=1)
+    return st["ok"]
 
 
 @pytest.mark.parametrize("n", [7, 9, 13])
