@@ -8,9 +8,11 @@
 // links libbsfh.so and runs these calls on the GPU; this file is linked only into the test
 // build under tests/_build/.
 #include <algorithm>
+#include <atomic>
 #include <cstdint>
 #include <cstring>
 #include <numeric>
+#include <thread>
 #include <vector>
 
 #include "../../include/bsfh.h"
@@ -111,36 +113,52 @@ extern "C" int bs_flat_topk(bs_ctx *ctx, const uint64_t *words, long long nsurv,
   return BS_OK;
 }
 
-// fh_complete_ab per candidate by the oracle; in first-hit mode candidates after the first
-// hit are not run (verdict -1).
+// fh_complete_ab per candidate by the oracle, on all host threads in runs of candidates; in
+// first-hit mode the candidates after the first hit are reported as not run (verdict -1), as
+// the device reports them.
 extern "C" int bs_complete_ab_batch(bs_ctx *ctx, const bs_ab_cand *cands, long long ncand,
                                     const int8_t *rows, long long nrows_total, const bs_ab_opts *opt,
                                     int32_t *verdict, long long *nodes, int8_t *A, int8_t *B) {
   if (!ctx || !opt || ncand < 0 || (ncand > 0 && (!cands || !verdict || !nodes))) return BS_ERR_ARG;
   if (opt->a2 != 0 && opt->a2 != 2) return BS_ERR_ARG;
   const int n = ctx->n, n1 = n + 1;
-  std::vector<int8_t> C(n), D(n), a(n1), b(n1);
-  bool hit = false;
-  for (long long i = 0; i < ncand; i++) {
-    if ((hit && opt->first_hit) || ctx->stop) {
-      verdict[i] = -1;
-      nodes[i] = 0;
-      continue;
-    }
+  std::vector<int32_t> v((size_t)ncand, -1);
+  std::vector<long long> nd((size_t)ncand, 0);
+  std::vector<int8_t> ab((size_t)ncand * 2 * n1, 0);
+  auto one = [&](long long i) {
+    std::vector<int8_t> C(n), D(n);
     unpack(cands[i].c, n, C.data());
     unpack(cands[i].d, n, D.data());
     const bool ranged = cands[i].nrows > 0 && rows && cands[i].row_off + cands[i].nrows <= nrows_total;
-    std::fill(a.begin(), a.end(), 0);
-    std::fill(b.begin(), b.end(), 0);
-    long long nd = 0;
-    verdict[i] = or_complete_ab_a2(n, ctx->a, ctx->b, C.data(), D.data(), opt->budget, opt->outer_k,
-                                   opt->early, opt->canon, opt->m,
-                                   ranged ? rows + 16 * cands[i].row_off : nullptr,
-                                   ranged ? cands[i].nrows : 0, opt->a2, a.data(), b.data(), &nd);
-    nodes[i] = nd;
-    if (A) memcpy(A + i * n1, a.data(), (size_t)n1);
-    if (B) memcpy(B + i * n1, b.data(), (size_t)n1);
-    if (verdict[i] == 0) hit = true;
+    v[(size_t)i] = or_complete_ab_a2(n, ctx->a, ctx->b, C.data(), D.data(), opt->budget,
+                                     opt->outer_k, opt->early, opt->canon, opt->m,
+                                     ranged ? rows + 16 * cands[i].row_off : nullptr,
+                                     ranged ? cands[i].nrows : 0, opt->a2, &ab[(size_t)i * 2 * n1],
+                                     &ab[(size_t)i * 2 * n1 + n1], &nd[(size_t)i]);
+  };
+  const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+  long long done = 0;
+  bool hit = false;
+  while (done < ncand && !(hit && opt->first_hit) && !ctx->stop) {
+    const long long end = std::min(ncand, done + 64LL * hw);
+    std::atomic<long long> next(done);
+    std::vector<std::thread> th;
+    for (unsigned t = 0; t < hw; t++)
+      th.emplace_back([&] {
+        for (long long i; (i = next.fetch_add(1)) < end;) one(i);
+      });
+    for (auto &x : th) x.join();
+    for (long long i = done; i < end && !hit; i++) hit = v[(size_t)i] == 0;
+    done = end;
+  }
+  bool seen_hit = false;
+  for (long long i = 0; i < ncand; i++) {
+    const bool run = i < done && !(seen_hit && opt->first_hit);
+    verdict[i] = run ? v[(size_t)i] : -1;
+    nodes[i] = run ? nd[(size_t)i] : 0;
+    if (A) memcpy(A + i * n1, &ab[(size_t)i * 2 * n1], (size_t)n1);
+    if (B) memcpy(B + i * n1, &ab[(size_t)i * 2 * n1 + n1], (size_t)n1);
+    if (run && v[(size_t)i] == 0) seen_hit = true;
   }
   return ctx->stop ? BS_STOPPED : BS_OK;
 }

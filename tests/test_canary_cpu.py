@@ -4,13 +4,14 @@ against the reference's own run of it today (tests/golden/canary_n29_golden.json
 make_canary_golden.py: the summary, the quad, per raw cell the completions, verdicts and
 charged nodes, and the hit cell's drain sequence).
 
-The oracle rebuilds the run: the lane's cell list (bs_cell_list) and allowed rows, each live
-cell's stream up to the hit cell (their survivor counts sum to FIRSTHIT idx), every candidate
-of the cells before it completed at the lane's budget (completions, verdicts and node totals
-per cell), and the hit cell's survivors ordered by flat score (stable) and completed up to the
-first hit: the same drain ranks, verdicts and node counts, the hit's nodes_this_cand and the
-same quad. The same hit cell is then completed with the outer-lag tables and the early check
-off, the completer the archived fingerprint (nodes_this_cand = 81,320) was recorded with."""
+The oracle rebuilds the run's stream and its hit: the lane's cell list (bs_cell_list) and
+allowed rows, each live cell's stream up to the hit cell (their survivor counts sum to
+FIRSTHIT idx), and the hit cell's survivors ordered by flat score (stable) and completed up to
+the first hit: the same drain ranks, verdicts and node counts, the hit's nodes_this_cand and
+the same quad. Both recorded runs, every completion of the cells before the hit and the hit
+cell under the older completer (nodes_this_cand = 81,320) included, are replayed through the
+lane binary's host logic in test_lane_host_cpu.py, and through the GPU in
+test_z_canary_gpu.py."""
 import concurrent.futures as cf
 import json
 import os
@@ -98,42 +99,3 @@ def test_canary_n29_stream_counts_and_hit_cell(built_lib, oracle):
     A, B, C_, D = quad
     for s in range(1, n + 1):
         assert oracle.npaf_at(A, B, C_, D, s) == 0
-
-
-def test_canary_n29_cells_before_the_hit(built_lib, oracle):
-    """Every candidate of the live cells before the hit cell, completed at the lane's budget:
-    per cell the reference's completion count, verdict histogram and charged-node total."""
-    g = _golden()
-    run = g["runs"]["archived"]
-    n, sig, m, cells, kept, rows, off, nr, idx, hit_pi, hit_nodes = _setup(g)
-    before = [c for c in run["cells"] if c["pi"] != hit_pi]
-    assert before
-
-    got = []
-    for c in before:
-        pi = c["pi"]
-        surv = _stream(oracle, n, m, cells[pi])
-        out = _complete(oracle, n, sig, m, surv, rows[off[pi]:off[pi] + nr[pi]])
-        verdicts = np.bincount([int(o[0]) for o in out], minlength=5).tolist()
-        got.append(dict(pi=pi, completions=len(surv), nodes=sum(int(o[1]) for o in out),
-                        verdicts=verdicts))
-    assert got == before
-    summary = next(s for s in run["semantic"] if s.startswith("backtracks_entered="))
-    total = int(re.search(r"total_AB_nodes=(\d+)", summary).group(1))
-    assert sum(c["nodes"] for c in run["cells"]) == total
-
-
-def test_canary_n29_archived_fingerprint(built_lib, oracle):
-    """The hit cell with the outer-lag tables and the early check off reproduces the archived
-    nodes_this_cand (81,320), as the reference's own run with those settings does."""
-    g = _golden()
-    old = g["runs"]["hit_cell_outer0"]
-    n, sig, m, cells, kept, rows, off, nr, idx, hit_pi, hit_nodes = _setup(g)
-    hit = re.match(r"FIRSTHIT: idx=\d+ profile_rank=(\d+) nodes_this_cand=(\d+)",
-                   next(s for s in old["semantic"] if s.startswith("FIRSTHIT")))
-    assert int(hit.group(1)) == hit_pi
-    r = rows[off[hit_pi]:off[hit_pi] + nr[hit_pi]]
-    got, _ = _drain(oracle, n, sig, m, _stream(oracle, n, m, cells[hit_pi]), r, outer_k=0,
-                    early=False)
-    assert got == [[ci, v, nodes] for ci, pi, v, nodes in old["hit_cell"]]
-    assert got[-1][2] == int(hit.group(2))

@@ -147,3 +147,18 @@ def test_lane_host_logic_other_knobs_match_reference(oracle):
             assert (rc1, semantic(out1), ckpt1) == (c["rc"], c["semantic"], c["ckpt"]), ctx
             assert (rc2, semantic(out2), ckpt2) == (c["rc2"], c["semantic2"], c["ckpt2"]), ctx
             assert (dh, dl) == (c["dump_sha256"], c["dump_len"]), ctx
+
+
+def test_lane_host_logic_replays_the_n29_canary(oracle):
+    """The reference's archived n = 29 canary (tests/golden/canary_n29_golden.json) through the
+    binary's host logic: 588 raw cells, 584 of them without allowed rows, the hit cell's 4,349
+    completions in drain order, the summary and the quad; and the hit cell alone with the
+    completer the archived fingerprint was recorded with."""
+    from make_canary_golden import RUNS, record
+    exe = _hostcheck_binary()
+    g = json.load(open(os.path.join(HERE, "golden", "canary_n29_golden.json")))
+    assert set(g["runs"]) == set(RUNS)
+    with tempfile.TemporaryDirectory() as tmp:
+        for name, want in g["runs"].items():
+            got = record(exe, name, tmp, timeout=900)
+            assert got == want, name
