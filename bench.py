@@ -1022,6 +1022,11 @@ def main():
         }
         if not args.no_cpu_baseline:
             line["search"]["cpu_baseline"] = guarded(cpu_search_rate, os.cpu_count() or 1, cell42)
+        # the batch and its mask on the host for the CPU-baseline leg below, taken before the
+        # extra legs so that a failing leg cannot cost the headline its baseline
+        if not args.no_cpu_baseline:
+            words = d_words.cpu().numpy().view(np.uint64).reshape(-1, 2)
+            got = d_pass.cpu().numpy()
         # ---- the n = 36 first-hit lane (bounded) and the serving mix ----
         line["first_hit"] = guarded(run_first_hit, args.fh_seconds,
                                     with_cpu=not args.no_cpu_baseline)
@@ -1031,20 +1036,19 @@ def main():
                                   ref_seconds=0.0 if args.no_cpu_baseline else 45.0)
         line["completer_vs_reference_gpu_spike"] = guarded(run_spike)
         if not args.no_cpu_baseline:
-            ncpu = os.cpu_count() or 1
-            words = d_words.cpu().numpy().view(np.uint64).reshape(-1, 2)
-            rate, samp, thr, dt, kind, what, rmask = cpu_hall_rate(ncpu, words)
-            # parity of the device mask on every pair of the batch: against the oracle (the
-            # checker) and against the reference's own decisions from the timed leg
-            from bs45_quantum_explorer_gb300.workloads import unpack_pairs
-            omask = _oracle().hall_batch(N, unpack_pairs(words, N), nthreads=ncpu)
-            got = d_pass.cpu().numpy()
-            line["parity_sample"].update(
-                pairs=int(len(omask)), false_rejects=int(((omask == 1) & (got == 0)).sum()),
-                false_accepts=int(((omask == 0) & (got == 1)).sum()),
-                differs_from_reference_arm=int((rmask != got).sum()) if kind == "reference" else None)
-            line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": thr, "kind": kind,
-                                    "sample": what}
+            def cpu_leg():
+                ncpu = os.cpu_count() or 1
+                rate, samp, thr, dt, kind, what, rmask = cpu_hall_rate(ncpu, words)
+                # parity of the device mask on every pair of the batch: against the oracle (the
+                # checker) and against the reference's own decisions from the timed leg
+                from bs45_quantum_explorer_gb300.workloads import unpack_pairs
+                omask = _oracle().hall_batch(N, unpack_pairs(words, N), nthreads=ncpu)
+                line["parity_sample"].update(
+                    pairs=int(len(omask)), false_rejects=int(((omask == 1) & (got == 0)).sum()),
+                    false_accepts=int(((omask == 0) & (got == 1)).sum()),
+                    differs_from_reference_arm=int((rmask != got).sum()) if kind == "reference" else None)
+                return {"value": rate, "unit": UNIT, "cores": thr, "kind": kind, "sample": what}
+            line["cpu_baseline"] = guarded(cpu_leg)
     if rank == 0:
         print(json.dumps(line), flush=True)
     ctx.close()
